@@ -1,0 +1,295 @@
+#!/usr/bin/env python
+"""Benchmark: batched adaptive DOP853 manifold propagation (FP64).
+
+Workload (one "step" = one pass of the hot path over the whole batch):
+stable manifold of the Earth-Moon (mu = 0.012150585609624) L1 southern halo
+with Az = 0.2 (x0, T as corrected by the reference): 512 phases x 32
+displacements log-uniform in [1e-7, 1e-5] along the stable eigenvector =
+16384 trajectories, DOP853 rtol = atol = 1e-12, integrated backward to
+t = -8 with a terminal event on the plane x = 1 - mu (uneven lengths),
+persistent lane-refill kernel.  Seeds are synthetic (seeded), computed on
+the GPU from the orbit's STM grid.
+
+Metric: accepted trajectory-steps per second (attempted steps reported
+beside it).  `value`: kernel throughput with the seeds resident in HBM;
+`e2e`: the same through the public API (hiten_gb300.manifold) from pinned
+host seeds, H2D and D2H copies inside the timed region.
+
+`--impl reference`: the reference's algorithm on the host cores (the CPU
+oracle in numba-lowering mode, one trajectory per task, all host threads),
+on a bounded sample of the same seeds.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "FP64 trajectory-steps/sec (DOP853 manifold propagation, accepted steps)"
+UNIT = "traj-steps/s"
+FLOPS_PER_ATTEMPT_D6 = 1314.0  # algorithmic flops of one attempted DOP853 step, d = 6
+N_PHASE, N_DISP = 512, 32
+TF = 8.0
+
+
+def config(n_gpus):
+    return {"workload": "manifold.compute: L1 halo Az=0.2 stable manifold, 512 phases x 32 displacements "
+                        "(16384 trajectories), DOP853 rtol=atol=1e-12 to t=-8, terminal event x=1-mu",
+            "trajectories_per_gpu": N_PHASE * N_DISP, "dim": 6, "rtol": 1e-12,
+            "parallelism": f"replicas x{n_gpus}", "l2": "flushed between timed steps (256 MiB write)"}
+
+
+def make_seeds(device):
+    from hiten_gb300 import manifold as M
+    from hiten_gb300 import workloads as W
+    mu = W.MU_EM
+    times, PHI = M.stm_grid(W.HALO_L1_AZ02_X0, W.HALO_L1_AZ02_T, mu, steps=2000, forward=-1, device=device)
+    v = M.stable_eigvec(PHI[-1, :36].reshape(6, 6), stable=True)
+    phases, disp = W.manifold_grid(N_PHASE, N_DISP, seed=0)
+    return M.seeds(times, PHI, W.HALO_L1_AZ02_T, phases, disp, v, direction=1)
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        for line in self.f.read().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                               p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.f.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference(seeds, sample, threads, mode_name="NUMBA"):
+    """Time the CPU oracle (reference algorithm) on `sample` seeds with all threads."""
+    from oracle import hgo
+    from hiten_gb300 import workloads as W
+    mu = W.MU_EM
+    hgo.set_mode(getattr(hgo, "MODE_" + mode_name))
+    s = seeds[:sample]
+    t0 = time.perf_counter()
+    r = hgo.dop853_event_batch(s, 0.0, TF, mu, 0, 1 - mu, 0, 1, max_step=1e4, fwd=-1, flip=(0, 6),
+                               threads=threads)
+    dt = time.perf_counter() - t0
+    return float(r["n_accept"].sum()) / dt, dt, int(r["n_accept"].sum())
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from hiten_gb300 import manifold as M
+    from hiten_gb300 import workloads as W
+    from oracle import hgo
+    # the same seeds as the GPU arm: the orbit's STM grid from the oracle
+    # (DEVICE mode is bit-identical to the GPU kernel), host seeding code
+    hgo.set_mode(hgo.MODE_DEVICE)
+    T = W.HALO_L1_AZ02_T
+    PHI, _, _, _ = hgo.dop853_dense(W.identity_stm_state(W.HALO_L1_AZ02_X0)[0], np.linspace(0.0, T, 2000), W.MU_EM,
+                                    fwd=-1, flip=(36, 42))
+    v = M.stable_eigvec(PHI[-1, :36].reshape(6, 6), stable=True)
+    phases, disp = W.manifold_grid(N_PHASE, N_DISP, seed=0)
+    seeds = M.seeds(-np.linspace(0.0, T, 2000), PHI, T, phases, disp, v, direction=1)
+    threads = os.cpu_count() or 1
+    sample = min(len(seeds), 2048)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, dt, n = cpu_reference(np.roll(seeds, -i * 97, axis=0), sample, threads)
+        if i >= args.warmup:
+            vals.append((v, dt))
+    value = statistics.median(v for v, _ in vals)
+    ms = statistics.median(dt for _, dt in vals) * 1e3
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": config(args.gpus),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": f"{sample} of the 16384 manifold seeds per step (CPU oracle, numba "
+                                      f"lowering of powers, libm pow), one trajectory per task"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    from hiten_gb300 import _lib
+    from hiten_gb300 import manifold as M
+    from hiten_gb300 import propagate as P
+    from hiten_gb300 import workloads as W
+    mu = W.MU_EM
+
+    seeds = make_seeds(dev)
+    N = len(seeds)
+    seeds_dev = torch.as_tensor(seeds, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > L2
+    stream = torch.cuda.current_stream(dev)
+
+    def one_step():
+        return M.propagate_to_plane(seeds_dev, mu, tf=TF, forward=-1, device=dev)
+
+    for _ in range(max(args.warmup, 3)):
+        r = one_step()
+    torch.cuda.synchronize(dev)
+
+    # ---- device-resident timing (CUDA events on the launching stream)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    acc = att = 0
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        results = []
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            evs[i][0].record(stream)
+            r = one_step()
+            evs[i][1].record(stream)
+            results.append(r)
+        torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    clocks = clk.summary()
+    times_ms = [a.elapsed_time(b) for a, b in evs]
+    for r in results:
+        acc += int(r.n_accept.sum().item())
+        att += int(r.n_accept.sum().item() + r.n_reject.sum().item())
+    total_ms = sum(times_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = acc * world / (total_ms * 1e-3)
+    kernel_ms = total_ms / args.steps
+    flops = FLOPS_PER_ATTEMPT_D6 * att / args.steps
+    peak = P.fp64_peak_tflops(dev)
+
+    # ---- end to end through the public API (pinned host seeds, H2D + D2H inside)
+    host_seeds = torch.as_tensor(seeds).pin_memory()
+    e2e_acc = 0
+    h2d = host_seeds.numel() * 8
+    d2h = 0
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        r = M.propagate_to_plane(host_seeds, mu, tf=TF, forward=-1, device=dev)
+        y_end = r.y_end.cpu()
+        hit_y = r.hit_y.cpu()
+        hit_t = r.hit_t.cpu()
+        n_acc = r.n_accept.cpu()
+        e2e_acc += int(n_acc.sum())
+        d2h = (y_end.numel() + hit_y.numel() + hit_t.numel()) * 8 + n_acc.numel() * 4
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = e2e_acc * world / e2e_s
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = 2048
+        v, dt, n = cpu_reference(seeds, sample, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"first {sample} of the 16384 seeds ({n} accepted steps, {dt:.1f} s), CPU oracle in "
+                         f"numba-lowering mode, one trajectory per thread task"}
+
+    if rank == 0:
+        prof = os.path.join(HERE, "profiles", "traffic_dop853_manifold.json")
+        traffic = None
+        if os.path.exists(prof):
+            with open(prof) as f:
+                traffic = json.load(f).get("dram_bytes_per_launch")
+        achieved = flops / (kernel_ms * 1e-3) / 1e12
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(world),
+               "attempted_steps_per_s": att * world / (total_ms * 1e-3),
+               "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                            "frac": achieved / peak if peak else None, "traffic": traffic,
+                            "peak_source": "measured: DFMA throughput probe (hg_probe_fp64_peak) on this GPU; "
+                                           "MEASURED_PEAKS.json has no FP64 entry",
+                            "flops_per_attempted_step": FLOPS_PER_ATTEMPT_D6},
+               "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+               "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": args.steps,
+               "library": os.path.basename(_lib.load()._name)}
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,128 @@
+"""ctypes binding of ``libhitengpu.so`` (C ABI declared in include/hitengpu.h).
+
+There is no CPU fallback: importing the binding on a machine without the
+library or without a CUDA device raises, and every non-zero call status is
+turned into an exception.
+"""
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+HG_OK = 0
+HG_MAX_STEPS = 1
+HG_STEP_UNDERFLOW = 2
+HG_NONFINITE = 3
+HG_NEWTON_DIVERGED = 4
+HG_EVENT_NOT_FOUND = 5
+HG_ERR_ARGS = 10
+HG_ERR_CUDA = 11
+HG_ERR_NO_DEVICE = 12
+
+STATUS_NAMES = {0: "OK", 1: "MAX_STEPS", 2: "STEP_UNDERFLOW", 3: "NONFINITE", 4: "NEWTON_DIVERGED",
+                5: "EVENT_NOT_FOUND", 10: "ERR_ARGS", 11: "ERR_CUDA", 12: "ERR_NO_DEVICE"}
+
+EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg_propagate_fixed",
+            "hg_propagate_dop853", "hg_probe_fp64_peak")
+
+
+class HitenGpuError(RuntimeError):
+    """A hitengpu call returned a non-zero status."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"hitengpu error {code} ({STATUS_NAMES.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class hg_event(C.Structure):
+    _fields_ = [("index", C.c_int), ("offset", C.c_double), ("direction", C.c_int), ("max_hits", C.c_int),
+                ("xtol", C.c_double), ("gtol", C.c_double)]
+
+
+class hg_dop853_opts(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("max_step", C.c_double), ("min_step", C.c_double),
+                ("max_steps", C.c_longlong), ("fwd", C.c_int), ("flip_lo", C.c_int), ("flip_hi", C.c_int)]
+
+
+class hg_config(C.Structure):
+    _fields_ = [("device", C.c_int)]
+
+
+_P = C.c_void_p
+_lib = None
+_lock = threading.Lock()
+
+
+def load(build_if_missing=True):
+    """Load (building first if needed) the shared library; no fallback."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_missing and _build.stale():
+            _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError(f"hitengpu library missing at {path}; run hiten_gb300.build.build()")
+        L = C.CDLL(path)
+        L.hg_create.argtypes = [C.POINTER(hg_config), C.POINTER(_P)]
+        L.hg_create.restype = C.c_int
+        L.hg_destroy.argtypes = [_P]
+        L.hg_destroy.restype = C.c_int
+        L.hg_last_error_string.argtypes = [_P]
+        L.hg_last_error_string.restype = C.c_char_p
+        L.hg_version.restype = C.c_char_p
+        L.hg_propagate_fixed.argtypes = [_P, C.c_double, C.c_int, C.c_int, C.c_int, _P, C.c_longlong, _P, C.c_int,
+                                         C.c_int, _P, C.c_longlong, C.c_int, C.c_int, C.c_int, _P, _P]
+        L.hg_propagate_fixed.restype = C.c_int
+        L.hg_propagate_dop853.argtypes = [_P, C.c_double, C.c_int, C.c_int, _P, C.c_longlong, _P, _P, C.c_double,
+                                          C.c_double, C.POINTER(hg_dop853_opts), C.POINTER(hg_event), C.c_int,
+                                          C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]
+        L.hg_propagate_dop853.restype = C.c_int
+        L.hg_probe_fp64_peak.argtypes = [_P, C.POINTER(C.c_double)]
+        L.hg_probe_fp64_peak.restype = C.c_int
+        _lib = L
+        return L
+
+
+class Handle:
+    """Owns one ``hg_handle`` (per device)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = _P()
+        cfg = hg_config(int(device))
+        rc = self.lib.hg_create(C.byref(cfg), C.byref(h))
+        if rc != HG_OK:
+            raise HitenGpuError(rc, "hg_create failed (no CUDA device?)")
+        self.ptr = h
+        self.device = int(device)
+
+    def check(self, rc):
+        if rc != HG_OK:
+            msg = self.lib.hg_last_error_string(self.ptr)
+            raise HitenGpuError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.lib.hg_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_handles = {}
+
+
+def handle(device=0):
+    """Process-wide handle for a device (created on first use)."""
+    h = _handles.get(device)
+    if h is None:
+        h = Handle(device)
+        _handles[device] = h
+    return h

@@ -1,0 +1,231 @@
+// Correctly rounded power functions in FP64 for the propagation kernels.
+//
+// The reference evaluates x**1.5, x**2.5 (CR3BP Jacobian, dynamics/rtbp.py:117-122,
+// :232-235) and err**(-1/9), err**(0.4/9), err**(-1/8) (PI step-size
+// controller, integrators/utils.py:218-296) with libm pow.  These kernels
+// return the correctly rounded result (the exact power rounded once to
+// nearest), which is what a perfect libm returns; libm itself misrounds
+// about one call in a thousand.  The CPU oracle's DEVICE mode computes the same
+// values in quad precision.
+//
+// Methods (all error-free transforms are Dekker/Knuth two-product and
+// two-sum on fused multiply-add hardware):
+//   * hg_pow15 / hg_pow25: x*sqrt(x) in double-double.  s = RN(sqrt(x)),
+//     the residual x - s^2 is exact (fma), sqrt(x) = s + (x - s^2)/(2s) to
+//     ~2^-104, and x*s is split exactly; total error ~2^-100 before the
+//     final rounding.
+//   * hg_pow: exp(y * log(x)).  log by Tang's table method (F_j = 1+j/1024,
+//     log(1+v) series, v = (m-F)/F in double-double), exp by Tang's table
+//     method (2^(j/256) in double-double, Cody-Waite reduction with ln2/256
+//     split in three parts, Taylor polynomial for exp(r)-1).  Relative
+//     error before the final rounding is ~2^-83 for |y log x| <= 85.
+//
+// The header compiles as device code (nvcc) and as host C++ (g++ with
+// -ffp-contract=off) so the same arithmetic can be unit-tested on the CPU.
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "hg_crmath_tables.h"
+
+#if defined(__CUDACC__)
+#define HG_HD __host__ __device__ __forceinline__
+#else
+#define HG_HD static inline
+#endif
+
+#if defined(__CUDACC__)
+__device__ static const double hg_d_log_invf[HG_LOG_N] = HG_LOG_INVF_INIT;
+__device__ static const double hg_d_log_th[HG_LOG_N] = HG_LOG_TH_INIT;
+__device__ static const double hg_d_log_tl[HG_LOG_N] = HG_LOG_TL_INIT;
+__device__ static const double hg_d_exp_th[256] = HG_EXP_TH_INIT;
+__device__ static const double hg_d_exp_tl[256] = HG_EXP_TL_INIT;
+#endif
+static const double hg_h_log_invf[HG_LOG_N] = HG_LOG_INVF_INIT;
+static const double hg_h_log_th[HG_LOG_N] = HG_LOG_TH_INIT;
+static const double hg_h_log_tl[HG_LOG_N] = HG_LOG_TL_INIT;
+static const double hg_h_exp_th[256] = HG_EXP_TH_INIT;
+static const double hg_h_exp_tl[256] = HG_EXP_TL_INIT;
+
+#if defined(__CUDA_ARCH__)
+#define HG_TAB(name, i) __ldg(&hg_d_##name[i])
+#else
+#define HG_TAB(name, i) (hg_h_##name[i])
+#endif
+
+HG_HD uint64_t hg_bits(double x) {
+#if defined(__CUDA_ARCH__)
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  return b;
+#endif
+}
+
+HG_HD double hg_from_bits(uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)b);
+#else
+  double x;
+  memcpy(&x, &b, 8);
+  return x;
+#endif
+}
+
+HG_HD double hg_rsqrt_approx(double x) {
+#if defined(__CUDA_ARCH__)
+  return rsqrt(x);
+#else
+  return 1.0 / sqrt(x);
+#endif
+}
+
+HG_HD void hg_two_prod(double a, double b, double& p, double& e) {
+  p = a * b;
+  e = fma(a, b, -p);
+}
+
+HG_HD void hg_two_sum(double a, double b, double& s, double& e) {
+  s = a + b;
+  const double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+HG_HD void hg_fast_two_sum(double a, double b, double& s, double& e) {
+  s = a + b;
+  e = b - (s - a);
+}
+
+// x^1.5 as an unevaluated sum hi + lo (|lo| <= ~1.5 ulp(hi)), x > 0 normal.
+HG_HD void hg_pow15_dd(double x, double& hi, double& lo) {
+  const double s = sqrt(x);
+  const double rho = fma(-s, s, x);              // exact residual x - s^2
+  const double d = rho * (0.5 * hg_rsqrt_approx(x));  // sqrt(x) - s to ~2^-50 relative
+  hi = x * s;
+  lo = fma(x, s, -hi);
+  lo = fma(x, d, lo);
+}
+
+HG_HD double hg_pow15(double x) {
+  if (!(x > 0.0) || !(x < 1e300) || x < 1e-290) return pow(x, 1.5);
+  double hi, lo;
+  hg_pow15_dd(x, hi, lo);
+  return hi + lo;
+}
+
+// Both x^1.5 and x^2.5 (shared square root).
+HG_HD void hg_pow15_25(double x, double& p15, double& p25) {
+  if (!(x > 0.0) || !(x < 1e120) || x < 1e-120) {
+    p15 = pow(x, 1.5);
+    p25 = pow(x, 2.5);
+    return;
+  }
+  double hi, lo;
+  hg_pow15_dd(x, hi, lo);
+  p15 = hi + lo;
+  const double h2 = x * hi;
+  double l2 = fma(x, hi, -h2);
+  l2 = fma(x, lo, l2);
+  p25 = h2 + l2;
+}
+
+// log(x) as double-double, x > 0 finite.  Absolute error <~ 2^-85.
+HG_HD void hg_log_dd(double x, double& Lh, double& Ll) {
+  int e = 0;
+  if (x < 2.2250738585072014e-308) {
+    x *= 18014398509481984.0;  // 2^54
+    e = -54;
+  }
+  const uint64_t b = hg_bits(x);
+  e += (int)((b >> 52) & 0x7ff) - 1023;
+  double m = hg_from_bits((b & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull);
+  if (m > 1.4142135623730951) {
+    m *= 0.5;
+    e += 1;
+  }
+  const int j = (int)rint((m - 1.0) * 1024.0);
+  const double F = 1.0 + (double)j * 0.0009765625;
+  const double f = m - F;  // exact (Sterbenz)
+  const int ti = j - HG_LOG_JMIN;
+  const double invF = HG_TAB(log_invf, ti);
+  const double vh = f * invF;
+  const double vl = fma(-vh, F, f) * invF;  // v = vh + vl = f/F to ~2^-104
+  // log(1+v) = v - v^2/2 + v^3 * S(v)
+  double q, qe;
+  hg_two_prod(vh, vh, q, qe);
+  double S = -0.125;                         // -1/8
+  S = fma(S, vh, 0.14285714285714285);       // 1/7
+  S = fma(S, vh, -0.16666666666666666);      // -1/6
+  S = fma(S, vh, 0.2);                       // 1/5
+  S = fma(S, vh, -0.25);                     // -1/4
+  S = fma(S, vh, 0.3333333333333333);        // 1/3
+  // 1/3 etc. are rounded; their error (2^-55 relative) times v^3 (<2^-31)
+  // stays below 2^-86.
+  const double T = (q * vh) * S;
+  double A, Ae;
+  hg_two_sum(vh, -0.5 * q, A, Ae);
+  const double Pl = Ae + (vl + ((-0.5 * qe - vh * vl) + T));
+  // L = e*ln2 + log(F) + (A + Pl)
+  const double a = (double)e * HG_LN2_HI;  // exact (40-bit constant)
+  double s1, e1, s2, e2;
+  hg_two_sum(a, HG_TAB(log_th, ti), s1, e1);
+  hg_two_sum(s1, A, s2, e2);
+  const double low = ((e1 + e2) + (HG_TAB(log_tl, ti) + Pl)) + (double)e * HG_LN2_LO;
+  hg_fast_two_sum(s2, low, Lh, Ll);
+}
+
+// exp(th + tl), |th| <= 85, correctly rounded except with probability ~2^-29.
+HG_HD double hg_exp_dd(double th, double tl) {
+  if (th > 85.0) return 8.0e36;
+  if (th < -85.0) return 1.2e-37;
+  const double kd = rint(th * HG_INV_L256);
+  const int k = (int)kd;
+  const double r0 = th - kd * HG_L256_1;  // exact (Sterbenz, 38-bit constant)
+  double r1, r1e;
+  hg_two_sum(r0, -kd * HG_L256_2, r1, r1e);  // kd*L2 exact (38-bit constant)
+  double rh, rl;
+  hg_fast_two_sum(r1, (r1e + tl) - kd * HG_L256_3, rh, rl);
+  // exp(r) - 1 = r + r^2/2 + r^3 * S(r),  |r| <= ln2/512
+  double q, qe;
+  hg_two_prod(rh, rh, q, qe);
+  double S = 1.3888888888888889e-03;          // 1/720
+  S = fma(S, rh, 8.3333333333333332e-03);     // 1/120
+  S = fma(S, rh, 4.1666666666666664e-02);     // 1/24
+  S = fma(S, rh, 1.6666666666666666e-01);     // 1/6
+  const double T = (q * rh) * S;
+  double E, Ee;
+  hg_two_sum(rh, 0.5 * q, E, Ee);
+  const double El = Ee + (rl + ((0.5 * qe + rh * rl) + T));
+  // 2^(j/256) * (1 + E + El)
+  const int jj = k & 255;
+  const int sh = (k - jj) / 256;
+  const double Th = HG_TAB(exp_th, jj);
+  const double Tl = HG_TAB(exp_tl, jj);
+  double ph, pe;
+  hg_two_prod(Th, E, ph, pe);
+  const double cl = ((pe + Th * El) + Tl) + Tl * E;
+  double s, se;
+  hg_two_sum(Th, ph, s, se);
+  const double res = s + (se + cl);
+  // scale by 2^sh (|sh| <= 123: exact power of two, result stays normal)
+  return res * hg_from_bits((uint64_t)(sh + 1023) << 52);
+}
+
+// Correctly rounded x^y for x > 0 finite and |y log x| <= 85; other inputs
+// fall back to the platform pow (never reached by the step-size controller
+// for finite errors, where the result is clamped anyway).
+HG_HD double hg_pow(double x, double y) {
+  if (!(x > 0.0) || !(x < 1.0e308) || !(y == y)) return pow(x, y);
+  if (x == 1.0 || y == 0.0) return 1.0;
+  double Lh, Ll;
+  hg_log_dd(x, Lh, Ll);
+  double th, pe;
+  hg_two_prod(y, Lh, th, pe);
+  const double tl = fma(y, Ll, pe);
+  double Th, Tl;
+  hg_fast_two_sum(th, tl, Th, Tl);
+  return hg_exp_dd(Th, Tl);
+}

@@ -1,0 +1,862 @@
+// sm_103a kernels for the CR3BP propagation path (FP64 throughout).
+//
+// Execution model.  GB300 issues FP64 at a small fraction of its FP32 rate,
+// so the kernels are bound by the FP64 pipe, not by HBM: state and Runge-
+// Kutta stages live in registers, HBM sees only initial states and sampled
+// outputs.  Two lane layouts:
+//   * G = 1  (6-dim state): one lane owns one trajectory.
+//   * G = 7  (42-dim state + STM): a group of 7 lanes owns one trajectory;
+//            lane j < 6 holds STM column j (components 6r+j, r = 0..5), lane 6
+//            holds the state (components 36..41).  Column j of dPhi = F(x)Phi
+//            needs only the state, which the state lane broadcasts by shuffle
+//            at every stage; every lane of the group computes the Hessian of
+//            the effective potential from it.  Four groups fill lanes 0..27.
+// Group-wide decisions (accept/reject, events) use values that every lane of
+// the group computes identically, so control flow stays group-uniform.
+//
+// Arithmetic follows the reference's expression order exactly (no
+// contraction: the library is built with --fmad=false; fma appears only in
+// explicit error-free transforms and in the numpy-dot order), so results are
+// bit-identical to the CPU oracle's DEVICE mode.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+#include <utility>
+
+#include "hg_crmath.cuh"
+#include "hg_tableaux.h"
+#include "hitengpu.h"
+
+namespace hg {
+
+template <int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  [&]<int... I>(std::integer_sequence<int, I...>) {
+    (f(std::integral_constant<int, I>{}), ...);
+  }(std::make_integer_sequence<int, N>{});
+}
+
+// ---------------------------------------------------------------------------
+// Fixed-step tableaux (integrators/coefficients/{rk4,rk6,rk8}.py)
+// ---------------------------------------------------------------------------
+template <int ORDER>
+struct FixedTab;
+template <>
+struct FixedTab<4> {
+  static constexpr int S = 4;
+  __host__ __device__ static constexpr double a(int i, int j) { return HG_RK4_A[i][j]; }
+  __host__ __device__ static constexpr double b(int j) { return HG_RK4_B[j]; }
+};
+template <>
+struct FixedTab<6> {
+  static constexpr int S = 7;
+  __host__ __device__ static constexpr double a(int i, int j) { return HG_RK6_A[i][j]; }
+  __host__ __device__ static constexpr double b(int j) { return HG_RK6_B[j]; }
+};
+template <>
+struct FixedTab<8> {
+  static constexpr int S = 13;
+  __host__ __device__ static constexpr double a(int i, int j) { return HG_RK8_A[i][j]; }
+  __host__ __device__ static constexpr double b(int j) { return HG_RK8_B[j]; }
+};
+
+// DOP853 (integrators/coefficients/dop853.py): A[:12,:12], B = A[12,:12],
+// E5/E3 over 13 stages, extended rows 13..15 and D for dense output.
+struct DopTab {
+  static constexpr int S = HG_DOP_N_STAGES;       // 12
+  static constexpr int SE = HG_DOP_N_STAGES_EXT;  // 16
+  static constexpr int IP = HG_DOP_INTERP_POWER;  // 7
+  __host__ __device__ static constexpr double a(int i, int j) { return HG_DOP_A[i][j]; }
+  __host__ __device__ static constexpr double b(int j) { return HG_DOP_B[j]; }
+  __host__ __device__ static constexpr double e5(int j) { return HG_DOP_E5[j]; }
+  __host__ __device__ static constexpr double e3(int j) { return HG_DOP_E3[j]; }
+  __host__ __device__ static constexpr double d(int i, int j) { return HG_DOP_D[i][j]; }
+};
+
+// ---------------------------------------------------------------------------
+// Vector fields
+// ---------------------------------------------------------------------------
+
+// dynamics/rtbp.py:30-74 (_crtbp_accel), numba lowering of ** (x*x, x*(x*x)).
+__device__ __forceinline__ void rhs6(const double (&s)[6], double mu, double (&d)[6]) {
+  const double x = s[0], y = s[1], z = s[2], vx = s[3], vy = s[4];
+  const double omu = 1.0 - mu;
+  const double t1 = x + mu;
+  const double yy = y * y;
+  const double zz = z * z;
+  const double r1 = sqrt((t1 * t1 + yy) + zz);
+  const double t2 = x - omu;
+  const double r2 = sqrt((t2 * t2 + yy) + zz);
+  const double r1c = r1 * (r1 * r1);
+  const double r2c = r2 * (r2 * r2);
+  d[0] = vx;
+  d[1] = vy;
+  d[2] = s[5];
+  d[3] = ((2.0 * vy + x) - (omu * t1) / r1c) - (mu * ((x - 1.0) + mu)) / r2c;
+  d[4] = ((-2.0 * vx + y) - (omu * y) / r1c) - (mu * y) / r2c;
+  d[5] = ((-omu) * z) / r1c - (mu * z) / r2c;
+}
+
+// Hessian of the effective potential and the state accelerations,
+// dynamics/rtbp.py:76-165 and :215-238.
+struct Hess {
+  double xx, yy, zz, xy, xz, yz;
+  double ax, ay, az;
+};
+
+__device__ __forceinline__ Hess hessian42(double x, double y, double z, double vx, double vy, double mu) {
+  Hess H;
+  const double mu2 = 1.0 - mu;
+  const double t1 = x + mu;
+  const double t2 = x - mu2;
+  const double ys = y * y;
+  const double zs = z * z;
+  const double t1s = t1 * t1;
+  const double t2s = t2 * t2;
+  const double r2 = (t1s + ys) + zs;
+  const double R2 = (t2s + ys) + zs;
+  double r3, r5, R3, R5;
+  hg_pow15_25(r2, r3, r5);
+  hg_pow15_25(R2, R3, R5);
+  const double qa = mu2 / r5;
+  const double qb = mu / R5;
+  const double c3 = mu2 / r3 + mu / R3;
+  const double a3 = qa * 3.0;
+  const double b3 = qb * 3.0;
+  H.xx = ((1.0 + a3 * t1s) + b3 * t2s) - c3;
+  H.yy = ((1.0 + a3 * ys) + b3 * ys) - c3;
+  H.zz = (a3 * zs + b3 * zs) - c3;
+  const double sxy = (mu2 * t1) / r5 + (mu * t2) / R5;
+  H.xy = (3.0 * y) * sxy;
+  H.xz = (3.0 * z) * sxy;
+  H.yz = ((3.0 * y) * z) * (qa + qb);
+  H.ax = ((x - mu2 * (t1 / r3)) - mu * (t2 / R3)) + 2.0 * vy;
+  H.ay = ((y - mu2 * (y / r3)) - mu * (y / R3)) - 2.0 * vx;
+  H.az = (-mu2) * (z / r3) - mu * (z / R3);
+  return H;
+}
+
+// ---------------------------------------------------------------------------
+// Lane layout
+// ---------------------------------------------------------------------------
+struct Dir {
+  int neg_lo, neg_hi;  // component range whose derivative is negated (fwd=-1)
+};
+
+template <int G>
+struct Layout;
+
+template <>
+struct Layout<1> {
+  static constexpr int D = 6;
+  static constexpr int TPW = 32;  // trajectories per warp
+  int role;                       // always 6 ("state" lane of a 6-dim system)
+  __device__ __forceinline__ int comp(int r) const { return r; }
+  __device__ __forceinline__ void rhs(const double (&v)[6], double mu, const Dir& dir, double (&dv)[6]) const {
+    rhs6(v, mu, dv);
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+      if (r >= dir.neg_lo && r < dir.neg_hi) dv[r] = -dv[r];
+  }
+  template <typename T>
+  __device__ __forceinline__ T from_state(T v) const { return v; }
+};
+
+template <>
+struct Layout<7> {
+  static constexpr int D = 42;
+  static constexpr int TPW = 4;
+  int role;        // 0..5 STM column, 6 state
+  int base;        // first lane of the group
+  unsigned gmask;  // lanes of the group
+  __device__ __forceinline__ int comp(int r) const { return role < 6 ? 6 * r + role : 36 + r; }
+  template <typename T>
+  __device__ __forceinline__ T from_state(T v) const { return __shfl_sync(gmask, v, base + 6); }
+  __device__ __forceinline__ void rhs(const double (&v)[6], double mu, const Dir& dir, double (&dv)[6]) const {
+    const double x = from_state(v[0]);
+    const double y = from_state(v[1]);
+    const double z = from_state(v[2]);
+    const double vx = from_state(v[3]);
+    const double vy = from_state(v[4]);
+    const Hess H = hessian42(x, y, z, vx, vy, mu);
+    if (role < 6) {
+      // rows of F(x) @ Phi[:, j] (dynamics/rtbp.py:204-209), zero terms skipped
+      dv[0] = v[3];
+      dv[1] = v[4];
+      dv[2] = v[5];
+      dv[3] = ((H.xx * v[0] + H.xy * v[1]) + H.xz * v[2]) + 2.0 * v[4];
+      dv[4] = ((H.xy * v[0] + H.yy * v[1]) + H.yz * v[2]) + (-2.0) * v[3];
+      dv[5] = (H.xz * v[0] + H.yz * v[1]) + H.zz * v[2];
+    } else {
+      dv[0] = v[3];
+      dv[1] = v[4];
+      dv[2] = v[5];
+      dv[3] = H.ax;
+      dv[4] = H.ay;
+      dv[5] = H.az;
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      const int c = comp(r);
+      if (c >= dir.neg_lo && c < dir.neg_hi) dv[r] = -dv[r];
+    }
+  }
+};
+
+// numpy float64 dot order of the host the reference fixtures come from:
+// sequential fused accumulation for n < 16, a 32-element blocked sum plus a
+// fused tail for n = 42.  v is the full vector (identical in every lane).
+template <int D>
+__device__ __forceinline__ double np_dot_self(const double* v) {
+  if constexpr (D == 6) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s = fma(v[i], v[i], s);
+    return s;
+  } else {
+    double a[4][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int m = 0; m < 4; ++m) a[k][m] = v[8 * k + m] * v[8 * k + m] + v[8 * k + 4 + m] * v[8 * k + 4 + m];
+    double s[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) s[m] = ((a[0][m] + a[1][m]) + a[2][m]) + a[3][m];
+    double dot = (s[0] + s[2]) + (s[1] + s[3]);
+#pragma unroll
+    for (int i = 32; i < 42; ++i) dot = fma(v[i], v[i], dot);
+    return dot;
+  }
+}
+
+// Squared 2-norm of the full D-vector whose 6 components per lane are v, in
+// the numpy dot order above.  G = 1: the vector is the lane's own registers;
+// G = 7: the group assembles it in a 42-double shared-memory slot.
+template <int G>
+struct Gather;
+template <>
+struct Gather<1> {
+  __device__ __forceinline__ double dot(const Layout<1>&, const double (&v)[6]) const {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s = fma(v[i], v[i], s);
+    return s;
+  }
+};
+template <>
+struct Gather<7> {
+  double* slot;  // 42 doubles in shared memory
+  __device__ __forceinline__ double dot(const Layout<7>& L, const double (&v)[6]) const {
+    __syncwarp(L.gmask);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) slot[L.comp(r)] = v[r];
+    __syncwarp(L.gmask);
+    return np_dot_self<42>(slot);
+  }
+};
+
+// v[r] for a runtime r without dynamic register indexing.
+__device__ __forceinline__ double pick6(const double (&v)[6], int r) {
+  double o = v[0];
+#pragma unroll
+  for (int i = 1; i < 6; ++i) o = (r == i) ? v[i] : o;
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// Step-size helpers, integrators/utils.py:126-296
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double clamp_step(double h, double max_step, double min_step) {
+  if (h > max_step) h = max_step;
+  if (h < min_step) h = min_step;
+  return h;
+}
+__device__ __forceinline__ double adjust_step_to_endpoint(double t, double h, double t_end) {
+  if (t + h > t_end) return fabs(t_end - t);
+  return h;
+}
+__device__ __forceinline__ double select_initial_step(double d0, double d1, double min_step, double max_step) {
+  double h;
+  if (d0 < 1.0e-5 || d1 < 1.0e-5)
+    h = 1.0e-6;
+  else
+    h = (0.01 * d0) / d1;
+  if (h > max_step) h = max_step;
+  if (h < min_step) h = min_step;
+  return h;
+}
+// PI controller (order 8): beta = 1/9, alpha = 0.4*beta; reject exponent 1/8.
+// err_pow_alpha caches err_prev**alpha from the previous accepted step.
+__device__ __forceinline__ double pi_accept_factor(double err_norm, double err_prev, double& next_prev_pow) {
+  const double beta = 1.0 / (8.0 + 1.0);
+  const double alpha = 0.4 * beta;
+  double factor;
+  if (err_norm == 0.0) {
+    factor = 10.0;
+    next_prev_pow = 0.0;
+  } else {
+    double Lh, Ll;
+    hg_log_dd(err_norm, Lh, Ll);
+    double th, pe, Th, Tl;
+    hg_two_prod(-beta, Lh, th, pe);
+    hg_fast_two_sum(th, fma(-beta, Ll, pe), Th, Tl);
+    const double p1 = hg_exp_dd(Th, Tl);
+    hg_two_prod(alpha, Lh, th, pe);
+    hg_fast_two_sum(th, fma(alpha, Ll, pe), Th, Tl);
+    const double pa = hg_exp_dd(Th, Tl);
+    if (err_prev < 0.0)
+      factor = 0.9 * p1;
+    else
+      factor = (0.9 * p1) * next_prev_pow;
+    next_prev_pow = pa;
+  }
+  if (!(factor == factor)) factor = 10.0;
+  if (factor < 0.2) factor = 0.2;
+  if (factor > 10.0) factor = 10.0;
+  return factor;
+}
+__device__ __forceinline__ double pi_reject_factor(double err_norm) {
+  const double err_exp = 1.0 / 8.0;
+  double factor;
+  if (err_norm <= 0.0)
+    factor = 0.2;
+  else
+    factor = 0.9 * hg_pow(err_norm, -err_exp);
+  if (!(factor == factor)) factor = 0.2;
+  if (factor < 0.2) factor = 0.2;
+  if (factor > 10.0) factor = 10.0;
+  return factor;
+}
+
+// integrators/utils.py:13-68
+__device__ __forceinline__ bool event_crossed(double g_prev, double g_new, int dir) {
+  if (dir == 0) return (g_prev < 0.0 && g_new > 0.0) || (g_prev > 0.0 && g_new < 0.0) || (g_new == 0.0);
+  if (dir > 0) return (g_prev < 0.0 && g_new > 0.0) || (g_new == 0.0);
+  return (g_prev > 0.0 && g_new < 0.0) || (g_new == 0.0);
+}
+__device__ __forceinline__ bool crossed_direction(double g_left, double g_mid, int dir) {
+  if (dir == 0) return (g_left < 0.0 && g_mid > 0.0) || (g_left > 0.0 && g_mid < 0.0);
+  if (dir > 0) return (g_left < 0.0 && g_mid > 0.0);
+  return (g_left > 0.0 && g_mid < 0.0);
+}
+
+__device__ __forceinline__ double np_maximum(double a, double b) {
+  if (a != a || b != b) return a + b;  // NaN propagates
+  return a >= b ? a : b;
+}
+
+// ---------------------------------------------------------------------------
+// Fixed-step RK kernels, integrators/rk.py:154-215 and :531-588
+// ---------------------------------------------------------------------------
+template <int ORDER, int G>
+__device__ __forceinline__ void rk_fixed_step(const Layout<G>& L, const double (&y)[6], double h, double mu,
+                                              const Dir& dir, double (&yn)[6]) {
+  using T = FixedTab<ORDER>;
+  double k[T::S][6];
+  L.rhs(y, mu, dir, k[0]);
+  static_for<T::S - 1>([&](auto ic) {
+    constexpr int i = decltype(ic)::value + 1;
+    double ys[6];
+#pragma unroll
+    for (int d = 0; d < 6; ++d) ys[d] = y[d];
+    static_for<i>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      constexpr double a = T::a(i, j);
+      if constexpr (a != 0.0) {
+        const double c = h * a;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) ys[d] = ys[d] + c * k[j][d];
+      }
+    });
+    L.rhs(ys, mu, dir, k[i]);
+  });
+#pragma unroll
+  for (int d = 0; d < 6; ++d) yn[d] = y[d];
+  static_for<T::S>([&](auto jc) {
+    constexpr int j = decltype(jc)::value;
+    constexpr double b = T::b(j);
+    if constexpr (b != 0.0) {
+      const double c = h * b;
+#pragma unroll
+      for (int d = 0; d < 6; ++d) yn[d] = yn[d] + c * k[j][d];
+    }
+  });
+}
+
+struct FixedParams {
+  int N;
+  double mu;
+  Dir dir;
+  const double* y0;  // [D][ld_in]
+  long long ld_in;
+  const double* t_vals;  // [n]
+  int n;
+  int out_every;      // write rows 0, out_every, 2*out_every, ... (and nothing else)
+  double* out;        // [n_out][D][ld_out]
+  long long ld_out;
+  int* status;        // [N] or null
+};
+
+template <int ORDER, int G>
+__global__ void __launch_bounds__(128) fixed_rk_kernel(FixedParams p) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  Layout<G> L;
+  int traj;
+  if constexpr (G == 1) {
+    L.role = 6;
+    traj = warp * 32 + lane;
+  } else {
+    if (lane >= 28) return;
+    const int g = lane / 7;
+    L.role = lane % 7;
+    L.base = g * 7;
+    L.gmask = 0x7Fu << L.base;
+    traj = warp * 4 + g;
+  }
+  if (traj >= p.N) return;
+  double y[6];
+#pragma unroll
+  for (int r = 0; r < 6; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld_in + traj];
+  const int n_out = (p.n - 1) / p.out_every + 1;
+  (void)n_out;
+#pragma unroll
+  for (int r = 0; r < 6; ++r) p.out[(long long)L.comp(r) * p.ld_out + traj] = y[r];
+  const long long row = (long long)Layout<G>::D * p.ld_out;
+  bool finite = true;
+  for (int idx = 0; idx < p.n - 1; ++idx) {
+    const double h = p.t_vals[idx + 1] - p.t_vals[idx];
+    double yn[6];
+    rk_fixed_step<ORDER, G>(L, y, h, p.mu, p.dir, yn);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      y[r] = yn[r];
+      finite = finite && isfinite(yn[r]);
+    }
+    if ((idx + 1) % p.out_every == 0) {
+      double* o = p.out + (long long)((idx + 1) / p.out_every) * row;
+#pragma unroll
+      for (int r = 0; r < 6; ++r) o[(long long)L.comp(r) * p.ld_out + traj] = y[r];
+    }
+  }
+  if (p.status) {
+    if constexpr (G == 7) {
+      finite = __all_sync(L.gmask, finite);
+      if (L.role != 6) return;
+    }
+    p.status[traj] = finite ? HG_OK : HG_NONFINITE;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// DOP853, integrators/rk.py:1636-1708, :1790-2102, :2375-2549, :2678-2803
+// ---------------------------------------------------------------------------
+struct DopParams {
+  int N;
+  double mu;
+  Dir dir;
+  const double* y0;  // [D][ld]
+  long long ld;
+  const double* t0_arr;  // [N] or null -> t0
+  const double* tmax_arr;
+  double t0, tmax;
+  double rtol, atol, max_step, min_step;
+  long long max_steps;
+  // plane event g = y[ev_index] - ev_offset (ev_index < 0: none)
+  int ev_index;
+  double ev_offset;
+  int ev_dir;
+  int max_hits;
+  double xtol, gtol;
+  // dense samples at linspace(t0_i, tmax_i, m) (m >= 2); dense_last: only the
+  // final sample is evaluated and written (row 0 of y_out)
+  int m;
+  int dense_last;
+  double* y_out;  // [m or 1][D][ld]
+  // outputs
+  double* y_end;  // [D][ld]
+  double* t_end;  // [N]
+  double* hit_t;  // [max_hits][ld]
+  double* hit_y;  // [max_hits][D][ld]
+  int* n_hits;
+  int* n_accept;
+  int* n_reject;
+  int* status;
+  // persistent lane refill
+  int* next_traj;  // scratch counter (zeroed before launch) or null: static assignment
+  int stride;      // trajectories assigned in the first wave (grid lanes / G)
+};
+
+template <int G>
+struct DopLane {
+  // one attempted DOP853 step; k[0] = f(t, y) on entry; k[12] = f(t+h, y_high)
+  // on exit.
+  __device__ __forceinline__ static void step(const Layout<G>& L, const double (&y)[6], double h, double mu,
+                                              const Dir& dir, double (&k)[13][6], double (&yh)[6],
+                                              double (&e5)[6], double (&e3)[6]) {
+    using T = DopTab;
+    static_for<T::S - 1>([&](auto ic) {
+      constexpr int i = decltype(ic)::value + 1;
+      double ys[6];
+#pragma unroll
+      for (int d = 0; d < 6; ++d) ys[d] = y[d];
+      static_for<i>([&](auto jc) {
+        constexpr int j = decltype(jc)::value;
+        constexpr double a = T::a(i, j);
+        if constexpr (a != 0.0) {
+          const double c = h * a;
+#pragma unroll
+          for (int d = 0; d < 6; ++d) ys[d] = ys[d] + c * k[j][d];
+        }
+      });
+      L.rhs(ys, mu, dir, k[i]);
+    });
+#pragma unroll
+    for (int d = 0; d < 6; ++d) yh[d] = y[d];
+    static_for<T::S>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      constexpr double b = T::b(j);
+      if constexpr (b != 0.0) {
+        const double c = h * b;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) yh[d] = yh[d] + c * k[j][d];
+      }
+    });
+    L.rhs(yh, mu, dir, k[12]);
+#pragma unroll
+    for (int d = 0; d < 6; ++d) {
+      e5[d] = 0.0;
+      e3[d] = 0.0;
+    }
+    static_for<13>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      constexpr double c5 = T::e5(j);
+      constexpr double c3 = T::e3(j);
+      if constexpr (c5 != 0.0) {
+#pragma unroll
+        for (int d = 0; d < 6; ++d) e5[d] = e5[d] + c5 * k[j][d];
+      }
+      if constexpr (c3 != 0.0) {
+#pragma unroll
+        for (int d = 0; d < 6; ++d) e3[d] = e3[d] + c3 * k[j][d];
+      }
+    });
+#pragma unroll
+    for (int d = 0; d < 6; ++d) {
+      e5[d] = e5[d] * h;
+      e3[d] = e3[d] * h;
+    }
+  }
+
+  // _dop853_build_dense_cache: F[0..6][6] for this lane's components.
+  __device__ __forceinline__ static void dense_cache(const Layout<G>& L, const double (&y_old)[6],
+                                                     const double (&y_new)[6], double hseg, double mu,
+                                                     const Dir& dir, const double (&k)[13][6],
+                                                     double (&F)[7][6]) {
+    using T = DopTab;
+    double kx[3][6];
+    static_for<3>([&](auto sc) {
+      constexpr int srow = decltype(sc)::value + 13;
+      double ys[6];
+#pragma unroll
+      for (int d = 0; d < 6; ++d) {
+        double acc = 0.0;
+        static_for<srow>([&](auto rc) {
+          constexpr int r = decltype(rc)::value;
+          constexpr double a = T::a(srow, r);
+          if constexpr (a != 0.0) {
+            if constexpr (r < 13)
+              acc = acc + a * k[r][d];
+            else
+              acc = acc + a * kx[r - 13][d];
+          }
+        });
+        ys[d] = y_old[d] + hseg * acc;
+      }
+      L.rhs(ys, mu, dir, kx[srow - 13]);
+    });
+#pragma unroll
+    for (int d = 0; d < 6; ++d) {
+      const double dy = y_new[d] - y_old[d];
+      F[0][d] = dy;
+      F[1][d] = hseg * k[0][d] - dy;
+      F[2][d] = 2.0 * dy - hseg * (k[12][d] + k[0][d]);
+    }
+    static_for<4>([&](auto ic) {
+      constexpr int irem = decltype(ic)::value;
+#pragma unroll
+      for (int d = 0; d < 6; ++d) {
+        double acc = 0.0;
+        static_for<16>([&](auto rc) {
+          constexpr int r = decltype(rc)::value;
+          constexpr double c = T::d(irem, r);
+          if constexpr (c != 0.0) {
+            if constexpr (r < 13)
+              acc = acc + c * k[r][d];
+            else
+              acc = acc + c * kx[r - 13][d];
+          }
+        });
+        F[3 + irem][d] = hseg * acc;
+      }
+    });
+  }
+
+  __device__ __forceinline__ static double eval_row(double y_old, const double (&f)[7], double x) {
+    double v = 0.0;
+#pragma unroll
+    for (int i = 6; i >= 0; --i) {
+      v = v + f[i];
+      if ((6 - i) % 2 == 0)
+        v = v * x;
+      else
+        v = v * (1.0 - x);
+    }
+    return v + y_old;
+  }
+
+  __device__ __forceinline__ static double eval1(double y_old, const double (&F)[7][6], int d, double x) {
+    double v = 0.0;
+#pragma unroll
+    for (int i = 6; i >= 0; --i) {
+      v = v + F[i][d];
+      if ((6 - i) % 2 == 0)
+        v = v * x;
+      else
+        v = v * (1.0 - x);
+    }
+    return v + y_old;
+  }
+};
+
+template <int G>
+__global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
+  constexpr int D = Layout<G>::D;
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  Layout<G> L;
+  Gather<G> gat;
+  int traj;
+  __shared__ double sm_gather[(G == 7) ? 4 * 4 * 42 : 1];  // 4 warps x 4 groups
+  if constexpr (G == 1) {
+    L.role = 6;
+    traj = warp * 32 + lane;
+  } else {
+    if (lane >= 28) return;
+    const int g = lane / 7;
+    L.role = lane % 7;
+    L.base = g * 7;
+    L.gmask = 0x7Fu << L.base;
+    traj = warp * 4 + g;
+    gat.slot = sm_gather + (wib * 4 + g) * 42;
+  }
+  const bool has_event = p.ev_index >= 0 && p.max_hits > 0;
+  // event component: which lane/slot holds it
+  int ev_r = 0;
+  bool ev_mine = false;
+  if (has_event) {
+    if constexpr (G == 1) {
+      ev_r = p.ev_index;
+      ev_mine = true;
+    } else {
+      if (p.ev_index >= 36) {
+        ev_r = p.ev_index - 36;
+        ev_mine = (L.role == 6);
+      } else {
+        ev_r = p.ev_index / 6;
+        ev_mine = (L.role == p.ev_index % 6);
+      }
+    }
+  }
+  int ev_src = lane;
+  if constexpr (G == 7) ev_src = L.base + (p.ev_index >= 36 ? 6 : (p.ev_index % 6));
+  auto bcast_ev = [&](double v) -> double {
+    if constexpr (G == 1)
+      return v;
+    else
+      return __shfl_sync(L.gmask, v, ev_src);
+  };
+
+  while (traj < p.N) {
+    const double t0 = p.t0_arr ? p.t0_arr[traj] : p.t0;
+    const double tmax = p.tmax_arr ? p.tmax_arr[traj] : p.tmax;
+    double y[6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld + traj];
+    double k[13][6];
+    L.rhs(y, p.mu, p.dir, k[0]);
+    double g_prev = 0.0;
+    if (has_event) g_prev = bcast_ev(ev_mine ? (pick6(y, ev_r) - p.ev_offset) : 0.0);
+    double h;
+    {
+      double a[6], b[6];
+#pragma unroll
+      for (int d = 0; d < 6; ++d) {
+        const double scale0 = p.atol + p.rtol * fabs(y[d]);
+        a[d] = y[d] / scale0;
+        b[d] = k[0][d] / scale0;
+      }
+      const double sn = sqrt((double)D);
+      const double d0 = sqrt(gat.dot(L, a)) / sn;
+      const double d1 = sqrt(gat.dot(L, b)) / sn;
+      h = select_initial_step(d0, d1, p.min_step, p.max_step);
+    }
+    double t = t0;
+    double err_prev = -1.0;
+    double prev_pow = 0.0;
+    int acc = 0, rej = 0, hits = 0;
+    int status = HG_OK;
+    // dense sampling on linspace(t0, tmax, m)
+    int q_next = 0;
+    double step_ls = 0.0;
+    const bool dense = p.m >= 2;
+    if (dense) step_ls = (tmax - t0) / (double)(p.m - 1);
+    auto sample_t = [&](int q) -> double { return q == p.m - 1 ? tmax : (double)q * step_ls + t0; };
+    if (dense && p.dense_last) q_next = p.m - 1;
+
+    while ((t - tmax) * 1.0 < 0.0) {
+      if ((long long)(acc + rej) >= p.max_steps) {
+        status = HG_MAX_STEPS;
+        break;
+      }
+      h = clamp_step(h, p.max_step, p.min_step);
+      h = adjust_step_to_endpoint(t, h, tmax);
+      double yh[6], e5[6], e3[6];
+      DopLane<G>::step(L, y, h, p.mu, p.dir, k, yh, e5, e3);
+      double err_norm;
+      {
+        double s5[6], s3[6];
+#pragma unroll
+        for (int d = 0; d < 6; ++d) {
+          const double scale = p.atol + p.rtol * np_maximum(fabs(y[d]), fabs(yh[d]));
+          s5[d] = e5[d] / scale;
+          s3[d] = e3[d] / scale;
+        }
+        const double n5 = gat.dot(L, s5);
+        const double n3 = gat.dot(L, s3);
+        if (n5 == 0.0 && n3 == 0.0)
+          err_norm = 0.0;
+        else
+          err_norm = (fabs(h) * n5) / sqrt((n5 + 0.01 * n3) * (double)D);
+      }
+      if (err_norm <= 1.0) {
+        ++acc;
+        const double t_new = t + h;
+        bool stop = false;
+        // dense samples inside (t, t_new] (reference: searchsorted on nodes)
+        if (dense) {
+          const bool last = !((t_new - tmax) * 1.0 < 0.0);
+          if (q_next < p.m && (last || sample_t(q_next) < t_new)) {
+            const double hseg = t_new - t;
+            double F[7][6];
+            DopLane<G>::dense_cache(L, y, yh, hseg, p.mu, p.dir, k, F);
+            while (q_next < p.m && (last || sample_t(q_next) < t_new)) {
+              const double x = (sample_t(q_next) - t) / hseg;
+              double* o = p.y_out + (long long)(p.dense_last ? 0 : q_next) * D * p.ld;
+#pragma unroll
+              for (int d = 0; d < 6; ++d)
+                o[(long long)L.comp(d) * p.ld + traj] = DopLane<G>::eval1(y[d], F, d, x);
+              ++q_next;
+            }
+          }
+        }
+        if (has_event) {
+          const double g_new = bcast_ev(ev_mine ? (pick6(yh, ev_r) - p.ev_offset) : 0.0);
+          if (event_crossed(g_prev, g_new, p.ev_dir)) {
+            // _dop853_refine_in_step with the step size h
+            double F[7][6];
+            DopLane<G>::dense_cache(L, y, yh, h, p.mu, p.dir, k, F);
+            double fe[7];
+#pragma unroll
+            for (int i = 0; i < 7; ++i) fe[i] = pick6(F[i], ev_r);
+            const double ye = pick6(y, ev_r);
+            double a = 0.0, b = 1.0;
+            double g_left = g_prev;
+            double x_hit = -1.0;
+            for (int it = 0; it < 128; ++it) {
+              const double mid = 0.5 * (a + b);
+              const double g_mid = bcast_ev(ev_mine ? (DopLane<G>::eval_row(ye, fe, mid) - p.ev_offset) : 0.0);
+              if (fabs(g_mid) <= p.gtol) {
+                x_hit = mid;
+                break;
+              }
+              if (crossed_direction(g_left, g_mid, p.ev_dir)) {
+                b = mid;
+              } else {
+                a = mid;
+                g_left = g_mid;
+              }
+              if ((b - a) * fabs(h) <= p.xtol) break;
+            }
+            if (x_hit < 0.0) x_hit = b;
+            p.hit_t[(long long)hits * p.ld + traj] = t + x_hit * h;
+            double* o = p.hit_y + (long long)hits * D * p.ld;
+#pragma unroll
+            for (int d = 0; d < 6; ++d) o[(long long)L.comp(d) * p.ld + traj] = DopLane<G>::eval1(y[d], F, d, x_hit);
+            ++hits;
+            if (hits >= p.max_hits) stop = true;
+          }
+          g_prev = g_new;
+        }
+        t = t_new;
+        bool fin = true;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) {
+          y[d] = yh[d];
+          k[0][d] = k[12][d];
+          fin = fin && isfinite(yh[d]);
+        }
+        if (stop) break;
+        h = h * pi_accept_factor(err_norm, err_prev, prev_pow);
+        err_prev = err_norm;
+        if constexpr (G == 7) fin = __all_sync(L.gmask, fin);
+        if (!fin) {
+          status = HG_NONFINITE;
+          break;
+        }
+      } else {
+        ++rej;
+        h = h * pi_reject_factor(err_norm);
+        h = clamp_step(h, p.max_step, p.min_step);
+      }
+    }
+    // outputs
+    if (p.y_end) {
+#pragma unroll
+      for (int d = 0; d < 6; ++d) p.y_end[(long long)L.comp(d) * p.ld + traj] = y[d];
+    }
+    if (dense) {
+      // the reference's dense output falls back to the single stored node
+      // when no step was taken
+      while (q_next < p.m) {
+        double* o = p.y_out + (long long)(p.dense_last ? 0 : q_next) * D * p.ld;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) o[(long long)L.comp(d) * p.ld + traj] = y[d];
+        ++q_next;
+      }
+    }
+    if (L.role == 6) {
+      if (p.t_end) p.t_end[traj] = t;
+      if (p.n_hits) p.n_hits[traj] = hits;
+      if (p.n_accept) p.n_accept[traj] = acc;
+      if (p.n_reject) p.n_reject[traj] = rej;
+      if (p.status) p.status[traj] = status;
+    }
+    // next trajectory
+    if (p.next_traj == nullptr) break;
+    int nt = 0;
+    if constexpr (G == 1) {
+      nt = atomicAdd(p.next_traj, 1) + p.stride;
+    } else {
+      if (L.role == 0) nt = atomicAdd(p.next_traj, 1) + p.stride;
+      nt = __shfl_sync(L.gmask, nt, L.base);
+    }
+    traj = nt;
+  }
+}
+
+}  // namespace hg

@@ -1,0 +1,71 @@
+"""Manifold seeding and batched manifold propagation on the GPU.
+
+Follows algorithms/types/services/manifold.py: the STM grid of the periodic
+orbit (_compute_stm with steps=2000 and the manifold's direction, :215-245),
+the monodromy eigenvector (host numpy eig), seeds
+x0W = x(t_k) + (d / |(dir * Phi(t_k) v)[0:3]|) * dir * Phi(t_k) v at the grid
+time nearest to fraction * T (:470-573), then DOP853 propagation of all
+seeds at once with the flip of components 0:6 for backward time (:396-409).
+"""
+import numpy as np
+import torch
+
+from . import propagate as P
+from .workloads import identity_stm_state
+
+
+def stm_grid(x0, period, mu, steps=2000, forward=1, rtol=1e-12, atol=1e-12, device=None):
+    """(times, PHI) of _compute_stm: PHI (steps, 42) at linspace(0, T, steps), times signed."""
+    y0 = identity_stm_state(np.asarray(x0, dtype=np.float64))
+    r = P.propagate_dop853(y0, 0.0, float(period), mu, rtol=rtol, atol=atol, max_step=1e4, fwd=forward,
+                           flip=(36, 42), n_samples=int(steps), device=device)
+    PHI = r.samples[:, 0, :].cpu().numpy()
+    times = forward * np.linspace(0.0, float(period), int(steps))
+    return times, PHI
+
+
+def stable_eigvec(phi_T, stable=True):
+    """Real eigenvector of the monodromy for the smallest (stable) or largest
+    (unstable) real eigenvalue."""
+    w, V = np.linalg.eig(phi_T)
+    real = np.abs(w.imag) < 1e-10
+    idx = np.nonzero(real)[0]
+    mags = np.abs(w.real[idx])
+    k = idx[np.argmin(mags)] if stable else idx[np.argmax(mags)]
+    v = V[:, k].real
+    return v / np.linalg.norm(v)
+
+
+def seeds(times, PHI, period, fractions, displacements, eigvec, direction=1):
+    """Seeds for every (fraction, displacement) pair (fraction-major)."""
+    tt = np.abs(times)
+    xx = PHI[:, 36:42]
+    out = np.empty((len(fractions) * len(displacements), 6))
+    n = 0
+    for f in fractions:
+        k = int(np.argmin(np.abs(f * period - tt)))
+        phi = PHI[k, :36].reshape(6, 6)
+        man = direction * (phi @ eigvec)
+        mag = np.linalg.norm(man[0:3])
+        if mag < 1e-14:
+            mag = 1.0
+        for d in displacements:
+            x = xx[k] + (d / mag) * man
+            if abs(x[2]) < 1e-15:
+                x[2] = 0.0
+            if abs(x[5]) < 1e-15:
+                x[5] = 0.0
+            out[n] = x
+            n += 1
+    return out
+
+
+def propagate_to_plane(seeds_arr, mu, tf=8.0, forward=-1, plane_index=0, plane_offset=None, rtol=1e-12,
+                       atol=1e-12, max_hits=1, device=None):
+    """DOP853 from every seed to |t| = tf or the first crossing of
+    y[plane_index] = plane_offset (default x = 1 - mu), as a terminal event."""
+    if plane_offset is None:
+        plane_offset = 1.0 - mu
+    ev = P.EventSpec(index=plane_index, offset=float(plane_offset), direction=0, max_hits=max_hits)
+    return P.propagate_dop853(seeds_arr, 0.0, float(tf), mu, rtol=rtol, atol=atol, max_step=1e4, fwd=forward,
+                              flip=(0, 6), event=ev, device=device)

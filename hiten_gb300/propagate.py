@@ -1,0 +1,183 @@
+"""Batched trajectory propagation on the GPU (FP64), the array-level API
+under the reference-shaped drop-ins.
+
+Inputs may be numpy arrays or torch tensors of shape (N, dim); results are
+torch float64 CUDA tensors.  Device buffers are laid out structure-of-arrays
+([dim][N]) for the kernels and exposed to callers as (..., N, dim) views.
+Every call goes through ``libhitengpu.so``; there is no CPU path.
+"""
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+
+EPS = float(np.finfo(float).eps)
+
+
+def _device(device):
+    if device is None:
+        device = torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else None
+    if device is None:
+        raise RuntimeError("hiten_gb300 needs a CUDA device (no CPU fallback)")
+    return torch.device(device)
+
+
+def _to_soa(y, dim, device):
+    y = torch.as_tensor(y, dtype=torch.float64)
+    if y.ndim == 1:
+        y = y[None, :]
+    if y.shape[-1] != dim:
+        raise ValueError(f"Initial state dimension {y.shape[-1]} != system dimension {dim}")
+    return y.to(device).t().contiguous()  # (dim, N)
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream(device):
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _flip(dim, fwd, flip):
+    if flip is None:
+        return 0, dim
+    if isinstance(flip, slice):
+        lo = 0 if flip.start is None else int(flip.start)
+        hi = dim if flip.stop is None else int(flip.stop)
+        return lo, hi
+    lo, hi = flip
+    return int(lo), int(hi)
+
+
+def propagate_fixed(y0, t_vals, mu, order=8, out_every=1, fwd=1, flip=None, device=None, return_status=False):
+    """Fixed-step RK (order 4/6/8) over the nodes ``t_vals`` for N states.
+
+    Mirrors integrators/rk.py:531-588 (h_n = t_{n+1} - t_n).  Returns the
+    states at nodes 0, out_every, ... as a (n_out, N, dim) tensor.
+    """
+    dev = _device(device)
+    y0 = torch.as_tensor(y0, dtype=torch.float64)
+    dim = int(y0.shape[-1])
+    Y0 = _to_soa(y0, dim, dev)
+    N = Y0.shape[1]
+    tv = torch.as_tensor(np.ascontiguousarray(np.asarray(t_vals, dtype=np.float64))).to(dev)
+    n = int(tv.numel())
+    n_out = (n - 1) // int(out_every) + 1
+    out = torch.empty((n_out, dim, max(N, 1)), dtype=torch.float64, device=dev)
+    status = torch.zeros(max(N, 1), dtype=torch.int32, device=dev)
+    lo, hi = _flip(dim, fwd, flip)
+    H = _lib.handle(dev.index or 0)
+    with torch.cuda.device(dev):
+        H.check(H.lib.hg_propagate_fixed(H.ptr, float(mu), int(order), dim, N, _ptr(Y0), max(N, 1), _ptr(tv), n,
+                                         int(out_every), _ptr(out), max(N, 1), int(fwd), lo, hi, _ptr(status),
+                                         _stream(dev)))
+    res = out[:, :, :N].permute(0, 2, 1)
+    if return_status:
+        return res, status[:N]
+    return res
+
+
+@dataclass
+class EventSpec:
+    """Plane event g(y) = y[index] - offset (integrators/utils.py:13-123)."""
+
+    index: int
+    offset: float = 0.0
+    direction: int = 0
+    max_hits: int = 1
+    xtol: float = 1e-12
+    gtol: float = 1e-12
+
+
+@dataclass
+class Dop853Result:
+    y_end: torch.Tensor      # (N, dim) last accepted state
+    t_end: torch.Tensor      # (N,)
+    n_accept: torch.Tensor   # (N,)
+    n_reject: torch.Tensor
+    status: torch.Tensor
+    hit_t: torch.Tensor = None   # (N, max_hits)
+    hit_y: torch.Tensor = None   # (N, max_hits, dim)
+    n_hits: torch.Tensor = None  # (N,)
+    samples: torch.Tensor = None  # (n_samples or 1, N, dim)
+
+
+def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min_step=None,
+                     max_steps=100_000, fwd=1, flip=None, event=None, n_samples=0, sample_last_only=False,
+                     device=None, stream=None):
+    """Adaptive DOP853 for N states from t0 to tmax (scalars or (N,) arrays).
+
+    Mirrors integrators/rk.py:2375-2549 / :2678-2803 step for step.
+    ``event``: optional :class:`EventSpec`.  ``n_samples >= 2``: dense output
+    at linspace(t0_i, tmax_i, n_samples) (``sample_last_only``: final sample only).
+    """
+    dev = _device(device)
+    y0 = torch.as_tensor(y0, dtype=torch.float64)
+    dim = int(y0.shape[-1])
+    Y0 = _to_soa(y0, dim, dev)
+    N = Y0.shape[1]
+    ld = max(N, 1)
+    if min_step is None:
+        min_step = 10.0 * EPS
+    t0a = tmaxa = None
+    t0s = tmaxs = 0.0
+    if np.ndim(t0) == 0:
+        t0s = float(t0)
+    else:
+        t0a = torch.as_tensor(np.asarray(t0, dtype=np.float64)).to(dev).contiguous()
+    if np.ndim(tmax) == 0:
+        tmaxs = float(tmax)
+    else:
+        tmaxa = torch.as_tensor(np.asarray(tmax, dtype=np.float64)).to(dev).contiguous()
+    lo, hi = _flip(dim, fwd, flip)
+    opts = _lib.hg_dop853_opts(float(rtol), float(atol), float(max_step), float(min_step), int(max_steps),
+                               int(fwd), lo, hi)
+    y_end = torch.empty((dim, ld), dtype=torch.float64, device=dev)
+    t_end = torch.empty(ld, dtype=torch.float64, device=dev)
+    n_acc = torch.zeros(ld, dtype=torch.int32, device=dev)
+    n_rej = torch.zeros(ld, dtype=torch.int32, device=dev)
+    status = torch.zeros(ld, dtype=torch.int32, device=dev)
+    evp = None
+    hit_t = hit_y = n_hits = None
+    if event is not None:
+        mh = int(event.max_hits)
+        evp = _lib.hg_event(int(event.index), float(event.offset), int(event.direction), mh, float(event.xtol),
+                            float(event.gtol))
+        hit_t = torch.full((mh, ld), float("nan"), dtype=torch.float64, device=dev)
+        hit_y = torch.full((mh, dim, ld), float("nan"), dtype=torch.float64, device=dev)
+        n_hits = torch.zeros(ld, dtype=torch.int32, device=dev)
+    samples = None
+    if n_samples:
+        rows = 1 if sample_last_only else int(n_samples)
+        samples = torch.empty((rows, dim, ld), dtype=torch.float64, device=dev)
+    H = _lib.handle(dev.index or 0)
+    st = _stream(dev) if stream is None else C.c_void_p(stream)
+    with torch.cuda.device(dev):
+        H.check(H.lib.hg_propagate_dop853(H.ptr, float(mu), dim, N, _ptr(Y0), ld, _ptr(t0a), _ptr(tmaxa), t0s, tmaxs,
+                                          C.byref(opts), C.byref(evp) if evp is not None else None, int(n_samples),
+                                          1 if sample_last_only else 0, _ptr(samples), _ptr(y_end), _ptr(t_end),
+                                          _ptr(hit_t), _ptr(hit_y), _ptr(n_hits), _ptr(n_acc), _ptr(n_rej),
+                                          _ptr(status), st))
+    res = Dop853Result(y_end=y_end[:, :N].t(), t_end=t_end[:N], n_accept=n_acc[:N], n_reject=n_rej[:N],
+                       status=status[:N])
+    if event is not None:
+        res.hit_t = hit_t[:, :N].t()
+        res.hit_y = hit_y[:, :, :N].permute(2, 0, 1)
+        res.n_hits = n_hits[:N]
+    if samples is not None:
+        res.samples = samples[:, :, :N].permute(0, 2, 1)
+    return res
+
+
+def fp64_peak_tflops(device=None):
+    """Measured FP64 FMA throughput of the device (TFLOP/s)."""
+    dev = _device(device)
+    H = _lib.handle(dev.index or 0)
+    v = C.c_double(0.0)
+    with torch.cuda.device(dev):
+        H.check(H.lib.hg_probe_fp64_peak(H.ptr, C.byref(v)))
+    return v.value

@@ -1,0 +1,126 @@
+/*
+ * hitengpu -- C ABI of the GB300 (sm_103a) CR3BP trajectory-propagation path.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int status (HG_OK = 0) and is asynchronous on the given CUDA stream
+ * (`stream` is a cudaStream_t passed as void*; NULL = legacy default stream).
+ * All array arguments are caller-owned DEVICE memory laid out
+ * structure-of-arrays, component-major: element (component c, trajectory i)
+ * lives at base[c * ld + i] with ld >= N.  Component order follows the
+ * reference: 6-dim states are [x, y, z, vx, vy, vz]; 42-dim states are the
+ * row-major 6x6 STM Phi followed by the state (Phi[r][c] = y[6r + c],
+ * state = y[36:42]).  Arithmetic is IEEE FP64 in the reference's operation
+ * order (no contraction).  A handle is used by one host thread at a time;
+ * separate handles may share a device.  No call allocates memory after
+ * hg_create.
+ */
+#ifndef HITENGPU_H
+#define HITENGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (per call and per trajectory) */
+#define HG_OK 0
+#define HG_MAX_STEPS 1      /* adaptive step budget exhausted */
+#define HG_STEP_UNDERFLOW 2 /* reserved */
+#define HG_NONFINITE 3      /* state became NaN/Inf */
+#define HG_NEWTON_DIVERGED 4
+#define HG_EVENT_NOT_FOUND 5
+#define HG_ERR_ARGS 10      /* invalid argument (call status) */
+#define HG_ERR_CUDA 11      /* CUDA runtime error (call status) */
+#define HG_ERR_NO_DEVICE 12
+
+typedef struct hg_handle hg_handle;
+
+typedef struct {
+  int device;          /* CUDA device ordinal */
+} hg_config;
+
+/* Plane event g(y) = y[index] - offset.
+ * index < 0 disables the event.  direction: 0 any, +1 increasing,
+ * -1 decreasing (integrators/utils.py:13-68 semantics, endpoint zeros
+ * count).  max_hits = 1 stops at the first crossing (the reference's
+ * terminal event); max_hits > 1 records up to max_hits crossings without
+ * changing the step sequence.  xtol/gtol: bisection tolerances on the
+ * dense interpolant (reference defaults 1e-12). */
+typedef struct {
+  int index;
+  double offset;
+  int direction;
+  int max_hits;
+  double xtol;
+  double gtol;
+} hg_event;
+
+/* DOP853 controls (integrators/rk.py:786-838, dynamics/base.py:441-447).
+ * fwd = -1 integrates backward by negating the derivative components
+ * [flip_lo, flip_hi) (dynamics/base.py:272-310). */
+typedef struct {
+  double rtol;
+  double atol;
+  double max_step;
+  double min_step;
+  long long max_steps; /* attempted-step budget per trajectory */
+  int fwd;
+  int flip_lo;
+  int flip_hi;
+} hg_dop853_opts;
+
+/* Replaces: nothing (lifecycle).  Creates a handle bound to cfg->device. */
+int hg_create(const hg_config* cfg, hg_handle** out);
+int hg_destroy(hg_handle* h);
+/* Last error message recorded on this handle ("" if none). */
+const char* hg_last_error_string(hg_handle* h);
+/* Library version string. */
+const char* hg_version(void);
+
+/* Fixed-step explicit RK (order 4, 6 or 8) on dim 6 or 42, N trajectories,
+ * over the time nodes t_vals[0..n_nodes-1] (device array; h_n = t_{n+1} - t_n
+ * as the reference computes it).  Writes the states at nodes 0, out_every,
+ * 2*out_every, ... to y_out ([n_out][dim][ld_out], n_out = (n_nodes-1)/out_every + 1).
+ * status[i] (nullable): HG_OK or HG_NONFINITE.
+ * Replaces: integrators/rk.py:531-588 (_FixedStepRK._integrate_fixed_rk) as
+ * reached from dynamics/base.py:430-434 (_propagate_dynsys, method='fixed')
+ * and dynamics/rtbp.py:320-331 (_compute_stm). */
+int hg_propagate_fixed(hg_handle* h, double mu, int order, int dim, int N,
+                       const double* y0, long long ld_in,
+                       const double* t_vals, int n_nodes, int out_every,
+                       double* y_out, long long ld_out,
+                       int fwd, int flip_lo, int flip_hi,
+                       int* status, void* stream);
+
+/* Adaptive DOP853 on dim 6 or 42 from t0 to tmax (per trajectory arrays
+ * t0_arr/tmax_arr of length N, or NULL to use the scalars).
+ * Optional plane event ev (NULL = none).  Optional dense samples at
+ * linspace(t0_i, tmax_i, n_samples) into y_samples ([n_samples][dim][ld]);
+ * with sample_last_only != 0 only the final sample (t = tmax_i) is
+ * evaluated and written to row 0.  Outputs (all nullable): y_end [dim][ld]
+ * (last accepted state), t_end [N], hit_t [max_hits][ld],
+ * hit_y [max_hits][dim][ld], n_hits/n_accept/n_reject/status [N].
+ * Replaces: integrators/rk.py:2375-2549 (_DOP853._integrate_dop853) and
+ * :2678-2803 (_integrate_dop853_until_event with _dop853_refine_in_step
+ * :2005-2102), as reached from dynamics/base.py:435-453 and
+ * poincare/singlehit/backend.py:164-235. */
+int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N,
+                        const double* y0, long long ld,
+                        const double* t0_arr, const double* tmax_arr,
+                        double t0, double tmax,
+                        const hg_dop853_opts* opts, const hg_event* ev,
+                        int n_samples, int sample_last_only, double* y_samples,
+                        double* y_end, double* t_end,
+                        double* hit_t, double* hit_y, int* n_hits,
+                        int* n_accept, int* n_reject, int* status,
+                        void* stream);
+
+/* Measured FP64 fused-multiply-add throughput of this device (TFLOP/s,
+ * counting an FMA as 2 flops): runs a short dependent-chain-free DFMA loop
+ * on all SMs and times it with CUDA events.  Synchronous. */
+int hg_probe_fp64_peak(hg_handle* h, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HITENGPU_H */

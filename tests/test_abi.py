@@ -1,0 +1,44 @@
+"""The C-ABI library builds for sm_103a and exports every entry point that
+include/hitengpu.h declares (no GPU needed: nothing is called but hg_create,
+which must fail cleanly without a device)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import REPO
+
+
+def _declared():
+    src = open(os.path.join(REPO, "include", "hitengpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(hg_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    for n in ("hg_create", "hg_destroy", "hg_propagate_fixed", "hg_propagate_dop853", "hg_last_error_string"):
+        assert n in names
+
+
+def test_library_exports_all_declared_symbols():
+    from hiten_gb300 import build
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    for n in _declared():
+        assert hasattr(lib, n), f"{n} declared in hitengpu.h but not exported"
+
+
+def test_binding_covers_all_symbols():
+    from hiten_gb300 import _lib
+    assert sorted(_lib.EXPORTED) == _declared()
+
+
+def test_create_without_device_fails_cleanly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    from hiten_gb300 import _lib
+    with pytest.raises(_lib.HitenGpuError):
+        _lib.Handle(0)

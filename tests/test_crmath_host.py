@@ -1,0 +1,20 @@
+"""The correctly rounded power functions of the kernels (csrc/hg_crmath.cuh),
+compiled as host C++, agree with quad-precision pow rounded once."""
+import os
+import platform
+import subprocess
+
+from conftest import REPO
+
+
+def test_crmath_matches_quad_pow(tmp_path):
+    exe = str(tmp_path / "crmath_check")
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-builtin",
+           "-I" + os.path.join(REPO, "hiten_gb300", "csrc"), os.path.join(REPO, "tests", "native", "crmath_check.cpp"),
+           "-o", exe]
+    if platform.machine() not in ("aarch64", "arm64"):
+        cmd.append("-lquadmath")
+    subprocess.check_call(cmd)
+    out = subprocess.check_output([exe, "200000"]).decode().split()
+    n, bad15, bad25, badp = map(int, out)
+    assert n == 200000 and bad15 == 0 and bad25 == 0 and badp == 0
