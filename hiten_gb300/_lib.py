@@ -24,7 +24,7 @@ STATUS_NAMES = {0: "OK", 1: "MAX_STEPS", 2: "STEP_UNDERFLOW", 3: "NONFINITE", 4:
                 5: "EVENT_NOT_FOUND", 10: "ERR_ARGS", 11: "ERR_CUDA", 12: "ERR_NO_DEVICE"}
 
 EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg_propagate_fixed",
-            "hg_propagate_dop853", "hg_probe_fp64_peak")
+            "hg_propagate_dop853", "hg_probe_fp64_peak", "hg_propagate_dop853_noalloc")
 
 
 class HitenGpuError(RuntimeError):
@@ -80,6 +80,11 @@ def load(build_if_missing=True):
                                           C.c_double, C.POINTER(hg_dop853_opts), C.POINTER(hg_event), C.c_int,
                                           C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]
         L.hg_propagate_dop853.restype = C.c_int
+        L.hg_propagate_dop853_noalloc.argtypes = [C.c_double, C.c_int, C.c_int, _P, C.c_longlong, _P, _P,
+                                                  C.c_double, C.c_double, C.POINTER(hg_dop853_opts),
+                                                  C.POINTER(hg_event), C.c_int, C.c_int, _P, _P, _P, _P, _P, _P,
+                                                  _P, _P, _P, _P]
+        L.hg_propagate_dop853_noalloc.restype = C.c_int
         L.hg_probe_fp64_peak.argtypes = [_P, C.POINTER(C.c_double)]
         L.hg_probe_fp64_peak.restype = C.c_int
         _lib = L

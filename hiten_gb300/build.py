@@ -1,7 +1,7 @@
 """Compile the CUDA library ``hiten_gb300/libhitengpu.so`` for sm_103a.
 
-One translation unit (csrc/hg_api.cu including the kernel header), built
-in-tree with nvcc: ``-gencode arch=compute_103a,code=sm_103a``, C++20,
+Translation units csrc/hg_*.cu (each including the kernel header) are
+compiled in parallel and linked in-tree with nvcc: ``-gencode arch=compute_103a,code=sm_103a``, C++20,
 ``--fmad=false`` (no multiply-add contraction: every product and sum is
 rounded separately, as in the reference's numba kernels; fused operations
 appear only as explicit fma() calls).  The CUDA runtime is linked
@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libhitengpu.so")
-SOURCES = [os.path.join(CSRC, "hg_api.cu")]
+BUILD_DIR = os.path.join(HERE, "_build")
+SOURCES = [os.path.join(CSRC, "hg_api.cu"), os.path.join(CSRC, "hg_noalloc.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("hg_kernels.cuh", "hg_crmath.cuh", "hg_crmath_tables.h",
                                                   "hg_tableaux.h")] + [os.path.join(REPO, "include", "hitengpu.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
@@ -41,11 +42,18 @@ def build(force=False, verbose=False):
     if not force and not stale():
         return LIB
     tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc(), "-std=c++20", ARCH, "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-shared",
-           "-cudart", "static", "-I" + os.path.join(REPO, "include"), "-I" + CSRC, "-o", tmp] + SOURCES
+    flags = ["-std=c++20", ARCH, "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
+             "-I" + os.path.join(REPO, "include"), "-I" + CSRC]
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    subprocess.check_call(cmd)
+        flags.append("-Xptxas=-v")
+    objs = [os.path.join(BUILD_DIR, os.path.basename(s) + ".o") for s in SOURCES]
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    # one translation unit per process, compiled in parallel
+    procs = [subprocess.Popen([nvcc(), "-c"] + flags + ["-o", o, s]) for s, o in zip(SOURCES, objs)]
+    rcs = [p.wait() for p in procs]
+    if any(rcs):
+        raise RuntimeError(f"nvcc failed ({rcs})")
+    subprocess.check_call([nvcc(), ARCH, "-shared", "-cudart", "static", "-o", tmp] + objs)
     os.replace(tmp, LIB)
     return LIB
 

@@ -114,6 +114,31 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N,
                         int* n_accept, int* n_reject, int* status,
                         void* stream);
 
+/* No counterpart in the reference.  The DOP853 propagation of
+ * hg_propagate_dop853, for callers that cannot call cudaMalloc (an embedding
+ * runtime that owns all device memory, a loop that must not allocate after
+ * start-up, a plugin that may not create a handle).  It takes no handle and
+ * allocates nothing: the lane-refill counter, its only scratch, lives in a
+ * file-scope __device__ array of HG_NOALLOC_SCRATCH_BYTES per device, held
+ * until the process exits.  Runs on the current device.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress); make
+ * it before any stream capture.  The counter is cleared at the start of each
+ * call and shared by all calls: calls that overlap on the GPU race, so
+ * serialize them.  N > HG_NOALLOC_MAX_N (the 32-bit counter's safe range) is
+ * rejected with HG_ERR_ARGS; errors are reported by return code only. */
+#define HG_NOALLOC_SCRATCH_BYTES 256
+#define HG_NOALLOC_MAX_N (1 << 30)
+int hg_propagate_dop853_noalloc(double mu, int dim, int N,
+                                const double* y0, long long ld,
+                                const double* t0_arr, const double* tmax_arr,
+                                double t0, double tmax,
+                                const hg_dop853_opts* opts, const hg_event* ev,
+                                int n_samples, int sample_last_only, double* y_samples,
+                                double* y_end, double* t_end,
+                                double* hit_t, double* hit_y, int* n_hits,
+                                int* n_accept, int* n_reject, int* status,
+                                void* stream);
+
 /* Measured FP64 fused-multiply-add throughput of this device (TFLOP/s,
  * counting an FMA as 2 flops): runs a short dependent-chain-free DFMA loop
  * on all SMs and times it with CUDA events.  Synchronous. */
