@@ -49,7 +49,7 @@ hg::Dir make_dir(int dim, int fwd, int flip_lo, int flip_hi) {
   return d;
 }
 
-constexpr int kBlock = 128;
+constexpr int kBlock = 32;  // one warp per block: spreads small batches over all 152 SMs
 
 template <int ORDER, int G>
 int launch_fixed(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {

@@ -99,6 +99,29 @@ HG_HD void hg_fast_two_sum(double a, double b, double& s, double& e) {
   e = b - (s - a);
 }
 
+// Correctly rounded quotient a / b from the correctly rounded reciprocal
+// rb = RN(1/b) (Markstein's theorem, IBM J. Res. Dev. 34(1), 1990; see also
+// the Handbook of Floating-Point Arithmetic, sec. 4.7): q0 = RN(a*rb) is
+// within one ulp of a/b, the remainder r = a - b*q0 is exact with an fma,
+// and RN(q0 + r*rb) = RN(a/b).  Valid for finite, normal operands whose
+// quotient and remainder neither overflow nor underflow -- the CR3BP values
+// on this path (distances 1e-3..1e3) stay far from those limits.  One
+// reciprocal serves every quotient with the same denominator: 3 FP64
+// operations per quotient instead of a full division.
+HG_HD double hg_div_rn(double a, double b, double rb) {
+  const double q0 = a * rb;
+  const double r = fma(-b, q0, a);
+  return fma(r, rb, q0);
+}
+
+HG_HD double hg_rcp_rn(double b) {
+#if defined(__CUDA_ARCH__)
+  return __drcp_rn(b);
+#else
+  return 1.0 / b;
+#endif
+}
+
 // x^1.5 as an unevaluated sum hi + lo (|lo| <= ~1.5 ulp(hi)), x > 0 normal.
 HG_HD void hg_pow15_dd(double x, double& hi, double& lo) {
   const double s = sqrt(x);

@@ -81,6 +81,8 @@ struct DopTab {
 // ---------------------------------------------------------------------------
 
 // dynamics/rtbp.py:30-74 (_crtbp_accel), numba lowering of ** (x*x, x*(x*x)).
+// The six quotients share the two denominators r1^3 and r2^3: each is the
+// correctly rounded quotient (hg_div_rn), i.e. the same bits as `/`.
 __device__ __forceinline__ void rhs6(const double (&s)[6], double mu, double (&d)[6]) {
   const double x = s[0], y = s[1], z = s[2], vx = s[3], vy = s[4];
   const double omu = 1.0 - mu;
@@ -92,12 +94,14 @@ __device__ __forceinline__ void rhs6(const double (&s)[6], double mu, double (&d
   const double r2 = sqrt((t2 * t2 + yy) + zz);
   const double r1c = r1 * (r1 * r1);
   const double r2c = r2 * (r2 * r2);
+  const double i1 = hg_rcp_rn(r1c);
+  const double i2 = hg_rcp_rn(r2c);
   d[0] = vx;
   d[1] = vy;
   d[2] = s[5];
-  d[3] = ((2.0 * vy + x) - (omu * t1) / r1c) - (mu * ((x - 1.0) + mu)) / r2c;
-  d[4] = ((-2.0 * vx + y) - (omu * y) / r1c) - (mu * y) / r2c;
-  d[5] = ((-omu) * z) / r1c - (mu * z) / r2c;
+  d[3] = ((2.0 * vy + x) - hg_div_rn(omu * t1, r1c, i1)) - hg_div_rn(mu * ((x - 1.0) + mu), r2c, i2);
+  d[4] = ((-2.0 * vx + y) - hg_div_rn(omu * y, r1c, i1)) - hg_div_rn(mu * y, r2c, i2);
+  d[5] = hg_div_rn((-omu) * z, r1c, i1) - hg_div_rn(mu * z, r2c, i2);
 }
 
 // Hessian of the effective potential and the state accelerations,
@@ -121,21 +125,22 @@ __device__ __forceinline__ Hess hessian42(double x, double y, double z, double v
   double r3, r5, R3, R5;
   hg_pow15_25(r2, r3, r5);
   hg_pow15_25(R2, R3, R5);
-  const double qa = mu2 / r5;
-  const double qb = mu / R5;
-  const double c3 = mu2 / r3 + mu / R3;
+  const double i_r3 = hg_rcp_rn(r3), i_r5 = hg_rcp_rn(r5), i_R3 = hg_rcp_rn(R3), i_R5 = hg_rcp_rn(R5);
+  const double qa = hg_div_rn(mu2, r5, i_r5);
+  const double qb = hg_div_rn(mu, R5, i_R5);
+  const double c3 = hg_div_rn(mu2, r3, i_r3) + hg_div_rn(mu, R3, i_R3);
   const double a3 = qa * 3.0;
   const double b3 = qb * 3.0;
   H.xx = ((1.0 + a3 * t1s) + b3 * t2s) - c3;
   H.yy = ((1.0 + a3 * ys) + b3 * ys) - c3;
   H.zz = (a3 * zs + b3 * zs) - c3;
-  const double sxy = (mu2 * t1) / r5 + (mu * t2) / R5;
+  const double sxy = hg_div_rn(mu2 * t1, r5, i_r5) + hg_div_rn(mu * t2, R5, i_R5);
   H.xy = (3.0 * y) * sxy;
   H.xz = (3.0 * z) * sxy;
   H.yz = ((3.0 * y) * z) * (qa + qb);
-  H.ax = ((x - mu2 * (t1 / r3)) - mu * (t2 / R3)) + 2.0 * vy;
-  H.ay = ((y - mu2 * (y / r3)) - mu * (y / R3)) - 2.0 * vx;
-  H.az = (-mu2) * (z / r3) - mu * (z / R3);
+  H.ax = ((x - mu2 * hg_div_rn(t1, r3, i_r3)) - mu * hg_div_rn(t2, R3, i_R3)) + 2.0 * vy;
+  H.ay = ((y - mu2 * hg_div_rn(y, r3, i_r3)) - mu * hg_div_rn(y, R3, i_R3)) - 2.0 * vx;
+  H.az = (-mu2) * hg_div_rn(z, r3, i_r3) - mu * hg_div_rn(z, R3, i_R3);
   return H;
 }
 
@@ -343,9 +348,18 @@ __device__ __forceinline__ bool crossed_direction(double g_left, double g_mid, i
   return (g_left > 0.0 && g_mid < 0.0);
 }
 
-__device__ __forceinline__ double np_maximum(double a, double b) {
-  if (a != a || b != b) return a + b;  // NaN propagates
-  return a >= b ? a : b;
+// numpy.maximum(|a|, |b|) on the integer pipe: the bit patterns of
+// non-negative doubles order like unsigned integers, and a NaN pattern
+// compares above +inf, so NaN propagates as numpy's maximum does.
+__device__ __forceinline__ double np_maximum_abs(double a, double b) {
+  const unsigned long long ua = (unsigned long long)__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFull;
+  const unsigned long long ub = (unsigned long long)__double_as_longlong(b) & 0x7FFFFFFFFFFFFFFFull;
+  return __longlong_as_double((long long)(ua > ub ? ua : ub));
+}
+
+// isfinite on the integer pipe (exponent field not all ones).
+__device__ __forceinline__ bool finite_bits(double a) {
+  return ((unsigned long long)__double_as_longlong(a) & 0x7FF0000000000000ull) != 0x7FF0000000000000ull;
 }
 
 // ---------------------------------------------------------------------------
@@ -434,7 +448,7 @@ __global__ void __launch_bounds__(128) fixed_rk_kernel(FixedParams p) {
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
       y[r] = yn[r];
-      finite = finite && isfinite(yn[r]);
+      finite = finite && finite_bits(yn[r]);
     }
     if ((idx + 1) % p.out_every == 0) {
       double* o = p.out + (long long)((idx + 1) / p.out_every) * row;
@@ -732,9 +746,10 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
         double s5[6], s3[6];
 #pragma unroll
         for (int d = 0; d < 6; ++d) {
-          const double scale = p.atol + p.rtol * np_maximum(fabs(y[d]), fabs(yh[d]));
-          s5[d] = e5[d] / scale;
-          s3[d] = e3[d] / scale;
+          const double scale = p.atol + p.rtol * np_maximum_abs(y[d], yh[d]);
+          const double is = hg_rcp_rn(scale);
+          s5[d] = hg_div_rn(e5[d], scale, is);
+          s3[d] = hg_div_rn(e3[d], scale, is);
         }
         const double n5 = gat.dot(L, s5);
         const double n3 = gat.dot(L, s3);
@@ -808,7 +823,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
         for (int d = 0; d < 6; ++d) {
           y[d] = yh[d];
           k[0][d] = k[12][d];
-          fin = fin && isfinite(yh[d]);
+          fin = fin && finite_bits(yh[d]);
         }
         if (stop) break;
         h = h * pi_accept_factor(err_norm, err_prev, prev_pow);

@@ -33,7 +33,7 @@
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr int kBlock = 128;
+constexpr int kBlock = 32;  // one warp per block: spreads small batches over all 152 SMs
 
 static __device__ __align__(256) int hg_noalloc_scratch[HG_NOALLOC_SCRATCH_BYTES / sizeof(int)];
 

@@ -1,0 +1,38 @@
+"""Batched halo correction on the GPU: bit-identical to the same Newton
+logic driven by the CPU oracle (DEVICE mode), and within 1e-10 of the
+reference's orbit.correct() (corrected states and periods)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle_backends import OracleShootingBackend
+from hiten_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gpu_corrector_matches_oracle_bitexact(gpu, oracle):
+    from hiten_gb300 import corrector, halo
+    mu = W.MU_EM
+    pt, az, zen = W.halo_guess_params(24, seed=3)
+    guesses = np.concatenate([halo.third_order_guess(mu, int(p), a, z) for p, a, z in zip(pt, az, zen)])
+    res = corrector.correct_halo(guesses, mu)
+    ref = corrector.correct_halo(guesses, mu, backend=OracleShootingBackend(oracle, mu, oracle.MODE_DEVICE))
+    oracle.set_mode(oracle.MODE_PYTHON)
+    assert np.array_equal(res.status, ref.status)
+    assert np.array_equal(res.iterations, ref.iterations)
+    assert np.array_equal(res.x0, ref.x0)
+    assert np.array_equal(res.period, ref.period, equal_nan=True)
+    assert np.all(res.status == 0)
+
+
+def test_gpu_corrector_vs_reference_golden(gpu):
+    from hiten_gb300 import corrector
+    h = np.load(os.path.join(GOLDEN, "halo.npz"))
+    res = corrector.correct_halo(h["guess"], float(h["mu"]))
+    assert np.all(res.status == 0)
+    assert np.max(np.abs(res.x0 - h["x0"])) <= 1e-10
+    assert np.max(np.abs(res.period - h["period"])) <= 1e-10
+    assert np.array_equal(res.iterations, h["iterations"])
