@@ -24,7 +24,10 @@ STATUS_NAMES = {0: "OK", 1: "MAX_STEPS", 2: "STEP_UNDERFLOW", 3: "NONFINITE", 4:
                 5: "EVENT_NOT_FOUND", 10: "ERR_ARGS", 11: "ERR_CUDA", 12: "ERR_NO_DEVICE"}
 
 EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg_propagate_fixed",
-            "hg_propagate_dop853", "hg_probe_fp64_peak", "hg_propagate_dop853_noalloc")
+            "hg_propagate_dop853", "hg_probe_fp64_peak", "hg_propagate_dop853_noalloc", "hg_set_tuning",
+            "hg_get_tuning")
+HG_TUNE_BLOCK_THREADS = 1
+HG_TUNE_DOP853_LANES_D6 = 2
 
 
 class HitenGpuError(RuntimeError):
@@ -85,6 +88,10 @@ def load(build_if_missing=True):
                                                   C.POINTER(hg_event), C.c_int, C.c_int, _P, _P, _P, _P, _P, _P,
                                                   _P, _P, _P, _P]
         L.hg_propagate_dop853_noalloc.restype = C.c_int
+        L.hg_set_tuning.argtypes = [_P, C.c_int, C.c_int]
+        L.hg_set_tuning.restype = C.c_int
+        L.hg_get_tuning.argtypes = [_P, C.c_int, C.POINTER(C.c_int)]
+        L.hg_get_tuning.restype = C.c_int
         L.hg_probe_fp64_peak.argtypes = [_P, C.POINTER(C.c_double)]
         L.hg_probe_fp64_peak.restype = C.c_int
         _lib = L
@@ -108,6 +115,14 @@ class Handle:
         if rc != HG_OK:
             msg = self.lib.hg_last_error_string(self.ptr)
             raise HitenGpuError(rc, msg.decode() if msg else "")
+
+    def set_tuning(self, key, value):
+        self.check(self.lib.hg_set_tuning(self.ptr, int(key), int(value)))
+
+    def get_tuning(self, key):
+        v = C.c_int(0)
+        self.check(self.lib.hg_get_tuning(self.ptr, int(key), C.byref(v)))
+        return v.value
 
     def close(self):
         if getattr(self, "ptr", None):

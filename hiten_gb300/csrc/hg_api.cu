@@ -15,6 +15,8 @@ struct hg_handle {
   int device = 0;
   int sm_count = 0;
   int* counters = nullptr;  // scratch: lane-refill counters
+  int block = 32;           // threads per block (32, 64 or 128)
+  int lanes_d6 = 0;         // lanes per 6-dim DOP853 trajectory: 0 auto, 1, 2
   char err[512] = {0};
 };
 
@@ -49,19 +51,20 @@ hg::Dir make_dir(int dim, int fwd, int flip_lo, int flip_hi) {
   return d;
 }
 
-constexpr int kBlock = 32;  // one warp per block: spreads small batches over all 152 SMs
+// Blocks default to one warp: small batches then spread over all SMs.
 
 template <int ORDER, int G>
 int launch_fixed(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
-  const int tpb = (kBlock / 32) * hg::Layout<G>::TPW;  // trajectories per block
+  const int tpb = (h->block / 32) * hg::Layout<G>::TPW;  // trajectories per block
   const int grid = (p.N + tpb - 1) / tpb;
-  if (grid > 0) hg::fixed_rk_kernel<ORDER, G><<<grid, kBlock, 0, s>>>(p);
+  if (grid > 0) hg::fixed_rk_kernel<ORDER, G><<<grid, h->block, 0, s>>>(p);
   return check_launch(h, "fixed_rk_kernel");
 }
 
 template <int G>
 int launch_dop853(hg_handle* h, hg::DopParams p, cudaStream_t s) {
   if (p.N <= 0) return HG_OK;
+  const int kBlock = h->block;
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hg::dop853_kernel<G>, kBlock, 0);
   if (e != cudaSuccess || per_sm < 1) per_sm = 1;
@@ -231,8 +234,39 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
   p.n_reject = n_reject;
   p.status = status;
   cudaStream_t s = (cudaStream_t)stream;
-  if (dim == 6) return launch_dop853<1>(h, p, s);
+  if (dim == 6) {
+    int lanes = h->lanes_d6;
+    // auto: pairs while two lanes per trajectory still fit one warp per SM
+    // sub-partition (shortest per-step latency), single lanes beyond
+    if (lanes == 0) lanes = (2LL * N <= 4LL * 32 * h->sm_count) ? 2 : 1;
+    if (lanes == 2) return launch_dop853<2>(h, p, s);
+    return launch_dop853<1>(h, p, s);
+  }
   return launch_dop853<7>(h, p, s);
+}
+
+int hg_set_tuning(hg_handle* h, int key, int value) {
+  if (!h) return HG_ERR_ARGS;
+  switch (key) {
+    case HG_TUNE_BLOCK_THREADS:
+      if (value != 32 && value != 64 && value != 128) return fail(h, HG_ERR_ARGS, "block must be 32, 64 or 128");
+      h->block = value;
+      return HG_OK;
+    case HG_TUNE_DOP853_LANES_D6:
+      if (value < 0 || value > 2) return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 1 or 2");
+      h->lanes_d6 = value;
+      return HG_OK;
+    default:
+      return fail(h, HG_ERR_ARGS, "unknown tuning key %d", key);
+  }
+}
+
+int hg_get_tuning(hg_handle* h, int key, int* value) {
+  if (!h || !value) return HG_ERR_ARGS;
+  if (key == HG_TUNE_BLOCK_THREADS) *value = h->block;
+  else if (key == HG_TUNE_DOP853_LANES_D6) *value = h->lanes_d6;
+  else return fail(h, HG_ERR_ARGS, "unknown tuning key %d", key);
+  return HG_OK;
 }
 
 int hg_probe_fp64_peak(hg_handle* h, double* tflops) {

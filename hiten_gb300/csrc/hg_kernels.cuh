@@ -157,7 +157,10 @@ struct Layout;
 template <>
 struct Layout<1> {
   static constexpr int D = 6;
+  static constexpr int NC = 6;    // components per lane
   static constexpr int TPW = 32;  // trajectories per warp
+  __device__ __forceinline__ int owner(int c) const { return 0; }
+  __device__ __forceinline__ int local(int c) const { return c; }
   int role;                       // always 6 ("state" lane of a 6-dim system)
   __device__ __forceinline__ int comp(int r) const { return r; }
   __device__ __forceinline__ void rhs(const double (&v)[6], double mu, const Dir& dir, double (&dv)[6]) const {
@@ -173,7 +176,10 @@ struct Layout<1> {
 template <>
 struct Layout<7> {
   static constexpr int D = 42;
+  static constexpr int NC = 6;
   static constexpr int TPW = 4;
+  __device__ __forceinline__ int owner(int c) const { return c >= 36 ? 6 : c % 6; }
+  __device__ __forceinline__ int local(int c) const { return c >= 36 ? c - 36 : c / 6; }
   int role;        // 0..5 STM column, 6 state
   int base;        // first lane of the group
   unsigned gmask;  // lanes of the group
@@ -207,6 +213,65 @@ struct Layout<7> {
     for (int r = 0; r < 6; ++r) {
       const int c = comp(r);
       if (c >= dir.neg_lo && c < dir.neg_hi) dv[r] = -dv[r];
+    }
+  }
+};
+
+// G = 2 (6-dim state, latency layout): a lane pair owns one trajectory;
+// role 0 holds the position (x, y, z), role 1 the velocity.  The right-hand
+// side splits by primary: role 0 evaluates the terms of the first primary,
+// role 1 those of the second, with one instruction stream and per-lane
+// constants, and the pair exchanges the three quotients.  Every operation
+// is the one rhs6 performs (x - (1-mu) == x + (-(1-mu)), x - 1 == x + (-1)),
+// so the result is bit-identical; the per-step FP64 critical path is about
+// half that of G = 1, at ~7% more total work.
+template <>
+struct Layout<2> {
+  static constexpr int D = 6;
+  static constexpr int NC = 3;
+  static constexpr int TPW = 16;
+  int role;        // 0 position, 1 velocity
+  int base;        // first lane of the pair
+  unsigned gmask;  // the pair
+  __device__ __forceinline__ int comp(int r) const { return 3 * role + r; }
+  __device__ __forceinline__ int owner(int c) const { return c / 3; }
+  __device__ __forceinline__ int local(int c) const { return c % 3; }
+  __device__ __forceinline__ void rhs(const double (&v)[3], double mu, const Dir& dir, double (&dv)[3]) const {
+    const bool r0 = role == 0;
+    const double o0 = __shfl_xor_sync(gmask, v[0], 1);
+    const double o1 = __shfl_xor_sync(gmask, v[1], 1);
+    const double o2 = __shfl_xor_sync(gmask, v[2], 1);
+    const double x = r0 ? v[0] : o0, y = r0 ? v[1] : o1, z = r0 ? v[2] : o2;
+    const double vx = r0 ? o0 : v[0], vy = r0 ? o1 : v[1], vz = r0 ? o2 : v[2];
+    const double omu = 1.0 - mu;
+    const double cb = r0 ? mu : -omu;   // x + cb = x + mu | x - (1 - mu)
+    const double a1 = r0 ? mu : -1.0;   // numerator of the x-term: (x + a1) + a2
+    const double a2 = r0 ? 0.0 : mu;
+    const double mb = r0 ? omu : mu;
+    const double mz = r0 ? -omu : mu;
+    const double t = x + cb;
+    const double yy = y * y;
+    const double zz = z * z;
+    const double r = sqrt((t * t + yy) + zz);
+    const double rc = r * (r * r);
+    const double ir = hg_rcp_rn(rc);
+    const double qx = hg_div_rn(mb * ((x + a1) + a2), rc, ir);
+    const double qy = hg_div_rn(mb * y, rc, ir);
+    const double qz = hg_div_rn(mz * z, rc, ir);
+    const double px = __shfl_xor_sync(gmask, qx, 1);
+    const double py = __shfl_xor_sync(gmask, qy, 1);
+    const double pz = __shfl_xor_sync(gmask, qz, 1);
+    // role 1 owns the accelerations: q1 = partner (first primary), q2 = own
+    const double ax = ((2.0 * vy + x) - px) - qx;
+    const double ay = ((-2.0 * vx + y) - py) - qy;
+    const double az = pz - qz;
+    dv[0] = r0 ? vx : ax;
+    dv[1] = r0 ? vy : ay;
+    dv[2] = r0 ? vz : az;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const int c = comp(i);
+      if (c >= dir.neg_lo && c < dir.neg_hi) dv[i] = -dv[i];
     }
   }
 };
@@ -263,11 +328,27 @@ struct Gather<7> {
   }
 };
 
+template <>
+struct Gather<2> {
+  // sequential fused accumulation over components 0..5: the position lane's
+  // partial sum seeds the velocity lane's
+  __device__ __forceinline__ double dot(const Layout<2>& L, const double (&v)[3]) const {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) s = fma(v[i], v[i], s);
+    s = __shfl_sync(L.gmask, s, L.base);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) s = fma(v[i], v[i], s);
+    return __shfl_sync(L.gmask, s, L.base + 1);
+  }
+};
+
 // v[r] for a runtime r without dynamic register indexing.
-__device__ __forceinline__ double pick6(const double (&v)[6], int r) {
+template <int NC>
+__device__ __forceinline__ double pick(const double (&v)[NC], int r) {
   double o = v[0];
 #pragma unroll
-  for (int i = 1; i < 6; ++i) o = (r == i) ? v[i] : o;
+  for (int i = 1; i < NC; ++i) o = (r == i) ? v[i] : o;
   return o;
 }
 
@@ -506,42 +587,43 @@ struct DopParams {
 
 template <int G>
 struct DopLane {
+  static constexpr int NC = Layout<G>::NC;
   // one attempted DOP853 step; k[0] = f(t, y) on entry; k[12] = f(t+h, y_high)
   // on exit.
-  __device__ __forceinline__ static void step(const Layout<G>& L, const double (&y)[6], double h, double mu,
-                                              const Dir& dir, double (&k)[13][6], double (&yh)[6],
-                                              double (&e5)[6], double (&e3)[6]) {
+  __device__ __forceinline__ static void step(const Layout<G>& L, const double (&y)[NC], double h, double mu,
+                                              const Dir& dir, double (&k)[13][NC], double (&yh)[NC],
+                                              double (&e5)[NC], double (&e3)[NC]) {
     using T = DopTab;
     static_for<T::S - 1>([&](auto ic) {
       constexpr int i = decltype(ic)::value + 1;
-      double ys[6];
+      double ys[NC];
 #pragma unroll
-      for (int d = 0; d < 6; ++d) ys[d] = y[d];
+      for (int d = 0; d < NC; ++d) ys[d] = y[d];
       static_for<i>([&](auto jc) {
         constexpr int j = decltype(jc)::value;
         constexpr double a = T::a(i, j);
         if constexpr (a != 0.0) {
           const double c = h * a;
 #pragma unroll
-          for (int d = 0; d < 6; ++d) ys[d] = ys[d] + c * k[j][d];
+          for (int d = 0; d < NC; ++d) ys[d] = ys[d] + c * k[j][d];
         }
       });
       L.rhs(ys, mu, dir, k[i]);
     });
 #pragma unroll
-    for (int d = 0; d < 6; ++d) yh[d] = y[d];
+    for (int d = 0; d < NC; ++d) yh[d] = y[d];
     static_for<T::S>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
       constexpr double b = T::b(j);
       if constexpr (b != 0.0) {
         const double c = h * b;
 #pragma unroll
-        for (int d = 0; d < 6; ++d) yh[d] = yh[d] + c * k[j][d];
+        for (int d = 0; d < NC; ++d) yh[d] = yh[d] + c * k[j][d];
       }
     });
     L.rhs(yh, mu, dir, k[12]);
 #pragma unroll
-    for (int d = 0; d < 6; ++d) {
+    for (int d = 0; d < NC; ++d) {
       e5[d] = 0.0;
       e3[d] = 0.0;
     }
@@ -551,32 +633,32 @@ struct DopLane {
       constexpr double c3 = T::e3(j);
       if constexpr (c5 != 0.0) {
 #pragma unroll
-        for (int d = 0; d < 6; ++d) e5[d] = e5[d] + c5 * k[j][d];
+        for (int d = 0; d < NC; ++d) e5[d] = e5[d] + c5 * k[j][d];
       }
       if constexpr (c3 != 0.0) {
 #pragma unroll
-        for (int d = 0; d < 6; ++d) e3[d] = e3[d] + c3 * k[j][d];
+        for (int d = 0; d < NC; ++d) e3[d] = e3[d] + c3 * k[j][d];
       }
     });
 #pragma unroll
-    for (int d = 0; d < 6; ++d) {
+    for (int d = 0; d < NC; ++d) {
       e5[d] = e5[d] * h;
       e3[d] = e3[d] * h;
     }
   }
 
   // _dop853_build_dense_cache: F[0..6][6] for this lane's components.
-  __device__ __forceinline__ static void dense_cache(const Layout<G>& L, const double (&y_old)[6],
-                                                     const double (&y_new)[6], double hseg, double mu,
-                                                     const Dir& dir, const double (&k)[13][6],
-                                                     double (&F)[7][6]) {
+  __device__ __forceinline__ static void dense_cache(const Layout<G>& L, const double (&y_old)[NC],
+                                                     const double (&y_new)[NC], double hseg, double mu,
+                                                     const Dir& dir, const double (&k)[13][NC],
+                                                     double (&F)[7][NC]) {
     using T = DopTab;
-    double kx[3][6];
+    double kx[3][NC];
     static_for<3>([&](auto sc) {
       constexpr int srow = decltype(sc)::value + 13;
-      double ys[6];
+      double ys[NC];
 #pragma unroll
-      for (int d = 0; d < 6; ++d) {
+      for (int d = 0; d < NC; ++d) {
         double acc = 0.0;
         static_for<srow>([&](auto rc) {
           constexpr int r = decltype(rc)::value;
@@ -593,7 +675,7 @@ struct DopLane {
       L.rhs(ys, mu, dir, kx[srow - 13]);
     });
 #pragma unroll
-    for (int d = 0; d < 6; ++d) {
+    for (int d = 0; d < NC; ++d) {
       const double dy = y_new[d] - y_old[d];
       F[0][d] = dy;
       F[1][d] = hseg * k[0][d] - dy;
@@ -602,7 +684,7 @@ struct DopLane {
     static_for<4>([&](auto ic) {
       constexpr int irem = decltype(ic)::value;
 #pragma unroll
-      for (int d = 0; d < 6; ++d) {
+      for (int d = 0; d < NC; ++d) {
         double acc = 0.0;
         static_for<16>([&](auto rc) {
           constexpr int r = decltype(rc)::value;
@@ -632,7 +714,7 @@ struct DopLane {
     return v + y_old;
   }
 
-  __device__ __forceinline__ static double eval1(double y_old, const double (&F)[7][6], int d, double x) {
+  __device__ __forceinline__ static double eval1(double y_old, const double (&F)[7][NC], int d, double x) {
     double v = 0.0;
 #pragma unroll
     for (int i = 6; i >= 0; --i) {
@@ -649,6 +731,7 @@ struct DopLane {
 template <int G>
 __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
   constexpr int D = Layout<G>::D;
+  constexpr int NC = Layout<G>::NC;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -659,6 +742,12 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
   if constexpr (G == 1) {
     L.role = 6;
     traj = warp * 32 + lane;
+  } else if constexpr (G == 2) {
+    const int g = lane >> 1;
+    L.role = lane & 1;
+    L.base = g * 2;
+    L.gmask = 0x3u << L.base;
+    traj = warp * 16 + g;
   } else {
     if (lane >= 28) return;
     const int g = lane / 7;
@@ -668,26 +757,21 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
     traj = warp * 4 + g;
     gat.slot = sm_gather + (wib * 4 + g) * 42;
   }
+  const bool leader = (G == 1) || (G == 2 && L.role == 0) || (G == 7 && L.role == 6);
   const bool has_event = p.ev_index >= 0 && p.max_hits > 0;
-  // event component: which lane/slot holds it
+  // event component: which lane of the group holds it, and where
   int ev_r = 0;
   bool ev_mine = false;
+  int ev_src = lane;
   if (has_event) {
+    ev_r = L.local(p.ev_index);
     if constexpr (G == 1) {
-      ev_r = p.ev_index;
       ev_mine = true;
     } else {
-      if (p.ev_index >= 36) {
-        ev_r = p.ev_index - 36;
-        ev_mine = (L.role == 6);
-      } else {
-        ev_r = p.ev_index / 6;
-        ev_mine = (L.role == p.ev_index % 6);
-      }
+      ev_mine = (L.role == L.owner(p.ev_index));
+      ev_src = L.base + L.owner(p.ev_index);
     }
   }
-  int ev_src = lane;
-  if constexpr (G == 7) ev_src = L.base + (p.ev_index >= 36 ? 6 : (p.ev_index % 6));
   auto bcast_ev = [&](double v) -> double {
     if constexpr (G == 1)
       return v;
@@ -698,18 +782,18 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
   while (traj < p.N) {
     const double t0 = p.t0_arr ? p.t0_arr[traj] : p.t0;
     const double tmax = p.tmax_arr ? p.tmax_arr[traj] : p.tmax;
-    double y[6];
+    double y[NC];
 #pragma unroll
-    for (int r = 0; r < 6; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld + traj];
-    double k[13][6];
+    for (int r = 0; r < NC; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld + traj];
+    double k[13][NC];
     L.rhs(y, p.mu, p.dir, k[0]);
     double g_prev = 0.0;
-    if (has_event) g_prev = bcast_ev(ev_mine ? (pick6(y, ev_r) - p.ev_offset) : 0.0);
+    if (has_event) g_prev = bcast_ev(ev_mine ? (pick<NC>(y, ev_r) - p.ev_offset) : 0.0);
     double h;
     {
-      double a[6], b[6];
+      double a[NC], b[NC];
 #pragma unroll
-      for (int d = 0; d < 6; ++d) {
+      for (int d = 0; d < NC; ++d) {
         const double scale0 = p.atol + p.rtol * fabs(y[d]);
         a[d] = y[d] / scale0;
         b[d] = k[0][d] / scale0;
@@ -739,13 +823,13 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
       }
       h = clamp_step(h, p.max_step, p.min_step);
       h = adjust_step_to_endpoint(t, h, tmax);
-      double yh[6], e5[6], e3[6];
+      double yh[NC], e5[NC], e3[NC];
       DopLane<G>::step(L, y, h, p.mu, p.dir, k, yh, e5, e3);
       double err_norm;
       {
-        double s5[6], s3[6];
+        double s5[NC], s3[NC];
 #pragma unroll
-        for (int d = 0; d < 6; ++d) {
+        for (int d = 0; d < NC; ++d) {
           const double scale = p.atol + p.rtol * np_maximum_abs(y[d], yh[d]);
           const double is = hg_rcp_rn(scale);
           s5[d] = hg_div_rn(e5[d], scale, is);
@@ -767,28 +851,28 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
           const bool last = !((t_new - tmax) * 1.0 < 0.0);
           if (q_next < p.m && (last || sample_t(q_next) < t_new)) {
             const double hseg = t_new - t;
-            double F[7][6];
+            double F[7][NC];
             DopLane<G>::dense_cache(L, y, yh, hseg, p.mu, p.dir, k, F);
             while (q_next < p.m && (last || sample_t(q_next) < t_new)) {
               const double x = (sample_t(q_next) - t) / hseg;
               double* o = p.y_out + (long long)(p.dense_last ? 0 : q_next) * D * p.ld;
 #pragma unroll
-              for (int d = 0; d < 6; ++d)
+              for (int d = 0; d < NC; ++d)
                 o[(long long)L.comp(d) * p.ld + traj] = DopLane<G>::eval1(y[d], F, d, x);
               ++q_next;
             }
           }
         }
         if (has_event) {
-          const double g_new = bcast_ev(ev_mine ? (pick6(yh, ev_r) - p.ev_offset) : 0.0);
+          const double g_new = bcast_ev(ev_mine ? (pick<NC>(yh, ev_r) - p.ev_offset) : 0.0);
           if (event_crossed(g_prev, g_new, p.ev_dir)) {
             // _dop853_refine_in_step with the step size h
-            double F[7][6];
+            double F[7][NC];
             DopLane<G>::dense_cache(L, y, yh, h, p.mu, p.dir, k, F);
             double fe[7];
 #pragma unroll
-            for (int i = 0; i < 7; ++i) fe[i] = pick6(F[i], ev_r);
-            const double ye = pick6(y, ev_r);
+            for (int i = 0; i < 7; ++i) fe[i] = pick<NC>(F[i], ev_r);
+            const double ye = pick<NC>(y, ev_r);
             double a = 0.0, b = 1.0;
             double g_left = g_prev;
             double x_hit = -1.0;
@@ -811,7 +895,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
             p.hit_t[(long long)hits * p.ld + traj] = t + x_hit * h;
             double* o = p.hit_y + (long long)hits * D * p.ld;
 #pragma unroll
-            for (int d = 0; d < 6; ++d) o[(long long)L.comp(d) * p.ld + traj] = DopLane<G>::eval1(y[d], F, d, x_hit);
+            for (int d = 0; d < NC; ++d) o[(long long)L.comp(d) * p.ld + traj] = DopLane<G>::eval1(y[d], F, d, x_hit);
             ++hits;
             if (hits >= p.max_hits) stop = true;
           }
@@ -820,7 +904,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
         t = t_new;
         bool fin = true;
 #pragma unroll
-        for (int d = 0; d < 6; ++d) {
+        for (int d = 0; d < NC; ++d) {
           y[d] = yh[d];
           k[0][d] = k[12][d];
           fin = fin && finite_bits(yh[d]);
@@ -828,7 +912,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
         if (stop) break;
         h = h * pi_accept_factor(err_norm, err_prev, prev_pow);
         err_prev = err_norm;
-        if constexpr (G == 7) fin = __all_sync(L.gmask, fin);
+        if constexpr (G > 1) fin = __all_sync(L.gmask, fin);
         if (!fin) {
           status = HG_NONFINITE;
           break;
@@ -842,7 +926,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
     // outputs
     if (p.y_end) {
 #pragma unroll
-      for (int d = 0; d < 6; ++d) p.y_end[(long long)L.comp(d) * p.ld + traj] = y[d];
+      for (int d = 0; d < NC; ++d) p.y_end[(long long)L.comp(d) * p.ld + traj] = y[d];
     }
     if (dense) {
       // the reference's dense output falls back to the single stored node
@@ -850,11 +934,11 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
       while (q_next < p.m) {
         double* o = p.y_out + (long long)(p.dense_last ? 0 : q_next) * D * p.ld;
 #pragma unroll
-        for (int d = 0; d < 6; ++d) o[(long long)L.comp(d) * p.ld + traj] = y[d];
+        for (int d = 0; d < NC; ++d) o[(long long)L.comp(d) * p.ld + traj] = y[d];
         ++q_next;
       }
     }
-    if (L.role == 6) {
+    if (leader) {
       if (p.t_end) p.t_end[traj] = t;
       if (p.n_hits) p.n_hits[traj] = hits;
       if (p.n_accept) p.n_accept[traj] = acc;

@@ -181,3 +181,26 @@ def fp64_peak_tflops(device=None):
     with torch.cuda.device(dev):
         H.check(H.lib.hg_probe_fp64_peak(H.ptr, C.byref(v)))
     return v.value
+
+
+class tuning:
+    """Set the launch shape of the device's handle (results are unchanged):
+    ``lanes_d6`` in {0 (auto), 1, 2} lanes per 6-dim DOP853 trajectory,
+    ``block`` in {32, 64, 128} threads per block.  Usable as a context
+    manager (restores the previous values on exit) or as a plain call."""
+
+    def __init__(self, lanes_d6=None, block=None, device=None):
+        dev = _device(device)
+        self.H = _lib.handle(dev.index or 0)
+        self.old = (self.H.get_tuning(_lib.HG_TUNE_DOP853_LANES_D6), self.H.get_tuning(_lib.HG_TUNE_BLOCK_THREADS))
+        if lanes_d6 is not None:
+            self.H.set_tuning(_lib.HG_TUNE_DOP853_LANES_D6, lanes_d6)
+        if block is not None:
+            self.H.set_tuning(_lib.HG_TUNE_BLOCK_THREADS, block)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.H.set_tuning(_lib.HG_TUNE_DOP853_LANES_D6, self.old[0])
+        self.H.set_tuning(_lib.HG_TUNE_BLOCK_THREADS, self.old[1])

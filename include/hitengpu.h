@@ -139,6 +139,19 @@ int hg_propagate_dop853_noalloc(double mu, int dim, int N,
                                 int* n_accept, int* n_reject, int* status,
                                 void* stream);
 
+/* Launch-shape tuning of a handle (set by hiten_gb300.autotune).
+ * HG_TUNE_BLOCK_THREADS: threads per block, 32 (default), 64 or 128.
+ * HG_TUNE_DOP853_LANES_D6: lanes per 6-dim DOP853 trajectory: 1 (one
+ * trajectory per lane: least total work), 2 (lane pairs: about half the
+ * per-step latency, for batches too small to fill the GPU, where the
+ * longest trajectory sets the time), 0 = automatic (the default).
+ * Results are bit-identical for every setting.
+ * Replaces: nothing (no reference counterpart; launch shape only). */
+#define HG_TUNE_BLOCK_THREADS 1
+#define HG_TUNE_DOP853_LANES_D6 2
+int hg_set_tuning(hg_handle* h, int key, int value);
+int hg_get_tuning(hg_handle* h, int key, int* value);
+
 /* Measured FP64 fused-multiply-add throughput of this device (TFLOP/s,
  * counting an FMA as 2 flops): runs a short dependent-chain-free DFMA loop
  * on all SMs and times it with CUDA events.  Synchronous. */

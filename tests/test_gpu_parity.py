@@ -15,6 +15,14 @@ pytestmark = pytest.mark.gpu
 MU = W.MU_EM
 
 
+@pytest.fixture(params=[(1, 32), (2, 32), (1, 128), (2, 64)], ids=["lanes1-b32", "lanes2-b32", "lanes1-b128",
+                                                                   "lanes2-b64"])
+def shape(request, gpu):
+    """Every launch shape must give the same bits."""
+    with gpu.tuning(lanes_d6=request.param[0], block=request.param[1]):
+        yield request.param
+
+
 @pytest.fixture(scope="module")
 def dev_oracle(oracle):
     oracle.set_mode(oracle.MODE_DEVICE)
@@ -29,7 +37,7 @@ def _np(t):
 # ------------------------------------------------------------------ fixed step
 @pytest.mark.parametrize("order", [4, 6, 8])
 @pytest.mark.parametrize("dim", [6, 42])
-def test_fixed_matches_oracle_bitexact(gpu, dev_oracle, order, dim):
+def test_fixed_matches_oracle_bitexact(gpu, shape, dev_oracle, order, dim):
     n_traj = 37  # crosses warp/group boundaries
     if dim == 42:
         y0 = W.stm_fixed_batch(1024, seed=0)[:n_traj]
@@ -88,7 +96,7 @@ def _cmp_event(res, ref, dim):
 
 
 @pytest.mark.parametrize("fwd", [1, -1])
-def test_dop853_manifold_event_bitexact(gpu, dev_oracle, fwd):
+def test_dop853_manifold_event_bitexact(gpu, shape, dev_oracle, fwd):
     rng = np.random.default_rng(7)
     y0 = W.HALO_L1_AZ02_X0 + rng.uniform(-1e-5, 1e-5, (45, 6))
     ev = gpu.EventSpec(index=0, offset=1 - MU, direction=0, max_hits=1)
@@ -97,7 +105,7 @@ def test_dop853_manifold_event_bitexact(gpu, dev_oracle, fwd):
     _cmp_event(res, ref, 6)
 
 
-def test_dop853_section_multihit_bitexact(gpu, dev_oracle):
+def test_dop853_section_multihit_bitexact(gpu, shape, dev_oracle):
     y0 = W.section_states(70, seed=9)
     ev = gpu.EventSpec(index=1, offset=0.0, direction=-1, max_hits=8)
     res = gpu.propagate_dop853(y0, 0.0, 20.0, MU, rtol=1e-11, atol=1e-11, event=ev)
@@ -106,7 +114,7 @@ def test_dop853_section_multihit_bitexact(gpu, dev_oracle):
     assert np.all(_np(res.status) == 0)
 
 
-def test_dop853_singlehit_window_bitexact(gpu, dev_oracle):
+def test_dop853_singlehit_window_bitexact(gpu, shape, dev_oracle):
     rng = np.random.default_rng(3)
     y0 = W.HALO_L1_AZ02_X0 + np.c_[rng.uniform(-1e-3, 1e-3, 33), np.zeros(33), rng.uniform(-1e-3, 1e-3, 33),
                                    np.zeros(33), rng.uniform(-1e-3, 1e-3, 33), np.zeros(33)]
@@ -116,7 +124,7 @@ def test_dop853_singlehit_window_bitexact(gpu, dev_oracle):
     _cmp_event(res, ref, 6)
 
 
-def test_dop853_stm_dense_bitexact(gpu, dev_oracle):
+def test_dop853_stm_dense_bitexact(gpu, shape, dev_oracle):
     x0 = W.HALO_L1_AZ02_X0
     y0 = np.array([stm_state(x0 + d) for d in np.linspace(-1e-4, 1e-4, 9)[:, None] * np.eye(6)[0]])
     T = W.HALO_L1_AZ02_T
@@ -162,7 +170,7 @@ def test_max_steps_status(gpu):
     assert np.all(_np(res.n_accept) + _np(res.n_reject) == 3)
 
 
-def test_lane_refill_matches_oracle(gpu, dev_oracle):
+def test_lane_refill_matches_oracle(gpu, shape, dev_oracle):
     """More trajectories than resident lanes: finished lanes take new ones."""
     y0 = W.section_states(60000, seed=4)
     ev = gpu.EventSpec(index=1, offset=0.0, direction=-1, max_hits=2)
