@@ -110,18 +110,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_reference(seeds, sample, threads, mode_name="NUMBA"):
-    """Time the CPU oracle (reference algorithm) on `sample` seeds with all threads."""
+def cpu_reference(seeds, sample, threads, mode_name="NUMBA", min_seconds=3.0):
+    """Time the CPU oracle (reference algorithm) on `sample` seeds with all threads, repeating the
+    sample until at least `min_seconds` of wall time are covered."""
     from oracle import hgo
     from hiten_gb300 import workloads as W
     mu = W.MU_EM
     hgo.set_mode(getattr(hgo, "MODE_" + mode_name))
     s = seeds[:sample]
+    acc = 0
     t0 = time.perf_counter()
-    r = hgo.dop853_event_batch(s, 0.0, TF, mu, 0, 1 - mu, 0, 1, max_step=1e4, fwd=-1, flip=(0, 6),
-                               threads=threads)
-    dt = time.perf_counter() - t0
-    return float(r["n_accept"].sum()) / dt, dt, int(r["n_accept"].sum())
+    while True:  # repeat the sample until the timing covers at least min_seconds
+        r = hgo.dop853_event_batch(s, 0.0, TF, mu, 0, 1 - mu, 0, 1, max_step=1e4, fwd=-1, flip=(0, 6),
+                                   threads=threads)
+        acc += int(r["n_accept"].sum())
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            break
+    return float(acc) / dt, dt, acc
 
 
 def run_reference_arm(args):
@@ -141,10 +147,10 @@ def run_reference_arm(args):
     phases, disp = W.manifold_grid(N_PHASE, N_DISP, seed=0)
     seeds = M.seeds(-np.linspace(0.0, T, 2000), PHI, T, phases, disp, v, direction=1)
     threads = os.cpu_count() or 1
-    sample = min(len(seeds), 2048)
+    sample = len(seeds)
     vals = []
     for i in range(args.warmup + args.steps):
-        v, dt, n = cpu_reference(np.roll(seeds, -i * 97, axis=0), sample, threads)
+        v, dt, n = cpu_reference(seeds, sample, threads, min_seconds=2.0)
         if i >= args.warmup:
             vals.append((v, dt))
     value = statistics.median(v for v, _ in vals)
@@ -154,8 +160,8 @@ def run_reference_arm(args):
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": config(args.gpus),
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": f"{sample} of the 16384 manifold seeds per step (CPU oracle, numba "
-                                      f"lowering of powers, libm pow), one trajectory per task"},
+                            "sample": f"all {sample} manifold seeds per step, repeated to >= 2 s (CPU oracle, "
+                                      f"numba lowering of powers, libm pow), one trajectory per task"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -183,6 +189,7 @@ def main():
         dist.init_process_group("nccl", device_id=dev)
 
     from hiten_gb300 import _lib
+    from hiten_gb300 import autotune
     from hiten_gb300 import manifold as M
     from hiten_gb300 import propagate as P
     from hiten_gb300 import workloads as W
@@ -200,6 +207,23 @@ def main():
     for _ in range(max(args.warmup, 3)):
         r = one_step()
     torch.cuda.synchronize(dev)
+    # launch shape (lanes per trajectory, block size) chosen by measurement on
+    # this workload; results are identical for every shape
+    shape, shape_ms = autotune.tune(f"manifold_{N}", one_step, device=dev)
+
+    # plain form: one kernel call per trajectory, the reference's call
+    # granularity (one _propagate_dynsys per seed), on a bounded sample
+    n_plain = 64
+    torch.cuda.synchronize(dev)
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    plain_acc = 0
+    plain_res = [M.propagate_to_plane(seeds_dev[i:i + 1], mu, tf=TF, forward=-1, device=dev) for i in range(n_plain)]
+    p1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_acc = sum(int(x.n_accept.sum().item()) for x in plain_res)
+    plain_value = plain_acc / (p0.elapsed_time(p1) * 1e-3)
 
     # ---- device-resident timing (CUDA events on the launching stream)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -261,10 +285,10 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        sample = 2048
-        v, dt, n = cpu_reference(seeds, sample, threads)
+        sample = len(seeds)
+        v, dt, n = cpu_reference(seeds, sample, threads, min_seconds=5.0)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"first {sample} of the 16384 seeds ({n} accepted steps, {dt:.1f} s), CPU oracle in "
+               "sample": f"all {sample} seeds, repeated: {n} accepted steps in {dt:.1f} s, CPU oracle in "
                          f"numba-lowering mode, one trajectory per thread task"}
 
     if rank == 0:
@@ -285,6 +309,11 @@ def main():
                             "flops_per_attempted_step": FLOPS_PER_ATTEMPT_D6},
                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": args.steps,
+               "launch_shape": {"lanes_per_trajectory": shape[0], "block_threads": shape[1],
+                                "autotune_ms": {f"lanes{k[0]}_block{k[1]}": v for k, v in shape_ms.items()}},
+               "plain_gpu": {"value": plain_value, "unit": UNIT,
+                             "form": f"one kernel call per trajectory (reference call granularity), "
+                                     f"{n_plain}-trajectory sample"},
                "library": os.path.basename(_lib.load()._name)}
         print(json.dumps(out))
     if world > 1:

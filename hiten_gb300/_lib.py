@@ -136,13 +136,19 @@ class Handle:
             pass
 
 
-_handles = {}
+_tls = threading.local()
 
 
 def handle(device=0):
-    """Process-wide handle for a device (created on first use)."""
-    h = _handles.get(device)
+    """This thread's handle for a device (created on first use).  A handle
+    owns the lane-refill scratch of the calls made through it, so each host
+    thread gets its own: calls from different threads on different streams
+    never share scratch."""
+    hs = getattr(_tls, "handles", None)
+    if hs is None:
+        hs = _tls.handles = {}
+    h = hs.get(device)
     if h is None:
         h = Handle(device)
-        _handles[device] = h
+        hs[device] = h
     return h

@@ -1,0 +1,226 @@
+"""Continuous-batching request server for manifold, correction and
+section-map solves (FP64, one GPU).
+
+Requests arrive at any time.  Every scheduler tick the engine:
+
+1. admits waiting requests in arrival order while their HBM footprint fits
+   the budget (a request that does not fit waits until running batches
+   release memory);
+2. merges the admitted requests of one kind into one batch and launches it
+   on its own CUDA stream, so batches of different kinds, and batches admitted
+   while others are still running, execute concurrently on the device;
+3. collects finished batches, splits the results back per request, releases
+   their memory and stamps the completion time.
+
+Trajectories are independent lanes in every kernel, so a request's result
+does not depend on what it was batched with (checked bit for bit by
+tests/test_gpu_serving.py).  `run_sequential` is the plain form: one request
+at a time, each with its own kernel calls, on one stream.
+
+Request kinds (types/services: manifold.py:293-442, orbits.py:114-151;
+poincare/synodic): 'manifold' (seeds, DOP853 1e-12 backward to t = -8 or the
+x = 1 - mu plane), 'correct' (halo guesses, batched Newton), 'synodic'
+(states, DOP853 1e-11 to t = 20, up to 8 decreasing y = 0 crossings).
+"""
+import concurrent.futures as cf
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import corrector
+from . import propagate as P
+
+BYTES_PER_TRAJ = {"manifold": 8 * (6 + 6 + 1 + 7) + 4 * 4,
+                  "synodic": 8 * (6 + 6 + 1 + 8 * 7) + 4 * 4,
+                  "correct": 8 * (42 * 3 + 6 * 4) + 4 * 4}
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str
+    payload: np.ndarray
+    arrival: float = 0.0
+    admitted: float = None
+    done: float = None
+    result: dict = None
+
+    @property
+    def footprint(self):
+        return BYTES_PER_TRAJ[self.kind] * len(self.payload)
+
+
+def _solve(kind, x, mu, device):
+    """Run one batch of one kind; returns host arrays per trajectory."""
+    if kind == "manifold":
+        ev = P.EventSpec(index=0, offset=1.0 - mu, direction=0, max_hits=1)
+        r = P.propagate_dop853(x, 0.0, 8.0, mu, rtol=1e-12, atol=1e-12, max_step=1e4, fwd=-1, flip=(0, 6),
+                               event=ev, device=device)
+        return {"y_end": r.y_end.cpu().numpy(), "t_end": r.t_end.cpu().numpy(), "n_hits": r.n_hits.cpu().numpy(),
+                "hit_t": r.hit_t.cpu().numpy(), "hit_y": r.hit_y.cpu().numpy(), "n_accept": r.n_accept.cpu().numpy(),
+                "status": r.status.cpu().numpy()}
+    if kind == "synodic":
+        ev = P.EventSpec(index=1, offset=0.0, direction=-1, max_hits=8)
+        r = P.propagate_dop853(x, 0.0, 20.0, mu, rtol=1e-11, atol=1e-11, max_step=1e4, event=ev, device=device)
+        return {"y_end": r.y_end.cpu().numpy(), "n_hits": r.n_hits.cpu().numpy(), "hit_t": r.hit_t.cpu().numpy(),
+                "hit_y": r.hit_y.cpu().numpy(), "n_accept": r.n_accept.cpu().numpy(), "status": r.status.cpu().numpy()}
+    if kind == "correct":
+        res = corrector.correct_halo(x, mu, device=device)
+        return {"x0": res.x0, "period": res.period, "iterations": res.iterations, "status": res.status}
+    raise ValueError(kind)
+
+
+def _split(kind, res, sizes):
+    out, off = [], 0
+    for n in sizes:
+        out.append({k: v[off:off + n] for k, v in res.items()})
+        off += n
+    return out
+
+
+@dataclass
+class ServingStats:
+    n: int = 0
+    wall_s: float = 0.0
+    latencies: list = field(default_factory=list)
+    traj_steps: int = 0
+    batches: int = 0
+
+    def summary(self):
+        lat = np.array(self.latencies) if self.latencies else np.zeros(1)
+        return {"requests": self.n, "wall_s": self.wall_s, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                "p99_ms": float(np.percentile(lat, 99) * 1e3), "traj_steps": self.traj_steps,
+                "traj_steps_per_s": self.traj_steps / self.wall_s if self.wall_s else 0.0,
+                "requests_per_s": self.n / self.wall_s if self.wall_s else 0.0, "batches": self.batches}
+
+
+class ServingEngine:
+    """Continuous batching with HBM-footprint admission (see module docstring)."""
+
+    def __init__(self, mu, device=None, hbm_budget_bytes=8 << 30, max_concurrent=6, tick_s=0.002):
+        self.mu = float(mu)
+        self.device = P._device(device)
+        self.budget = int(hbm_budget_bytes)
+        self.in_use = 0
+        self.tick_s = tick_s
+        self.pool = cf.ThreadPoolExecutor(max_workers=max_concurrent)
+        self.max_concurrent = max_concurrent
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_concurrent)]
+        self.free_streams = list(range(max_concurrent))
+        self.lock = threading.Lock()
+
+    def _run_batch(self, kind, reqs, sidx):
+        x = np.concatenate([r.payload for r in reqs])
+        with torch.cuda.stream(self.streams[sidx]):
+            res = _solve(kind, x, self.mu, self.device)
+            torch.cuda.current_stream(self.device).synchronize()
+        t = time.perf_counter()
+        for r, part in zip(reqs, _split(kind, res, [len(q.payload) for q in reqs])):
+            r.result = part
+            r.done = t
+        return kind, reqs, sidx
+
+    def serve(self, requests, t0=None):
+        """Serve `requests` (sorted by `arrival`, seconds relative to t0)."""
+        t0 = time.perf_counter() if t0 is None else t0
+        waiting = []
+        futures = set()
+        nxt = 0
+        stats = ServingStats()
+        while nxt < len(requests) or waiting or futures:
+            now = time.perf_counter() - t0
+            while nxt < len(requests) and requests[nxt].arrival <= now:
+                waiting.append(requests[nxt])
+                nxt += 1
+            # collect finished batches
+            done = {f for f in futures if f.done()}
+            for f in done:
+                kind, reqs, sidx = f.result()
+                with self.lock:
+                    self.in_use -= sum(r.footprint for r in reqs)
+                    self.free_streams.append(sidx)
+                stats.batches += 1
+            futures -= done
+            # admit in arrival order while the footprint fits; merge per kind
+            if waiting and self.free_streams:
+                admitted = {}
+                keep = []
+                for r in waiting:
+                    fits = self.in_use + r.footprint <= self.budget or (self.in_use == 0 and not admitted)
+                    if fits and (r.kind in admitted or len(admitted) < len(self.free_streams)):
+                        admitted.setdefault(r.kind, []).append(r)
+                        self.in_use += r.footprint
+                        r.admitted = time.perf_counter()
+                    else:
+                        keep.append(r)
+                waiting = keep
+                for kind, reqs in admitted.items():
+                    sidx = self.free_streams.pop()
+                    futures.add(self.pool.submit(self._run_batch, kind, reqs, sidx))
+            if not done:
+                time.sleep(self.tick_s)
+        stats.wall_s = time.perf_counter() - t0
+        for r in requests:
+            stats.n += 1
+            stats.latencies.append(r.done - (t0 + r.arrival))
+            if "n_accept" in r.result:
+                stats.traj_steps += int(np.sum(r.result["n_accept"]))
+        return stats
+
+    def close(self):
+        self.pool.shutdown(wait=True)
+
+
+def run_sequential(requests, mu, device=None, t0=None):
+    """Plain form: each request alone, in arrival order, on the current stream."""
+    dev = P._device(device)
+    t0 = time.perf_counter() if t0 is None else t0
+    stats = ServingStats()
+    for r in requests:
+        wait = r.arrival - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        r.admitted = time.perf_counter()
+        r.result = _solve(r.kind, r.payload, mu, dev)
+        torch.cuda.synchronize(dev)
+        r.done = time.perf_counter()
+        stats.n += 1
+        stats.latencies.append(r.done - (t0 + r.arrival))
+        if "n_accept" in r.result:
+            stats.traj_steps += int(np.sum(r.result["n_accept"]))
+    stats.wall_s = time.perf_counter() - t0
+    return stats
+
+
+def poisson_requests(rate_hz, duration_s, mu, seed=0, manifold_seeds=None, size_scale=1.0):
+    """Seeded Poisson stream: kinds uniform over manifold (64-4096 seeds),
+    correct (1-256 guesses) and synodic (1k-32k states), sizes log-uniform
+    (multiplied by size_scale, for small test streams)."""
+    from . import halo
+    from . import workloads as W
+    rng = np.random.default_rng(seed)
+    t, rid, out = 0.0, 0, []
+    if manifold_seeds is None:
+        manifold_seeds = W.section_states(4096, seed=seed + 1)
+    while True:
+        t += rng.exponential(1.0 / rate_hz)
+        if t >= duration_s:
+            break
+        kind = ("manifold", "correct", "synodic")[rng.integers(0, 3)]
+        lo, hi = {"manifold": (64, 4096), "correct": (1, 256), "synodic": (1024, 32768)}[kind]
+        n = int(np.exp(rng.uniform(np.log(lo), np.log(hi))) * size_scale)
+        n = max(1, n)
+        if kind == "manifold":
+            idx = rng.integers(0, len(manifold_seeds), n)
+            payload = manifold_seeds[idx]
+        elif kind == "correct":
+            pt, az, zen = W.halo_guess_params(n, seed=int(rng.integers(1 << 30)))
+            payload = np.concatenate([halo.third_order_guess(mu, int(p), a, z) for p, a, z in zip(pt, az, zen)])
+        else:
+            payload = W.section_states(n, seed=int(rng.integers(1 << 30)))
+        out.append(Request(rid=rid, kind=kind, payload=payload, arrival=t))
+        rid += 1
+    return out
