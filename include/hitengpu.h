@@ -139,6 +139,27 @@ int hg_propagate_dop853_noalloc(double mu, int dim, int N,
                                 int* n_accept, int* n_reject, int* status,
                                 void* stream);
 
+/* Plane crossings on sampled trajectories (the synodic Poincare map):
+ * plane g = y[axis] - offset; samples [m][6][ld] (e.g. the dense output of
+ * hg_propagate_dop853), times [m][times_ld] (times_ld = 0: one shared time
+ * grid [m]).  direction -1/0/+1; plane_u/plane_v: the projected coordinates
+ * used for de-duplication; segment_refine >= 1 sub-intervals per segment with
+ * linear (cubic = 0, the reference's default path) or cubic Hermite + Newton
+ * (cubic = 1) interpolation; tol_on_surface, dedup_time_tol,
+ * dedup_point_tol as the reference.  Stores up to max_hits hits per
+ * trajectory (hit_t [max_hits][ld], hit_y [max_hits][6][ld]); n_hits [N]
+ * (stored), n_found [N] (nullable; accepted, equal to n_hits).
+ * Replaces: poincare/synodic/backend.py:458-659 (_detect_with_segment_refine)
+ * and :382-455 (_order_and_dedup_hits), as reached from
+ * _SynodicDetectionBackend.detect_on_trajectory (:687-821). */
+int hg_section_detect(int N, int m, const double* samples, long long ld,
+                      const double* times, long long times_ld,
+                      int axis, double offset, int direction, int plane_u, int plane_v,
+                      int segment_refine, int cubic, int newton_max_iter,
+                      double tol_on_surface, double dedup_time_tol, double dedup_point_tol,
+                      int max_hits, double* hit_t, double* hit_y, int* n_hits, int* n_found,
+                      void* stream);
+
 /* Launch-shape tuning of a handle (set by hiten_gb300.autotune).
  * HG_TUNE_BLOCK_THREADS: threads per block, 32 (default), 64 or 128.
  * HG_TUNE_DOP853_LANES_D6: lanes per 6-dim DOP853 trajectory: 1 (one

@@ -719,3 +719,159 @@ int hgo_dop853_event_batch(int dim, double mu, int fwd, int flip_lo, int flip_hi
   run_job(&J, threads);
   return HGO_OK;
 }
+
+/* ---------------------------------------------------------------------------
+ * Section crossings on one sampled trajectory,
+ * poincare/synodic/backend.py:458-659 (_detect_with_segment_refine) and
+ * :382-455 (_order_and_dedup_hits), plane g = y[axis] - offset,
+ * poincare/utils.py:53-147 (_hermite_scalar / _hermite_der, numba-compiled:
+ * squares through hgo_ipow2 outside PYTHON mode; the state interpolation in
+ * backend.py is plain Python, so its squares are libm pow except in DEVICE
+ * mode).  times/states are (m,) and (m, 6) row-major.  Returns the number of
+ * accepted hits (all of them); stores at most max_hits.
+ * ------------------------------------------------------------------------- */
+static double sq_py(double x) { return g_mode == HGO_MODE_DEVICE ? x * x : pow(x, 2.0); }
+
+static double herm_s(double s, double y0, double y1, double dy0, double dy1, double dt) {
+  const double h00 = (1.0 + 2.0 * s) * hgo_ipow2(1.0 - s);
+  const double h10 = s * hgo_ipow2(1.0 - s);
+  const double h01 = hgo_ipow2(s) * (3.0 - 2.0 * s);
+  const double h11 = hgo_ipow2(s) * (s - 1.0);
+  return ((h00 * y0 + (h10 * dy0) * dt) + h01 * y1) + (h11 * dy1) * dt;
+}
+
+static double herm_d(double s, double y0, double y1, double dy0, double dy1, double dt) {
+  const double dh00 = ((6.0 * s) * (s - 1.0) + hgo_ipow2(1.0 - s) * 2.0) - (2.0 * (1.0 - s)) * (1.0 + 2.0 * s);
+  const double dh10 = hgo_ipow2(1.0 - s) + s * (2.0 * (s - 1.0));
+  const double dh01 = (6.0 * s) * (1.0 - s) - (2.0 * s) * (3.0 - 2.0 * s);
+  const double dh11 = (2.0 * s) * (s - 1.0) + hgo_ipow2(s);
+  return ((dh00 * y0 + (dh10 * dy0) * dt) + dh01 * y1) + (dh11 * dy1) * dt;
+}
+
+typedef struct {
+  int have, stored, found, max_hits, pu, pv;
+  double pt, pu_v, pv_v, dtt, dpt;
+  double *hit_t, *hit_y;
+} hgo_emit;
+
+static int emit(hgo_emit* E, double th, const double* x) {
+  if (E->max_hits > 0 && E->stored >= E->max_hits) return 1;
+  const double u = x[E->pu], v = x[E->pv];
+  if (E->have) {
+    if (fabs(th - E->pt) <= E->dtt) return 0;
+    const double du = u - E->pu_v, dv = v - E->pv_v;
+    if ((du * du + dv * dv) <= (E->dpt * E->dpt)) return 0;
+  }
+  E->have = 1;
+  E->pt = th;
+  E->pu_v = u;
+  E->pv_v = v;
+  E->found++;
+  E->hit_t[E->stored] = th;
+  memcpy(E->hit_y + 6 * E->stored, x, sizeof(double) * 6);
+  E->stored++;
+  return E->max_hits > 0 && E->stored >= E->max_hits;
+}
+
+int hgo_section_detect(const double* times, const double* states, int m, int axis, double offset, int direction,
+                       int pu, int pv, int segment_refine, int cubic, int newton_max_iter, double tol_on_surface,
+                       double dedup_time_tol, double dedup_point_tol, int max_hits, double* hit_t, double* hit_y,
+                       int* n_stored) {
+  hgo_emit E;
+  memset(&E, 0, sizeof(E));
+  E.max_hits = max_hits;
+  E.pu = pu;
+  E.pv = pv;
+  E.dtt = dedup_time_tol;
+  E.dpt = dedup_point_tol;
+  E.hit_t = hit_t;
+  E.hit_y = hit_y;
+  const int N = m, r = segment_refine;
+  if (r <= 0 || N < 2) {
+    *n_stored = 0;
+    return 0;
+  }
+  const double step = 1.0 / (r + 1);
+#define G(q) (states[6 * (q) + axis] - offset)
+  int stop = 0;
+  for (int k = 0; k < N - 1 && !stop; ++k) {
+    const double t0 = times[k], t1 = times[k + 1], dt = t1 - t0;
+    const double gk = G(k), gk1 = G(k + 1);
+    double d0 = 0.0, d1 = 0.0;
+    const int cub = cubic && dt > 0.0;
+    if (cub) {
+      d0 = (k - 1 >= 0) ? (G(k + 1) - G(k - 1)) / (times[k + 1] - times[k - 1]) : (G(k + 1) - G(k)) / (times[k + 1] - times[k]);
+      d1 = (k + 2 < N) ? (G(k + 2) - G(k)) / (times[k + 2] - times[k]) : (G(k + 1) - G(k)) / (times[k + 1] - times[k]);
+    }
+    int accept_left = 0;
+    if (fabs(gk) < tol_on_surface) {
+      if (direction == 0)
+        accept_left = 1;
+      else if (direction == 1)
+        accept_left = (gk1 >= 0.0) || (k - 1 >= 0 && G(k - 1) <= 0.0);
+      else
+        accept_left = (gk1 <= 0.0) || (k - 1 >= 0 && G(k - 1) >= 0.0);
+      if (accept_left) stop = emit(&E, t0, states + 6 * k);
+    }
+    for (int mm = 0; mm < r + 1 && !stop; ++mm) {
+      const double s_lo = mm * step, s_hi = (mm + 1) * step;
+      if (s_hi > 1.0 + 1e-15) break;
+      if (accept_left && mm == 0) continue;
+      double g_lo, g_hi;
+      if (cub) {
+        g_lo = herm_s(s_lo, gk, gk1, d0, d1, dt);
+        g_hi = herm_s(s_hi, gk, gk1, d0, d1, dt);
+      } else {
+        g_lo = (1.0 - s_lo) * gk + s_lo * gk1;
+        g_hi = (1.0 - s_hi) * gk + s_hi * gk1;
+      }
+      int crosses;
+      if (direction == 0)
+        crosses = (g_lo * g_hi <= 0.0) && (g_lo != g_hi);
+      else if (direction == 1)
+        crosses = (g_lo < 0.0) && (g_hi >= 0.0);
+      else
+        crosses = (g_lo > 0.0) && (g_hi <= 0.0);
+      if (!crosses) continue;
+      double s_star;
+      if (g_lo == g_hi) {
+        s_star = 0.5 * (s_lo + s_hi);
+      } else {
+        double a = g_lo / (g_lo - g_hi);
+        a = (a > 0.0) ? a : 0.0;
+        a = (1.0 < a) ? 1.0 : a;
+        s_star = s_lo + a * (s_hi - s_lo);
+      }
+      if (cub) {
+        for (int it = 0; it < newton_max_iter; ++it) {
+          const double f = herm_s(s_star, gk, gk1, d0, d1, dt);
+          const double df = herm_d(s_star, gk, gk1, d0, d1, dt);
+          if (df == 0.0) break;
+          s_star -= f / df;
+          if (s_star < s_lo) { s_star = s_lo; break; }
+          if (s_star > s_hi) { s_star = s_hi; break; }
+        }
+      }
+      const double th = (1.0 - s_star) * t0 + s_star * t1;
+      double x[6];
+      if (cub && k - 1 >= 0 && k + 2 < N) {
+        const double s = s_star;
+        const double h00 = (1.0 + 2.0 * s) * sq_py(1.0 - s);
+        const double h10 = s * sq_py(1.0 - s);
+        const double h01 = sq_py(s) * (3.0 - 2.0 * s);
+        const double h11 = sq_py(s) * (s - 1.0);
+        for (int c = 0; c < 6; ++c) {
+          const double dxdt0 = (states[6 * (k + 1) + c] - states[6 * (k - 1) + c]) / (times[k + 1] - times[k - 1]);
+          const double dxdt1 = (states[6 * (k + 2) + c] - states[6 * k + c]) / (times[k + 2] - times[k]);
+          x[c] = ((h00 * states[6 * k + c] + (h10 * dxdt0) * dt) + h01 * states[6 * (k + 1) + c]) + (h11 * dxdt1) * dt;
+        }
+      } else {
+        for (int c = 0; c < 6; ++c) x[c] = states[6 * k + c] + s_star * (states[6 * (k + 1) + c] - states[6 * k + c]);
+      }
+      stop = emit(&E, th, x);
+    }
+  }
+#undef G
+  *n_stored = E.stored;
+  return E.found;
+}

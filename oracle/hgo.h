@@ -90,6 +90,15 @@ int hgo_dop853_event(int dim, double mu, int fwd, int flip_lo, int flip_hi,
                      double* hit_t, double* hit_y, int* n_hits,
                      double* t_end, double* y_end, long* n_accept, long* n_reject);
 
+/* Section crossings on one sampled trajectory (plane y[axis] = offset),
+ * poincare/synodic/backend.py:382-659.  times (m,), states (m, 6).  Stores
+ * at most max_hits hits (hit_t (max_hits,), hit_y (max_hits, 6)) and
+ * returns the number accepted. */
+int hgo_section_detect(const double* times, const double* states, int m, int axis, double offset, int direction,
+                       int pu, int pv, int segment_refine, int cubic, int newton_max_iter, double tol_on_surface,
+                       double dedup_time_tol, double dedup_point_tol, int max_hits, double* hit_t, double* hit_y,
+                       int* n_stored);
+
 /* Batched variants over independent trajectories, threaded over `threads`
  * host threads (one trajectory per task).  Arrays are trajectory-major:
  * y0 (N, dim), states (N, n, dim) ... */

@@ -165,6 +165,29 @@ def dop853_event(y0, t0, tmax, mu, ev_index, ev_offset=0.0, ev_dir=0, max_hits=1
                 y_end=y_end, n_accept=na.value, n_reject=nr.value, status=st)
 
 
+def section_detect(times, states, axis, offset=0.0, direction=0, plane=(1, 4), segment_refine=50, cubic=False,
+                   newton_max_iter=10, tol_on_surface=1e-6, dedup_time_tol=1e-9, dedup_point_tol=1e-6,
+                   max_hits=64):
+    """poincare/synodic/backend.py:458-659 on one sampled trajectory."""
+    L = lib()
+    if not hasattr(L, "_sec"):
+        L.hgo_section_detect.argtypes = [_DP, _DP, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                         C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, _DP, _DP,
+                                         _IP]
+        L.hgo_section_detect.restype = C.c_int
+        L._sec = True
+    times = np.ascontiguousarray(times, dtype=np.float64)
+    states = np.ascontiguousarray(states, dtype=np.float64)
+    hit_t = np.zeros(max_hits)
+    hit_y = np.zeros((max_hits, 6))
+    ns = C.c_int(0)
+    L.hgo_section_detect(_p(times), _p(states), len(times), int(axis), float(offset), int(direction), int(plane[0]),
+                         int(plane[1]), int(segment_refine), 1 if cubic else 0, int(newton_max_iter),
+                         float(tol_on_surface), float(dedup_time_tol), float(dedup_point_tol), int(max_hits),
+                         _p(hit_t), _p(hit_y), C.byref(ns))
+    return hit_t[:ns.value], hit_y[:ns.value]
+
+
 def dop853_event_batch(y0, t0, tmax, mu, ev_index, ev_offset=0.0, ev_dir=0, max_hits=1,
                        rtol=1e-12, atol=1e-12, max_step=np.inf, min_step=None, xtol=1e-12,
                        gtol=1e-12, max_steps=10_000_000, fwd=1, flip=None, threads=None):

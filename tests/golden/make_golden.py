@@ -131,6 +131,31 @@ def job_adaptive(args):
     raise ValueError(kind)
 
 
+def job_section(i):
+    """Sampled DOP853 trajectory + the synodic detection backend (linear and cubic)."""
+    from hiten.algorithms.dynamics.base import _propagate_dynsys
+    from hiten.algorithms.poincare.synodic.backend import _SynodicDetectionBackend
+    sysm = _ref()
+    y0 = W.section_states(64, seed=8)[i]
+    sol = _propagate_dynsys(sysm.dynsys, y0, 0.0, 12.0, forward=1, steps=600, method="adaptive", order=8,
+                            rtol=1e-11, atol=1e-11)
+    times, states = np.asarray(sol.times), np.asarray(sol.states)
+    out = {"times": times, "states": states}
+    be = _SynodicDetectionBackend()
+    for kind in ("linear", "cubic"):
+        for name, normal, off, direction, plane in (("y0dn", [0, 1, 0, 0, 0, 0], 0.0, -1, ("x", "vx")),
+                                                     ("xany", [1, 0, 0, 0, 0, 0], float(W.X_L1 if y0[0] < 1 else
+                                                                                        W.X_L2), None, ("y", "vy"))):
+            hits = be.detect_on_trajectory(times, states, normal=np.array(normal, float), offset=off,
+                                           plane_coords=plane, interp_kind=kind, segment_refine=50,
+                                           tol_on_surface=1e-6, dedup_time_tol=1e-9, dedup_point_tol=1e-6,
+                                           max_hits_per_traj=None, newton_max_iter=10, direction=direction)
+            out[f"{kind}_{name}_t"] = np.array([h.time for h in hits], dtype=float)
+            out[f"{kind}_{name}_y"] = np.array([h.state for h in hits], dtype=float).reshape(-1, 6)
+            out[f"{kind}_{name}_off"] = off
+    return i, out
+
+
 def job_crossing(i):
     from hiten.algorithms.poincare.singlehit.backend import _y_plane_crossing
     sysm = _ref()
@@ -165,6 +190,7 @@ def main(ref_src):
                    + [("section", i) for i in range(12)])
         r_ad = pool.map_async(job_adaptive, ad_jobs)
         r_cross = pool.map_async(job_crossing, range(6))
+        r_sec = pool.map_async(job_section, range(8))
         halo_jobs = [(p, az, z) for p in (1, 2) for az in (0.05, 0.2) for z in ("southern", "northern")]
         r_halo = pool.map_async(job_halo, halo_jobs)
 
@@ -185,6 +211,11 @@ def main(ref_src):
         np.savez_compressed(os.path.join(HERE, "crossing.npz"), mu=MU,
                             y0=np.array([c[1] for c in cr]), t=np.array([c[2] for c in cr]),
                             state=np.array([c[3] for c in cr]))
+        sec = {}
+        for i, d in r_sec.get():
+            for k, v in d.items():
+                sec[f"{i}/{k}"] = v
+        np.savez_compressed(os.path.join(HERE, "section.npz"), mu=MU, **sec)
         hr = r_halo.get()
         np.savez_compressed(os.path.join(HERE, "halo.npz"), mu=MU,
                             point=np.array([h[0] for h in hr]), az=np.array([h[1] for h in hr]),
