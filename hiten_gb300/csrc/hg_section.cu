@@ -47,7 +47,7 @@ __device__ __forceinline__ double smp(const SecParams& p, int q, int c, int i) {
   return p.samples[((long long)q * 6 + c) * p.ld + i];
 }
 __device__ __forceinline__ double tim(const SecParams& p, int q, int i) {
-  return p.times[(long long)q * p.times_ld + (p.times_ld ? i : 0)];
+  return p.times_ld ? p.times[(long long)q * p.times_ld + i] : p.times[q];
 }
 
 // poincare/utils.py:53-147 (_hermite_scalar, _hermite_der: squares as x*x,
@@ -235,7 +235,55 @@ __global__ void __launch_bounds__(128) section_kernel(SecParams p) {
   if (p.n_found) p.n_found[i] = em.found;
 }
 
+// Manifold acceptance filters on sampled trajectories
+// (types/services/manifold.py:412-432): minimum distances to the primaries
+// (np.sqrt((x + mu)**2 + y**2 + z**2), numpy squares being x*x) and the
+// maximum relative Jacobi-constant drift of common/energy.py:26-74
+// (numba: squares x*x, **0.5 of a positive number = the correctly rounded
+// square root).  One thread per trajectory.
+__global__ void __launch_bounds__(128) filters_kernel(int N, int m, const double* samples, long long ld, double mu,
+                                                       double* min_r1, double* min_r2, double* max_rel_e) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const double mu1 = 1.0 - mu, mu2 = mu;
+  double C0 = 0.0, absC0 = 0.0, emax = 0.0, m1 = 0.0, m2 = 0.0;
+  for (int q = 0; q < m; ++q) {
+    const double* s = samples + (long long)q * 6 * ld + i;
+    const double x = s[0], y = s[ld], z = s[2 * ld], vx = s[3 * ld], vy = s[4 * ld], vz = s[5 * ld];
+    const double a = x + mu, b = (x - 1.0) + mu;
+    const double d1 = sqrt((a * a + y * y) + z * z);
+    const double d2 = sqrt((b * b + y * y) + z * z);
+    m1 = (q == 0 || d1 < m1) ? d1 : m1;
+    m2 = (q == 0 || d2 < m2) ? d2 : m2;
+    const double e = x + mu2, f = x - mu1;
+    const double r1 = sqrt((e * e + y * y) + z * z);
+    const double r2 = sqrt((f * f + y * y) + z * z);
+    const double C = ((x * x + y * y) + 2.0 * (mu1 / r1 + mu2 / r2)) - ((vx * vx + vy * vy) + vz * vz);
+    if (q == 0) {
+      C0 = C;
+      absC0 = fabs(C0);
+    } else {
+      const double rel = absC0 > 1e-14 ? fabs(C - C0) / absC0 : fabs(C - C0);
+      if (rel > emax) emax = rel;
+    }
+  }
+  min_r1[i] = m1;
+  min_r2[i] = m2;
+  max_rel_e[i] = emax;
+}
+
 }  // namespace
+
+extern "C" int hg_trajectory_filters(int N, int m, const double* samples, long long ld, double mu, double* min_r1,
+                                     double* min_r2, double* max_rel_energy, void* stream) {
+  if (N < 0 || m < 1 || ld < N) return HG_ERR_ARGS;
+  if (N > 0 && (!samples || !min_r1 || !min_r2 || !max_rel_energy)) return HG_ERR_ARGS;
+  if (N == 0) return HG_OK;
+  const int block = 128;
+  filters_kernel<<<(N + block - 1) / block, block, 0, (cudaStream_t)stream>>>(N, m, samples, ld, mu, min_r1, min_r2,
+                                                                              max_rel_energy);
+  return cudaGetLastError() == cudaSuccess ? HG_OK : HG_ERR_CUDA;
+}
 
 extern "C" int hg_section_detect(int N, int m, const double* samples, long long ld, const double* times,
                                  long long times_ld, int axis, double offset, int direction, int plane_u,

@@ -60,6 +60,62 @@ def seeds(times, PHI, period, fractions, displacements, eigvec, direction=1):
     return out
 
 
+def trajectory_filters(samples, mu, device=None):
+    """(min r1, min r2, max relative Jacobi drift) of every sampled trajectory
+    (samples (m, N, 6)), on the GPU (types/services/manifold.py:412-432,
+    common/energy.py:26-74)."""
+    import ctypes as C
+
+    from . import _lib
+    dev = P._device(device)
+    S = torch.as_tensor(samples, dtype=torch.float64, device=dev)
+    m, N, _ = S.shape
+    soa = S.permute(0, 2, 1).contiguous()
+    out = torch.empty((3, max(N, 1)), dtype=torch.float64, device=dev)
+    rc = _lib.load().hg_trajectory_filters(N, m, C.c_void_p(soa.data_ptr()), N, float(mu),
+                                           C.c_void_p(out[0].data_ptr()), C.c_void_p(out[1].data_ptr()),
+                                           C.c_void_p(out[2].data_ptr()),
+                                           C.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    if rc != _lib.HG_OK:
+        raise _lib.HitenGpuError(rc, "hg_trajectory_filters")
+    return out[0, :N], out[1, :N], out[2, :N]
+
+
+def compute(x0, period, mu, stable=True, direction=1, step=0.02, integration_fraction=0.75, NN=1,
+            displacement=1e-6, dt=1e-3, method="adaptive", order=8, energy_tol=1e-6, safe_r1=0.0, safe_r2=0.0,
+            displacements=None, device=None):
+    """Manifold.compute / _ManifoldDynamicsService._run_compute
+    (types/services/manifold.py:293-442), with every seed propagated in one
+    batched GPU call instead of a Python loop.
+
+    forward = -1 for the stable manifold; seeds at fractions arange(0, 1, step)
+    of the period (times the optional `displacements` array for a grid of
+    displacement magnitudes); trajectories sampled at
+    linspace(0, tf, max(int(tf/dt)+1, 100)) with tf = integration_fraction*2*pi;
+    rejected when they come within safe_r1/safe_r2 of a primary or drift in
+    Jacobi constant by more than energy_tol.  Returns the reference's tuple
+    (ysos, dysos, states_list, times_list, successes, attempts)."""
+    if method != "adaptive" or order != 8:
+        raise NotImplementedError("manifold propagation on the GPU path is DOP853")
+    forward = -1 if stable else 1
+    times, PHI = stm_grid(x0, period, mu, steps=2000, forward=forward, device=device)
+    eigvec = stable_eigvec(PHI[-1, :36].reshape(6, 6), stable=stable)
+    fractions = np.arange(0.0, 1.0, step)
+    disps = np.atleast_1d(displacement if displacements is None else displacements)
+    seeds_arr = seeds(times, PHI, period, fractions, disps, eigvec, direction=direction)
+    tf = integration_fraction * 2 * np.pi
+    steps = max(int(abs(tf) / dt) + 1, 100)
+    r = P.propagate_dop853(seeds_arr, 0.0, tf, mu, rtol=1e-12, atol=1e-12, max_step=1e4, fwd=forward,
+                           flip=(0, 6), n_samples=steps, device=device)
+    r1, r2, de = trajectory_filters(r.samples, mu, device=device)
+    ok = ((r1 >= safe_r1) & (r2 >= safe_r2) & (de <= energy_tol) & (r.status == 0)).cpu().numpy()
+    S = r.samples.permute(1, 0, 2).cpu().numpy()
+    t_signed = forward * np.linspace(0.0, tf, steps)
+    states_list = [S[i] for i in np.nonzero(ok)[0]]
+    times_list = [t_signed.copy() for _ in states_list]
+    return [], [], states_list, times_list, int(ok.sum()), len(seeds_arr)
+
+
 def propagate_to_plane(seeds_arr, mu, tf=8.0, forward=-1, plane_index=0, plane_offset=None, rtol=1e-12,
                        atol=1e-12, max_hits=1, device=None):
     """DOP853 from every seed to |t| = tf or the first crossing of

@@ -160,6 +160,14 @@ int hg_section_detect(int N, int m, const double* samples, long long ld,
                       int max_hits, double* hit_t, double* hit_y, int* n_hits, int* n_found,
                       void* stream);
 
+/* Manifold acceptance filters on sampled trajectories: per trajectory the
+ * minimum distances to the primaries and the maximum relative drift of the
+ * Jacobi constant over the samples ([m][6][ld]).
+ * Replaces: types/services/manifold.py:412-432 (body-radius filter) and
+ * common/energy.py:26-74 (_max_rel_energy_error). */
+int hg_trajectory_filters(int N, int m, const double* samples, long long ld, double mu,
+                          double* min_r1, double* min_r2, double* max_rel_energy, void* stream);
+
 /* Launch-shape tuning of a handle (set by hiten_gb300.autotune).
  * HG_TUNE_BLOCK_THREADS: threads per block, 32 (default), 64 or 128.
  * HG_TUNE_DOP853_LANES_D6: lanes per 6-dim DOP853 trajectory: 1 (one
