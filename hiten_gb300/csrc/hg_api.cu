@@ -57,8 +57,50 @@ template <int ORDER, int G>
 int launch_fixed(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
   const int tpb = (h->block / 32) * hg::Layout<G>::TPW;  // trajectories per block
   const int grid = (p.N + tpb - 1) / tpb;
-  if (grid > 0) hg::fixed_rk_kernel<ORDER, G><<<grid, h->block, 0, s>>>(p);
+  if (grid > 0) {
+    if (p.ev_index >= 0)
+      hg::fixed_rk_event_kernel<ORDER, G><<<grid, h->block, 0, s>>>(p);
+    else
+      hg::fixed_rk_kernel<ORDER, G><<<grid, h->block, 0, s>>>(p);
+  }
   return check_launch(h, "fixed_rk_kernel");
+}
+
+int fixed_common(hg_handle* h, double mu, int order, int dim, int N, const double* y0, long long ld_in,
+                 const double* t_vals, int n_nodes, int out_every, double* y_out, long long ld_out, int fwd,
+                 int flip_lo, int flip_hi, int* status, hg::FixedParams& p) {
+  if (order != 4 && order != 6 && order != 8) return fail(h, HG_ERR_ARGS, "order must be 4, 6 or 8 (got %d)", order);
+  if (dim != 6 && dim != 42) return fail(h, HG_ERR_ARGS, "dim must be 6 or 42 (got %d)", dim);
+  if (N < 0 || n_nodes < 1 || out_every < 1) return fail(h, HG_ERR_ARGS, "bad sizes");
+  if (ld_in < N || ld_out < N) return fail(h, HG_ERR_ARGS, "leading dimension < N");
+  if (N > 0 && (!y0 || !t_vals || !y_out)) return fail(h, HG_ERR_ARGS, "null array");
+  if (flip_lo < 0 || flip_hi > dim || flip_lo > flip_hi) return fail(h, HG_ERR_ARGS, "bad flip range");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, HG_ERR_CUDA, "cudaSetDevice");
+  memset(&p, 0, sizeof(p));
+  p.N = N;
+  p.mu = mu;
+  p.dir = make_dir(dim, fwd, flip_lo, flip_hi);
+  p.y0 = y0;
+  p.ld_in = ld_in;
+  p.t_vals = t_vals;
+  p.n = n_nodes;
+  p.out_every = out_every;
+  p.out = y_out;
+  p.ld_out = ld_out;
+  p.status = status;
+  p.ev_index = -1;
+  return HG_OK;
+}
+
+int fixed_dispatch(hg_handle* h, int order, int dim, const hg::FixedParams& p, cudaStream_t s) {
+  if (dim == 6) {
+    if (order == 4) return launch_fixed<4, 1>(h, p, s);
+    if (order == 6) return launch_fixed<6, 1>(h, p, s);
+    return launch_fixed<8, 1>(h, p, s);
+  }
+  if (order == 4) return launch_fixed<4, 7>(h, p, s);
+  if (order == 6) return launch_fixed<6, 7>(h, p, s);
+  return launch_fixed<8, 7>(h, p, s);
 }
 
 template <int G>
@@ -145,34 +187,34 @@ int hg_propagate_fixed(hg_handle* h, double mu, int order, int dim, int N, const
                        const double* t_vals, int n_nodes, int out_every, double* y_out, long long ld_out, int fwd,
                        int flip_lo, int flip_hi, int* status, void* stream) {
   if (!h) return HG_ERR_ARGS;
-  if (order != 4 && order != 6 && order != 8) return fail(h, HG_ERR_ARGS, "order must be 4, 6 or 8 (got %d)", order);
-  if (dim != 6 && dim != 42) return fail(h, HG_ERR_ARGS, "dim must be 6 or 42 (got %d)", dim);
-  if (N < 0 || n_nodes < 1 || out_every < 1) return fail(h, HG_ERR_ARGS, "bad sizes");
-  if (ld_in < N || ld_out < N) return fail(h, HG_ERR_ARGS, "leading dimension < N");
-  if (N > 0 && (!y0 || !t_vals || !y_out)) return fail(h, HG_ERR_ARGS, "null array");
-  if (flip_lo < 0 || flip_hi > dim || flip_lo > flip_hi) return fail(h, HG_ERR_ARGS, "bad flip range");
-  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, HG_ERR_CUDA, "cudaSetDevice");
   hg::FixedParams p;
-  p.N = N;
-  p.mu = mu;
-  p.dir = make_dir(dim, fwd, flip_lo, flip_hi);
-  p.y0 = y0;
-  p.ld_in = ld_in;
-  p.t_vals = t_vals;
-  p.n = n_nodes;
-  p.out_every = out_every;
-  p.out = y_out;
-  p.ld_out = ld_out;
-  p.status = status;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (dim == 6) {
-    if (order == 4) return launch_fixed<4, 1>(h, p, s);
-    if (order == 6) return launch_fixed<6, 1>(h, p, s);
-    return launch_fixed<8, 1>(h, p, s);
-  }
-  if (order == 4) return launch_fixed<4, 7>(h, p, s);
-  if (order == 6) return launch_fixed<6, 7>(h, p, s);
-  return launch_fixed<8, 7>(h, p, s);
+  const int rc = fixed_common(h, mu, order, dim, N, y0, ld_in, t_vals, n_nodes, out_every, y_out, ld_out, fwd, flip_lo,
+                              flip_hi, status, p);
+  if (rc != HG_OK) return rc;
+  return fixed_dispatch(h, order, dim, p, (cudaStream_t)stream);
+}
+
+int hg_propagate_fixed_event(hg_handle* h, double mu, int order, int dim, int N, const double* y0, long long ld_in,
+                             const double* t_vals, int n_nodes, int out_every, double* y_out, long long ld_out,
+                             int fwd, int flip_lo, int flip_hi, const hg_event* ev, double* hit_t, double* hit_y,
+                             int* n_hits, int* status, void* stream) {
+  if (!h) return HG_ERR_ARGS;
+  hg::FixedParams p;
+  const int rc = fixed_common(h, mu, order, dim, N, y0, ld_in, t_vals, n_nodes, out_every, y_out, ld_out, fwd, flip_lo,
+                              flip_hi, status, p);
+  if (rc != HG_OK) return rc;
+  if (!ev || ev->index < 0 || ev->index >= dim) return fail(h, HG_ERR_ARGS, "event index out of range");
+  if (ev->direction < -1 || ev->direction > 1) return fail(h, HG_ERR_ARGS, "bad event direction");
+  if (N > 0 && (!hit_t || !hit_y || !n_hits)) return fail(h, HG_ERR_ARGS, "hit buffers are null");
+  p.ev_index = ev->index;
+  p.ev_offset = ev->offset;
+  p.ev_dir = ev->direction;
+  p.xtol = ev->xtol;
+  p.gtol = ev->gtol;
+  p.hit_t = hit_t;
+  p.hit_y = hit_y;
+  p.n_hits = n_hits;
+  return fixed_dispatch(h, order, dim, p, (cudaStream_t)stream);
 }
 
 int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y0, long long ld,

@@ -493,7 +493,128 @@ struct FixedParams {
   double* out;        // [n_out][D][ld_out]
   long long ld_out;
   int* status;        // [N] or null
+  // optional terminal plane event g = y[ev_index] - ev_offset (ev_index < 0: none)
+  int ev_index;
+  double ev_offset;
+  int ev_dir;
+  double xtol, gtol;
+  double* hit_t;  // [ld_out]
+  double* hit_y;  // [D][ld_out]
+  int* n_hits;    // [N]
 };
+
+// _hermite_eval_dense (integrators/rk.py:286-327) for one component.
+__device__ __forceinline__ double hermite_eval(double y0, double f0, double y1, double f1, double x, double h) {
+  const double x2 = x * x;
+  const double x3 = x2 * x;
+  const double H00 = (2.0 * x3 - 3.0 * x2) + 1.0;
+  const double H10 = (x3 - 2.0 * x2) + x;
+  const double H01 = -2.0 * x3 + 3.0 * x2;
+  const double H11 = x3 - x2;
+  return ((H00 * y0 + H10 * (h * f0)) + H01 * y1) + H11 * (h * f1);
+}
+
+// Fixed step with a terminal plane event: integrators/rk.py:655-718
+// (_integrate_fixed_rk_until_event) and :330-391 (_hermite_refine_in_step).
+// Each step also evaluates f(y_{n+1}) for the cubic Hermite interpolant;
+// rows after the crossing are not written (the reference returns
+// [y0, y_hit] only).
+template <int ORDER, int G>
+__global__ void __launch_bounds__(128) fixed_rk_event_kernel(FixedParams p) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  Layout<G> L;
+  int traj;
+  if constexpr (G == 1) {
+    L.role = 6;
+    traj = warp * 32 + lane;
+  } else {
+    if (lane >= 28) return;
+    const int g = lane / 7;
+    L.role = lane % 7;
+    L.base = g * 7;
+    L.gmask = 0x7Fu << L.base;
+    traj = warp * 4 + g;
+  }
+  if (traj >= p.N) return;
+  const bool leader = (G == 1) || L.role == 6;
+  int ev_r = L.local(p.ev_index);
+  bool ev_mine = true;
+  int ev_src = lane;
+  if constexpr (G == 7) {
+    ev_mine = (L.role == L.owner(p.ev_index));
+    ev_src = L.base + L.owner(p.ev_index);
+  }
+  auto bcast = [&](double v) -> double {
+    if constexpr (G == 1)
+      return v;
+    else
+      return __shfl_sync(L.gmask, v, ev_src);
+  };
+  double y[6];
+#pragma unroll
+  for (int r = 0; r < 6; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld_in + traj];
+#pragma unroll
+  for (int r = 0; r < 6; ++r) p.out[(long long)L.comp(r) * p.ld_out + traj] = y[r];
+  const long long row = (long long)Layout<G>::D * p.ld_out;
+  double f_prev[6];
+  L.rhs(y, p.mu, p.dir, f_prev);
+  double g_prev = bcast(ev_mine ? (pick<6>(y, ev_r) - p.ev_offset) : 0.0);
+  bool finite = true;
+  int hit = 0;
+  for (int idx = 0; idx < p.n - 1; ++idx) {
+    const double t_n = p.t_vals[idx];
+    const double h = p.t_vals[idx + 1] - t_n;
+    double yn[6], f_new[6];
+    rk_fixed_step<ORDER, G>(L, y, h, p.mu, p.dir, yn);
+    L.rhs(yn, p.mu, p.dir, f_new);
+    const double g_new = bcast(ev_mine ? (pick<6>(yn, ev_r) - p.ev_offset) : 0.0);
+    if (event_crossed(g_prev, g_new, p.ev_dir)) {
+      const double ye = pick<6>(y, ev_r), fe0 = pick<6>(f_prev, ev_r), ye1 = pick<6>(yn, ev_r),
+                   fe1 = pick<6>(f_new, ev_r);
+      double a = 0.0, b = 1.0, g_left = g_prev, x_hit = -1.0;
+      for (int it = 0; it < 128; ++it) {
+        const double mid = 0.5 * (a + b);
+        const double g_mid = bcast(ev_mine ? (hermite_eval(ye, fe0, ye1, fe1, mid, h) - p.ev_offset) : 0.0);
+        if (fabs(g_mid) <= p.gtol) {
+          x_hit = mid;
+          break;
+        }
+        if (crossed_direction(g_left, g_mid, p.ev_dir)) {
+          b = mid;
+        } else {
+          a = mid;
+          g_left = g_mid;
+        }
+        if ((b - a) * fabs(h) <= p.xtol) break;
+      }
+      if (x_hit < 0.0) x_hit = b;
+      if (leader) p.hit_t[traj] = t_n + x_hit * h;
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+        p.hit_y[(long long)L.comp(r) * p.ld_out + traj] = hermite_eval(y[r], f_prev[r], yn[r], f_new[r], x_hit, h);
+      hit = 1;
+      break;
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      y[r] = yn[r];
+      f_prev[r] = f_new[r];
+      finite = finite && finite_bits(yn[r]);
+    }
+    g_prev = g_new;
+    if ((idx + 1) % p.out_every == 0) {
+      double* o = p.out + (long long)((idx + 1) / p.out_every) * row;
+#pragma unroll
+      for (int r = 0; r < 6; ++r) o[(long long)L.comp(r) * p.ld_out + traj] = y[r];
+    }
+  }
+  if constexpr (G == 7) finite = __all_sync(L.gmask, finite);
+  if (leader) {
+    p.n_hits[traj] = hit;
+    if (p.status) p.status[traj] = finite ? HG_OK : HG_NONFINITE;
+  }
+}
 
 template <int ORDER, int G>
 __global__ void __launch_bounds__(128) fixed_rk_kernel(FixedParams p) {

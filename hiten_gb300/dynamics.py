@@ -110,7 +110,13 @@ def propagate_dynsys(dynsys, state0, t0, tf, forward=1, steps=1000, method="adap
         ev = P.EventSpec(index=int(event_fn.index), offset=float(event_fn.offset), direction=int(cfg.direction),
                          max_hits=1, xtol=float(opt.xtol), gtol=float(opt.gtol))
         if method == "fixed":
-            raise NotImplementedError("fixed-step integration with events is not on the GPU path")
+            out, ht, hy, nh = P.propagate_fixed_event(Y0, t_eval, dynsys.mu, ev, order=order, fwd=fwd, flip=flip)
+            hit = nh.cpu().numpy() > 0
+            times = np.stack([np.full(len(Y0), t_eval[0]), np.where(hit, ht.cpu().numpy(), t_eval[-1])], axis=1)
+            last = np.where(hit[:, None], hy.cpu().numpy(), out[-1].cpu().numpy())
+            states = np.stack([Y0, last], axis=1)
+            times = times * fwd
+            return Solution(times[0] if single else times, states[0] if single else states)
         r = P.propagate_dop853(Y0, float(t_eval[0]), float(t_eval[-1]), dynsys.mu, rtol=kwargs.get("rtol", 1e-12),
                                atol=kwargs.get("atol", 1e-12), max_step=kwargs.get("max_step", 1e4), fwd=fwd,
                                flip=flip, event=ev)

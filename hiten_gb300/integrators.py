@@ -63,10 +63,21 @@ class GpuFixedRK(_GpuIntegrator):
         c = self._constant(y0, t_vals)
         if c is not None:
             return c
-        if event_fn is not None:
-            raise NotImplementedError("fixed-step integration with events is not on the GPU path")
         fwd, flip = self._dir(system)
         Y = np.atleast_2d(y0)
+        if event_fn is not None:
+            cfg = event_cfg or EventConfig()
+            opt = event_options or EventOptions()
+            ev = P.EventSpec(index=int(event_fn.index), offset=float(event_fn.offset), direction=int(cfg.direction),
+                             max_hits=1, xtol=float(opt.xtol), gtol=float(opt.gtol))
+            out, ht, hy, nh = P.propagate_fixed_event(Y, t_vals, system.mu, ev, order=self.order, fwd=fwd, flip=flip)
+            hit = nh.cpu().numpy() > 0
+            times = np.stack([np.full(len(Y), t_vals[0]), np.where(hit, ht.cpu().numpy(), t_vals[-1])], axis=1)
+            last = np.where(hit[:, None], hy.cpu().numpy(), out[-1].cpu().numpy())
+            states = np.stack([Y, last], axis=1)
+            if y0.ndim == 1:
+                return Solution(times=times[0], states=states[0])
+            return Solution(times=times, states=states)
         out = P.propagate_fixed(Y, t_vals, system.mu, order=self.order, fwd=fwd, flip=flip).permute(1, 0, 2)
         st = out.cpu().numpy()
         return Solution(times=t_vals.copy(), states=st[0] if y0.ndim == 1 else st)

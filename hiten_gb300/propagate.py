@@ -81,6 +81,35 @@ def propagate_fixed(y0, t_vals, mu, order=8, out_every=1, fwd=1, flip=None, devi
     return res
 
 
+def propagate_fixed_event(y0, t_vals, mu, event, order=8, out_every=1, fwd=1, flip=None, device=None):
+    """Fixed-step RK with a terminal plane event (integrators/rk.py:655-718).
+
+    Returns (states (n_out, N, dim) -- rows after a crossing unwritten --,
+    hit_t (N,), hit_y (N, dim), n_hits (N,))."""
+    dev = _device(device)
+    y0 = torch.as_tensor(y0, dtype=torch.float64)
+    dim = int(y0.shape[-1])
+    Y0 = _to_soa(y0, dim, dev)
+    N = Y0.shape[1]
+    ld = max(N, 1)
+    tv = torch.as_tensor(np.ascontiguousarray(np.asarray(t_vals, dtype=np.float64))).to(dev)
+    n = int(tv.numel())
+    n_out = (n - 1) // int(out_every) + 1
+    out = torch.full((n_out, dim, ld), float("nan"), dtype=torch.float64, device=dev)
+    hit_t = torch.full((ld,), float("nan"), dtype=torch.float64, device=dev)
+    hit_y = torch.full((dim, ld), float("nan"), dtype=torch.float64, device=dev)
+    n_hits = torch.zeros(ld, dtype=torch.int32, device=dev)
+    lo, hi = _flip(dim, fwd, flip)
+    evp = _lib.hg_event(int(event.index), float(event.offset), int(event.direction), 1, float(event.xtol),
+                        float(event.gtol))
+    H = _lib.handle(dev.index or 0)
+    with torch.cuda.device(dev):
+        H.check(H.lib.hg_propagate_fixed_event(H.ptr, float(mu), int(order), dim, N, _ptr(Y0), ld, _ptr(tv), n,
+                                               int(out_every), _ptr(out), ld, int(fwd), lo, hi, C.byref(evp),
+                                               _ptr(hit_t), _ptr(hit_y), _ptr(n_hits), None, _stream(dev)))
+    return out[:, :, :N].permute(0, 2, 1), hit_t[:N], hit_y[:, :N].t(), n_hits[:N]
+
+
 @dataclass
 class EventSpec:
     """Plane event g(y) = y[index] - offset (integrators/utils.py:13-123)."""

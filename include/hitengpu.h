@@ -91,6 +91,22 @@ int hg_propagate_fixed(hg_handle* h, double mu, int order, int dim, int N,
                        int fwd, int flip_lo, int flip_hi,
                        int* status, void* stream);
 
+/* hg_propagate_fixed with a terminal plane event (ev required; max_hits is
+ * ignored: the first crossing ends the trajectory).  Each step also
+ * evaluates f(y_{n+1}); on a sign change the crossing is bisected on the
+ * cubic Hermite interpolant of the step.  Rows of y_out after the crossing
+ * are not written.  Outputs: hit_t [ld_out], hit_y [dim][ld_out],
+ * n_hits [N] (0 or 1), status [N] (nullable).
+ * Replaces: integrators/rk.py:655-718 (_integrate_fixed_rk_until_event)
+ * and :286-391 (_hermite_eval_dense, _hermite_refine_in_step). */
+int hg_propagate_fixed_event(hg_handle* h, double mu, int order, int dim, int N,
+                             const double* y0, long long ld_in,
+                             const double* t_vals, int n_nodes, int out_every,
+                             double* y_out, long long ld_out,
+                             int fwd, int flip_lo, int flip_hi, const hg_event* ev,
+                             double* hit_t, double* hit_y, int* n_hits,
+                             int* status, void* stream);
+
 /* Adaptive DOP853 on dim 6 or 42 from t0 to tmax (per trajectory arrays
  * t0_arr/tmax_arr of length N, or NULL to use the scalars).
  * Optional plane event ev (NULL = none).  Optional dense samples at

@@ -620,6 +620,68 @@ int hgo_dop853_dense(int dim, double mu, int fwd, int flip_lo, int flip_hi, cons
   return status;
 }
 
+/* _hermite_eval_dense, integrators/rk.py:286-327 */
+static double hermite_eval(double y0, double f0, double y1, double f1, double x, double h) {
+  const double x2 = x * x;
+  const double x3 = x2 * x;
+  const double H00 = (2.0 * x3 - 3.0 * x2) + 1.0;
+  const double H10 = (x3 - 2.0 * x2) + x;
+  const double H01 = -2.0 * x3 + 3.0 * x2;
+  const double H11 = x3 - x2;
+  return ((H00 * y0 + H10 * (h * f0)) + H01 * y1) + H11 * (h * f1);
+}
+
+/* _integrate_fixed_rk_until_event (integrators/rk.py:655-718) with
+ * _hermite_refine_in_step (:330-391); plane g = y[ev_index] - ev_offset.
+ * Returns 1 on a crossing (t_hit, y_hit set), 0 otherwise; states (n, dim)
+ * rows are written up to the step before the crossing. */
+int hgo_fixed_rk_event(int order, int dim, double mu, int fwd, int flip_lo, int flip_hi, const double* y0,
+                       const double* t_vals, int n, int ev_index, double ev_offset, int ev_dir, double xtol,
+                       double gtol, double* states, double* t_hit, double* y_hit) {
+  hgo_tab T;
+  if (!get_fixed_tab(order, &T) || (dim != 6 && dim != 42) || n < 1) return -1;
+  hgo_sys S = {dim, mu, fwd, flip_lo, flip_hi};
+  double k[13][MAXD], f_prev[MAXD], f_new[MAXD], yn[MAXD];
+  memcpy(states, y0, sizeof(double) * dim);
+  sys_rhs(&S, y0, f_prev);
+  double g_prev = y0[ev_index] - ev_offset;
+  for (int idx = 0; idx < n - 1; ++idx) {
+    const double t_n = t_vals[idx];
+    const double h = t_vals[idx + 1] - t_n;
+    const double* y = states + (size_t)idx * dim;
+    rk_step(&S, &T, y, h, k, yn);
+    sys_rhs(&S, yn, f_new);
+    const double g_new = yn[ev_index] - ev_offset;
+    if (event_crossed(g_prev, g_new, ev_dir)) {
+      double a = 0.0, b = 1.0, g_left = g_prev, x_hit = -1.0;
+      const int e = ev_index;
+      for (int it = 0; it < 128; ++it) {
+        const double mid = 0.5 * (a + b);
+        const double g_mid = hermite_eval(y[e], f_prev[e], yn[e], f_new[e], mid, h) - ev_offset;
+        if (fabs(g_mid) <= gtol) {
+          x_hit = mid;
+          break;
+        }
+        if (crossed_direction(g_left, g_mid, ev_dir)) {
+          b = mid;
+        } else {
+          a = mid;
+          g_left = g_mid;
+        }
+        if ((b - a) * fabs(h) <= xtol) break;
+      }
+      if (x_hit < 0.0) x_hit = b;
+      *t_hit = t_n + x_hit * h;
+      for (int d = 0; d < dim; ++d) y_hit[d] = hermite_eval(y[d], f_prev[d], yn[d], f_new[d], x_hit, h);
+      return 1;
+    }
+    memcpy(states + (size_t)(idx + 1) * dim, yn, sizeof(double) * dim);
+    memcpy(f_prev, f_new, sizeof(double) * dim);
+    g_prev = g_new;
+  }
+  return 0;
+}
+
 /* ---------------------------------------------------------------------------
  * Threaded batches (one trajectory per task)
  * ------------------------------------------------------------------------- */

@@ -90,6 +90,12 @@ int hgo_dop853_event(int dim, double mu, int fwd, int flip_lo, int flip_hi,
                      double* hit_t, double* hit_y, int* n_hits,
                      double* t_end, double* y_end, long* n_accept, long* n_reject);
 
+/* Fixed step with a terminal plane event, integrators/rk.py:655-718.
+ * Returns 1 on a crossing (t_hit, y_hit (dim,)), 0 without, -1 on bad args. */
+int hgo_fixed_rk_event(int order, int dim, double mu, int fwd, int flip_lo, int flip_hi, const double* y0,
+                       const double* t_vals, int n, int ev_index, double ev_offset, int ev_dir, double xtol,
+                       double gtol, double* states, double* t_hit, double* y_hit);
+
 /* Section crossings on one sampled trajectory (plane y[axis] = offset),
  * poincare/synodic/backend.py:382-659.  times (m,), states (m, 6).  Stores
  * at most max_hits hits (hit_t (max_hits,), hit_y (max_hits, 6)) and

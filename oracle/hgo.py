@@ -165,6 +165,28 @@ def dop853_event(y0, t0, tmax, mu, ev_index, ev_offset=0.0, ev_dir=0, max_hits=1
                 y_end=y_end, n_accept=na.value, n_reject=nr.value, status=st)
 
 
+def fixed_rk_event(order, y0, t_vals, mu, ev_index, ev_offset=0.0, ev_dir=0, xtol=1e-12, gtol=1e-12, fwd=1,
+                   flip=None):
+    """integrators/rk.py:655-718 on one trajectory: (hit, t_hit, y_hit, states)."""
+    L = lib()
+    if not hasattr(L, "_fre"):
+        L.hgo_fixed_rk_event.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, _DP, _DP, C.c_int,
+                                         C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, _DP, _DP, _DP]
+        L.hgo_fixed_rk_event.restype = C.c_int
+        L._fre = True
+    y0 = np.ascontiguousarray(y0, dtype=np.float64)
+    t_vals = np.ascontiguousarray(t_vals, dtype=np.float64)
+    dim = y0.size
+    lo, hi = _flip(dim, fwd, flip)
+    states = np.full((t_vals.size, dim), np.nan)
+    th = C.c_double(np.nan)
+    yh = np.full(dim, np.nan)
+    hit = L.hgo_fixed_rk_event(int(order), dim, float(mu), int(fwd), lo, hi, _p(y0), _p(t_vals), t_vals.size,
+                               int(ev_index), float(ev_offset), int(ev_dir), float(xtol), float(gtol), _p(states),
+                               C.byref(th), _p(yh))
+    return hit, th.value, yh, states
+
+
 def section_detect(times, states, axis, offset=0.0, direction=0, plane=(1, 4), segment_refine=50, cubic=False,
                    newton_max_iter=10, tol_on_surface=1e-6, dedup_time_tol=1e-9, dedup_point_tol=1e-6,
                    max_hits=64):

@@ -118,6 +118,15 @@ def job_adaptive(args):
                                 flip_indices=slice(0, 6), rtol=1e-12, atol=1e-12, event_fn=g,
                                 event_cfg=EventConfig(direction=0, terminal=True))
         return kind, i, y0, np.asarray(sol.times), np.asarray(sol.states)
+    if kind == "fixed_event":
+        y0 = W.section_states(64, seed=9)[i]
+
+        def g(t, y):
+            return float(y[1])
+
+        sol = _propagate_dynsys(sysm.dynsys, y0, 0.0, 6.0, forward=1, steps=601, method="fixed", order=8,
+                                event_fn=g, event_cfg=EventConfig(direction=-1, terminal=True))
+        return kind, i, y0, np.asarray(sol.times), np.asarray(sol.states)
     if kind == "section":
         y0 = W.section_states(64, seed=7)[i]
 
@@ -187,7 +196,7 @@ def main(ref_src):
         r_fixed = pool.map_async(job_fixed, fixed_jobs)
         ad_jobs = ([("stm_halo", 0), ("stm_halo", 1)] + [("dense6", i) for i in range(4)]
                    + [(k, i) for k in ("manifold_fwd", "manifold_bwd") for i in range(4)]
-                   + [("section", i) for i in range(12)])
+                   + [("section", i) for i in range(12)] + [("fixed_event", i) for i in range(6)])
         r_ad = pool.map_async(job_adaptive, ad_jobs)
         r_cross = pool.map_async(job_crossing, range(6))
         r_sec = pool.map_async(job_section, range(8))

@@ -83,6 +83,10 @@ def test_adaptive_bit_exact(py_oracle, case):
             assert r["hit_t"][0] * fwd == t[-1] and np.array_equal(r["hit_y"][0], S[-1])
         else:
             assert t[-1] == 8.0 * fwd and np.array_equal(r["y_end"], S[-1])
+    elif kind == "fixed_event":
+        hit, th, yh, _ = py_oracle.fixed_rk_event(8, y0, np.linspace(0.0, 6.0, 601), mu, 1, 0.0, -1)
+        assert hit == 1
+        assert th == t[-1] and np.array_equal(yh, S[-1])
     else:  # section: y = 0, decreasing
         r = py_oracle.dop853_event(y0, 0.0, 20.0, mu, 1, 0.0, -1, 1, rtol=1e-11, atol=1e-11, max_step=1e4)
         assert r["n_hits"] == 1
