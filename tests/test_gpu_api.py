@@ -35,10 +35,18 @@ def test_adaptive_dense_and_stm_vs_golden(gpu, oracle):
     for i in range(4):
         y0 = a[f"dense6/{i}/y0"]
         sol = D.propagate_dynsys(D.CR3BPSystem(MU, 6), y0, 0.0, 4.0, steps=101, rtol=1e-11, atol=1e-11)
-        assert rowwise_rel(sol.states, a[f"dense6/{i}/states"]) <= 1e-9
         oracle.set_mode(oracle.MODE_DEVICE)
         ref, _, _, _ = oracle.dop853_dense(y0, np.linspace(0.0, 4.0, 101), MU, rtol=1e-11, atol=1e-11)
         assert np.array_equal(sol.states, ref)
+        # The golden run is the reference without numba: its x**3 is libm pow,
+        # numba's (the reference as shipped, and this kernel) is x*(x*x).  On an
+        # unstable arc that last-bit difference grows, so the bar is the
+        # reference's own run-mode spread: numba-mode vs pure-Python reference.
+        oracle.set_mode(oracle.MODE_NUMBA)
+        numba, _, _, _ = oracle.dop853_dense(y0, np.linspace(0.0, 4.0, 101), MU, rtol=1e-11, atol=1e-11)
+        spread = rowwise_rel(numba, a[f"dense6/{i}/states"])
+        assert rowwise_rel(sol.states, a[f"dense6/{i}/states"]) <= max(1e-9, 4.0 * spread)
+        assert rowwise_rel(sol.states, numba) <= max(1e-9, 4.0 * spread)
     for i, fwd in ((0, 1), (1, -1)):
         x, t, phiT, PHI = D.compute_stm(D.CR3BPSystem(MU, 42), a[f"stm_halo/{i}/y0"], W.HALO_L1_AZ02_T, steps=40,
                                         forward=fwd)
