@@ -125,6 +125,90 @@ int launch_dop853(hg_handle* h, hg::DopParams p, cudaStream_t s) {
   return check_launch(h, "dop853_kernel");
 }
 
+__global__ void seg_init_kernel(int N, int* list, int* count, int* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) {
+    list[i] = i;
+    status[i] = -2;  // not started
+  }
+  if (i == 0) *count = N;
+}
+
+// Workspace of the segmented DOP853 driver, carved from one caller buffer.
+struct SegWs {
+  int* list[2];
+  int* count;  // [2]
+  double* h;
+  double* err_prev;
+  double* prev_pow;
+  int* q;
+};
+
+long long seg_ws_layout(int N, char* base, SegWs* w) {
+  auto up = [](long long x) { return (x + 255) & ~255LL; };
+  long long off = 0;
+  const long long ni = up((long long)N * 4), nd = up((long long)N * 8);
+  if (w) w->list[0] = (int*)(base + off);
+  off += ni;
+  if (w) w->list[1] = (int*)(base + off);
+  off += ni;
+  if (w) w->count = (int*)(base + off);
+  off += 256;
+  if (w) w->h = (double*)(base + off);
+  off += nd;
+  if (w) w->err_prev = (double*)(base + off);
+  off += nd;
+  if (w) w->prev_pow = (double*)(base + off);
+  off += nd;
+  if (w) w->q = (int*)(base + off);
+  off += ni;
+  return off;
+}
+
+template <int G>
+int launch_dop853_seg(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_steps, int max_segments, int resume,
+                      cudaStream_t s) {
+  const int kBlock = h->block;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hg::dop853_kernel<G>, kBlock, 0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int tpb = (kBlock / 32) * hg::Layout<G>::TPW;
+  const int need = (p.N + tpb - 1) / tpb;
+  const int cap = per_sm * h->sm_count;
+  const int grid = need < cap ? need : cap;
+  p.stride = grid * tpb;
+  p.next_traj = nullptr;
+  p.seg = 1;
+  p.seg_steps = seg_steps;
+  p.ws_h = w.h;
+  p.ws_err_prev = w.err_prev;
+  p.ws_prev_pow = w.prev_pow;
+  p.ws_q = w.q;
+  if (!resume) {
+    seg_init_kernel<<<(p.N + 255) / 256, 256, 0, s>>>(p.N, w.list[0], w.count, p.status);
+    const int rc = check_launch(h, "seg_init_kernel");
+    if (rc != HG_OK) return rc;
+  }
+  for (int sgm = 0; sgm < max_segments; ++sgm) {
+    const int a = sgm & 1, b = a ^ 1;
+    if (cudaMemsetAsync(w.count + b, 0, sizeof(int), s) != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset");
+    p.active_in = w.list[a];
+    p.n_in = w.count + a;
+    p.active_out = w.list[b];
+    p.n_out = w.count + b;
+    hg::dop853_kernel<G><<<grid, kBlock, 0, s>>>(p);
+    const int rc = check_launch(h, "dop853_kernel (segment)");
+    if (rc != HG_OK) return rc;
+  }
+  if (max_segments & 1) {  // leave the live list in list[0] for a resume
+    if (cudaMemcpyAsync(w.list[0], w.list[1], sizeof(int) * (size_t)p.N, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(w.count, w.count + 1, sizeof(int), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return fail(h, HG_ERR_CUDA, "memcpy");
+  }
+  return HG_OK;
+}
+
 __global__ void fp64_probe_kernel(double* out, int iters, double a, double b) {
   double x0 = threadIdx.x * 1e-9, x1 = x0 + 1e-9, x2 = x0 + 2e-9, x3 = x0 + 3e-9;
   double x4 = x0 + 4e-9, x5 = x0 + 5e-9, x6 = x0 + 6e-9, x7 = x0 + 7e-9;
@@ -217,12 +301,14 @@ int hg_propagate_fixed_event(hg_handle* h, double mu, int order, int dim, int N,
   return fixed_dispatch(h, order, dim, p, (cudaStream_t)stream);
 }
 
-int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y0, long long ld,
+}  // extern "C"
+
+// Argument checks and kernel parameters shared by the DOP853 entry points.
+static int dop853_setup(hg_handle* h, double mu, int dim, int N, const double* y0, long long ld,
                         const double* t0_arr, const double* tmax_arr, double t0, double tmax,
                         const hg_dop853_opts* opts, const hg_event* ev, int n_samples, int sample_last_only,
                         double* y_samples, double* y_end, double* t_end, double* hit_t, double* hit_y, int* n_hits,
-                        int* n_accept, int* n_reject, int* status, void* stream) {
-  if (!h) return HG_ERR_ARGS;
+                        int* n_accept, int* n_reject, int* status, hg::DopParams& p) {
   if (dim != 6 && dim != 42) return fail(h, HG_ERR_ARGS, "dim must be 6 or 42 (got %d)", dim);
   if (N < 0 || ld < N) return fail(h, HG_ERR_ARGS, "bad N/ld");
   if (!opts) return fail(h, HG_ERR_ARGS, "opts is null");
@@ -234,7 +320,6 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
   if (opts->max_steps < 1) return fail(h, HG_ERR_ARGS, "max_steps must be >= 1");
   if (n_samples < 0 || n_samples == 1) return fail(h, HG_ERR_ARGS, "n_samples must be 0 or >= 2");
   if (n_samples >= 2 && !y_samples) return fail(h, HG_ERR_ARGS, "y_samples is null");
-  hg::DopParams p;
   memset(&p, 0, sizeof(p));
   p.ev_index = -1;
   if (ev && ev->index >= 0) {
@@ -275,6 +360,22 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
   p.n_accept = n_accept;
   p.n_reject = n_reject;
   p.status = status;
+  return HG_OK;
+}
+
+extern "C" {
+
+int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y0, long long ld,
+                        const double* t0_arr, const double* tmax_arr, double t0, double tmax,
+                        const hg_dop853_opts* opts, const hg_event* ev, int n_samples, int sample_last_only,
+                        double* y_samples, double* y_end, double* t_end, double* hit_t, double* hit_y, int* n_hits,
+                        int* n_accept, int* n_reject, int* status, void* stream) {
+  if (!h) return HG_ERR_ARGS;
+  hg::DopParams p;
+  const int rc = dop853_setup(h, mu, dim, N, y0, ld, t0_arr, tmax_arr, t0, tmax, opts, ev, n_samples,
+                              sample_last_only, y_samples, y_end, t_end, hit_t, hit_y, n_hits, n_accept, n_reject,
+                              status, p);
+  if (rc != HG_OK) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   if (dim == 6) {
     int lanes = h->lanes_d6;
@@ -285,6 +386,40 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
     return launch_dop853<1>(h, p, s);
   }
   return launch_dop853<7>(h, p, s);
+}
+
+long long hg_dop853_segmented_workspace_bytes(int N) { return N < 0 ? -1 : seg_ws_layout(N, nullptr, nullptr); }
+
+int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N, const double* y0, long long ld,
+                                  const double* t0_arr, const double* tmax_arr, double t0, double tmax,
+                                  const hg_dop853_opts* opts, const hg_event* ev, int n_samples,
+                                  int sample_last_only, double* y_samples, double* y_end, double* t_end,
+                                  double* hit_t, double* hit_y, int* n_hits, int* n_accept, int* n_reject,
+                                  int* status, int seg_steps, int max_segments, int resume, void* workspace,
+                                  long long workspace_bytes, void* stream) {
+  if (!h) return HG_ERR_ARGS;
+  if (seg_steps < 1 || max_segments < 1) return fail(h, HG_ERR_ARGS, "seg_steps and max_segments must be >= 1");
+  if (N > 0 && (!y_end || !t_end || !n_accept || !n_reject || !status))
+    return fail(h, HG_ERR_ARGS, "segmented runs keep their state in y_end/t_end/n_accept/n_reject/status");
+  if (ev && ev->index >= 0 && N > 0 && !n_hits) return fail(h, HG_ERR_ARGS, "n_hits is required with an event");
+  if (!workspace || workspace_bytes < seg_ws_layout(N, nullptr, nullptr))
+    return fail(h, HG_ERR_ARGS, "workspace smaller than hg_dop853_segmented_workspace_bytes(N)");
+  // argument checks and parameter setup shared with the single-pass entry
+  hg::DopParams p;
+  memset(&p, 0, sizeof(p));
+  int rc = dop853_setup(h, mu, dim, N, y0, ld, t0_arr, tmax_arr, t0, tmax, opts, ev, n_samples, sample_last_only,
+                        y_samples, y_end, t_end, hit_t, hit_y, n_hits, n_accept, n_reject, status, p);
+  if (rc != HG_OK || N == 0) return rc;
+  SegWs w;
+  seg_ws_layout(N, (char*)workspace, &w);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dim == 6) {
+    int lanes = h->lanes_d6;
+    if (lanes == 0) lanes = (2LL * N <= 4LL * 32 * h->sm_count) ? 2 : 1;
+    if (lanes == 2) return launch_dop853_seg<2>(h, p, w, seg_steps, max_segments, resume, s);
+    return launch_dop853_seg<1>(h, p, w, seg_steps, max_segments, resume, s);
+  }
+  return launch_dop853_seg<7>(h, p, w, seg_steps, max_segments, resume, s);
 }
 
 int hg_set_tuning(hg_handle* h, int key, int value) {

@@ -704,7 +704,26 @@ struct DopParams {
   // persistent lane refill
   int* next_traj;  // scratch counter (zeroed before launch) or null: static assignment
   int stride;      // trajectories assigned in the first wave (grid lanes / G)
+  // Segmented execution (seg != 0): the launch advances the trajectories
+  // listed in active_in[0 .. *n_in) by at most seg_steps attempted steps.
+  // The integration state persists between launches in the outputs (y_end,
+  // t_end, n_accept, n_reject, n_hits, status = HG_RUNNING) and in ws_*;
+  // unfinished trajectories are appended to active_out (count *n_out).
+  // Each launch starts every group with a full set of live trajectories, so
+  // lanes that finished early stop wasting the FP64 pipe.
+  int seg;
+  int seg_steps;
+  const int* active_in;
+  const int* n_in;
+  int* active_out;
+  int* n_out;
+  double* ws_h;
+  double* ws_err_prev;
+  double* ws_prev_pow;
+  int* ws_q;
 };
+
+#define HG_RUNNING (-1)
 
 template <int G>
 struct DopLane {
@@ -900,18 +919,43 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
       return __shfl_sync(L.gmask, v, ev_src);
   };
 
-  while (traj < p.N) {
+  int slot = traj;
+  while (true) {
+    if (p.seg) {
+      if (slot >= *p.n_in) break;
+      traj = p.active_in[slot];
+    } else if (traj >= p.N) {
+      break;
+    }
     const double t0 = p.t0_arr ? p.t0_arr[traj] : p.t0;
     const double tmax = p.tmax_arr ? p.tmax_arr[traj] : p.tmax;
+    const bool resume = p.seg && p.status[traj] == HG_RUNNING;
     double y[NC];
+    if (resume) {
 #pragma unroll
-    for (int r = 0; r < NC; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld + traj];
+      for (int r = 0; r < NC; ++r) y[r] = p.y_end[(long long)L.comp(r) * p.ld + traj];
+    } else {
+#pragma unroll
+      for (int r = 0; r < NC; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld + traj];
+    }
     double k[13][NC];
+    // on resume this is bitwise k[12] of the last accepted step
     L.rhs(y, p.mu, p.dir, k[0]);
     double g_prev = 0.0;
     if (has_event) g_prev = bcast_ev(ev_mine ? (pick<NC>(y, ev_r) - p.ev_offset) : 0.0);
-    double h;
-    {
+    double h, t, err_prev, prev_pow;
+    int acc, rej, hits, q_next;
+    const bool dense = p.m >= 2;
+    if (resume) {
+      h = p.ws_h[traj];
+      t = p.t_end[traj];
+      err_prev = p.ws_err_prev[traj];
+      prev_pow = p.ws_prev_pow[traj];
+      acc = p.n_accept[traj];
+      rej = p.n_reject[traj];
+      hits = (has_event && p.n_hits) ? p.n_hits[traj] : 0;
+      q_next = dense ? p.ws_q[traj] : 0;
+    } else {
       double a[NC], b[NC];
 #pragma unroll
       for (int d = 0; d < NC; ++d) {
@@ -923,21 +967,26 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
       const double d0 = sqrt(gat.dot(L, a)) / sn;
       const double d1 = sqrt(gat.dot(L, b)) / sn;
       h = select_initial_step(d0, d1, p.min_step, p.max_step);
+      t = t0;
+      err_prev = -1.0;
+      prev_pow = 0.0;
+      acc = rej = hits = 0;
+      q_next = (dense && p.dense_last) ? p.m - 1 : 0;
     }
-    double t = t0;
-    double err_prev = -1.0;
-    double prev_pow = 0.0;
-    int acc = 0, rej = 0, hits = 0;
     int status = HG_OK;
     // dense sampling on linspace(t0, tmax, m)
-    int q_next = 0;
     double step_ls = 0.0;
-    const bool dense = p.m >= 2;
     if (dense) step_ls = (tmax - t0) / (double)(p.m - 1);
     auto sample_t = [&](int q) -> double { return q == p.m - 1 ? tmax : (double)q * step_ls + t0; };
-    if (dense && p.dense_last) q_next = p.m - 1;
+    int seg_count = 0;
+    bool paused = false;
 
     while ((t - tmax) * 1.0 < 0.0) {
+      if (p.seg && seg_count >= p.seg_steps) {
+        paused = true;
+        break;
+      }
+      ++seg_count;
       if ((long long)(acc + rej) >= p.max_steps) {
         status = HG_MAX_STEPS;
         break;
@@ -1049,6 +1098,22 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
 #pragma unroll
       for (int d = 0; d < NC; ++d) p.y_end[(long long)L.comp(d) * p.ld + traj] = y[d];
     }
+    if (paused) {
+      if (leader) {
+        p.t_end[traj] = t;
+        p.ws_h[traj] = h;
+        p.ws_err_prev[traj] = err_prev;
+        p.ws_prev_pow[traj] = prev_pow;
+        if (dense) p.ws_q[traj] = q_next;
+        if (p.n_hits) p.n_hits[traj] = hits;
+        p.n_accept[traj] = acc;
+        p.n_reject[traj] = rej;
+        p.status[traj] = HG_RUNNING;
+        p.active_out[atomicAdd(p.n_out, 1)] = traj;
+      }
+      slot += p.stride;
+      continue;
+    }
     if (dense) {
       // the reference's dense output falls back to the single stored node
       // when no step was taken
@@ -1067,6 +1132,10 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
       if (p.status) p.status[traj] = status;
     }
     // next trajectory
+    if (p.seg) {
+      slot += p.stride;
+      continue;
+    }
     if (p.next_traj == nullptr) break;
     int nt = 0;
     if constexpr (G == 1) {

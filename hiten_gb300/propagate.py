@@ -137,12 +137,16 @@ class Dop853Result:
 
 def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min_step=None,
                      max_steps=100_000, fwd=1, flip=None, event=None, n_samples=0, sample_last_only=False,
-                     device=None, stream=None):
+                     device=None, stream=None, segmented=False, seg_steps=16, max_segments=8):
     """Adaptive DOP853 for N states from t0 to tmax (scalars or (N,) arrays).
 
     Mirrors integrators/rk.py:2375-2549 / :2678-2803 step for step.
     ``event``: optional :class:`EventSpec`.  ``n_samples >= 2``: dense output
     at linspace(t0_i, tmax_i, n_samples) (``sample_last_only``: final sample only).
+    ``segmented``: run in launches of at most ``seg_steps`` attempted steps per
+    trajectory (``max_segments`` launches per asynchronous call, repeated until
+    every trajectory finished), compacting the live trajectories between
+    launches; results are bit-identical.
     """
     dev = _device(device)
     y0 = torch.as_tensor(y0, dtype=torch.float64)
@@ -185,12 +189,25 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
         samples = torch.empty((rows, dim, ld), dtype=torch.float64, device=dev)
     H = _lib.handle(dev.index or 0)
     st = _stream(dev) if stream is None else C.c_void_p(stream)
+    args = (H.ptr, float(mu), dim, N, _ptr(Y0), ld, _ptr(t0a), _ptr(tmaxa), t0s, tmaxs, C.byref(opts),
+            C.byref(evp) if evp is not None else None, int(n_samples), 1 if sample_last_only else 0, _ptr(samples),
+            _ptr(y_end), _ptr(t_end), _ptr(hit_t), _ptr(hit_y), _ptr(n_hits), _ptr(n_acc), _ptr(n_rej), _ptr(status))
     with torch.cuda.device(dev):
-        H.check(H.lib.hg_propagate_dop853(H.ptr, float(mu), dim, N, _ptr(Y0), ld, _ptr(t0a), _ptr(tmaxa), t0s, tmaxs,
-                                          C.byref(opts), C.byref(evp) if evp is not None else None, int(n_samples),
-                                          1 if sample_last_only else 0, _ptr(samples), _ptr(y_end), _ptr(t_end),
-                                          _ptr(hit_t), _ptr(hit_y), _ptr(n_hits), _ptr(n_acc), _ptr(n_rej),
-                                          _ptr(status), st))
+        if not segmented:
+            H.check(H.lib.hg_propagate_dop853(*args, st))
+        else:
+            ws_bytes = int(H.lib.hg_dop853_segmented_workspace_bytes(N))
+            ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
+            segs = int(max_segments)
+            resume = 0
+            while True:
+                H.check(H.lib.hg_propagate_dop853_segmented(*args, int(seg_steps), segs, resume,
+                                                            _ptr(ws), ws_bytes, st))
+                # the caller's step budget bounds the total work; stop once no
+                # trajectory is left running
+                if N == 0 or not bool((status[:N] == _lib.HG_RUNNING).any()):
+                    break
+                resume = 1
     res = Dop853Result(y_end=y_end[:, :N].t(), t_end=t_end[:N], n_accept=n_acc[:N], n_reject=n_rej[:N],
                        status=status[:N])
     if event is not None:

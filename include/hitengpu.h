@@ -130,6 +130,32 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N,
                         int* n_accept, int* n_reject, int* status,
                         void* stream);
 
+/* hg_propagate_dop853 in segments: up to max_segments launches, each
+ * advancing every live trajectory by at most seg_steps attempted steps and
+ * compacting the live trajectories into a dense list for the next launch
+ * (lanes whose trajectory finished no longer idle in FP64 instructions).
+ * All work is asynchronous with no host synchronisation, so a call can be
+ * captured in a CUDA graph.  State persists in the outputs (y_end, t_end,
+ * n_accept, n_reject, n_hits, status -- all required; status = -1 marks a
+ * trajectory still running) and in `workspace` (caller device memory of at
+ * least hg_dop853_segmented_workspace_bytes(N) bytes); resume = 1 continues
+ * a previous call's unfinished trajectories.  Results are bit-identical to
+ * hg_propagate_dop853.
+ * Replaces: as hg_propagate_dop853 (execution schedule only). */
+long long hg_dop853_segmented_workspace_bytes(int N);
+int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N,
+                                  const double* y0, long long ld,
+                                  const double* t0_arr, const double* tmax_arr,
+                                  double t0, double tmax,
+                                  const hg_dop853_opts* opts, const hg_event* ev,
+                                  int n_samples, int sample_last_only, double* y_samples,
+                                  double* y_end, double* t_end,
+                                  double* hit_t, double* hit_y, int* n_hits,
+                                  int* n_accept, int* n_reject, int* status,
+                                  int seg_steps, int max_segments, int resume,
+                                  void* workspace, long long workspace_bytes,
+                                  void* stream);
+
 /* No counterpart in the reference.  The DOP853 propagation of
  * hg_propagate_dop853, for callers that cannot call cudaMalloc (an embedding
  * runtime that owns all device memory, a loop that must not allocate after

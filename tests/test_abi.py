@@ -42,3 +42,16 @@ def test_create_without_device_fails_cleanly():
     from hiten_gb300 import _lib
     with pytest.raises(_lib.HitenGpuError):
         _lib.Handle(0)
+
+
+def test_segmented_workspace_query():
+    """Pure host arithmetic: 256-byte aligned sub-buffers, grows with N."""
+    from hiten_gb300 import _lib
+    L = _lib.load()
+    assert L.hg_dop853_segmented_workspace_bytes(-1) == -1
+    prev = L.hg_dop853_segmented_workspace_bytes(0)
+    assert prev > 0 and prev % 256 == 0
+    for n in (1, 63, 64, 65, 16384, 1 << 20):
+        b = L.hg_dop853_segmented_workspace_bytes(n)
+        assert b % 256 == 0 and b >= prev and b >= n * (3 * 4 + 3 * 8)
+        prev = b
