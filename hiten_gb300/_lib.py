@@ -26,10 +26,12 @@ STATUS_NAMES = {0: "OK", 1: "MAX_STEPS", 2: "STEP_UNDERFLOW", 3: "NONFINITE", 4:
 EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg_propagate_fixed",
             "hg_propagate_dop853", "hg_probe_fp64_peak", "hg_propagate_dop853_noalloc", "hg_set_tuning",
             "hg_get_tuning", "hg_section_detect", "hg_trajectory_filters", "hg_propagate_fixed_event",
-            "hg_dop853_segmented_workspace_bytes", "hg_propagate_dop853_segmented")
+            "hg_dop853_segmented_workspace_bytes", "hg_propagate_dop853_segmented",
+            "hg_propagate_dop853_scheduled")
 HG_RUNNING = -1
 HG_TUNE_BLOCK_THREADS = 1
 HG_TUNE_DOP853_LANES_D6 = 2
+HG_TUNE_SEG_STEPS = 3
 
 
 class HitenGpuError(RuntimeError):
@@ -100,11 +102,13 @@ def load(build_if_missing=True):
                                                C.c_int, C.c_int, _P, C.c_longlong, C.c_int, C.c_int, C.c_int,
                                                C.POINTER(hg_event), _P, _P, _P, _P, _P]
         L.hg_propagate_fixed_event.restype = C.c_int
-        L.hg_dop853_segmented_workspace_bytes.argtypes = [C.c_int]
+        L.hg_dop853_segmented_workspace_bytes.argtypes = [C.c_int, C.c_int]
         L.hg_dop853_segmented_workspace_bytes.restype = C.c_longlong
         L.hg_propagate_dop853_segmented.argtypes = (L.hg_propagate_dop853.argtypes[:-1]
                                                     + [C.c_int, C.c_int, C.c_int, _P, C.c_longlong, _P])
         L.hg_propagate_dop853_segmented.restype = C.c_int
+        L.hg_propagate_dop853_scheduled.argtypes = L.hg_propagate_dop853.argtypes[:-1] + [_P, C.c_longlong, _P]
+        L.hg_propagate_dop853_scheduled.restype = C.c_int
         L.hg_set_tuning.argtypes = [_P, C.c_int, C.c_int]
         L.hg_set_tuning.restype = C.c_int
         L.hg_get_tuning.argtypes = [_P, C.c_int, C.POINTER(C.c_int)]

@@ -16,7 +16,11 @@ struct hg_handle {
   int sm_count = 0;
   int* counters = nullptr;  // scratch: lane-refill counters
   int block = 32;           // threads per block (32, 64 or 128)
-  int lanes_d6 = 0;         // lanes per 6-dim DOP853 trajectory: 0 auto, 1, 2
+  int lanes_d6 = 0;         // lanes per 6-dim DOP853 trajectory: 0 auto, 1, 2, 6
+  int seg_steps = 16;       // attempted steps per segment of the scheduled DOP853 driver
+  int* host_count = nullptr;  // pinned: live-trajectory count read back between segments
+  char* scratch = nullptr;    // grow-only: saved crossing steps of single-pass calls
+  long long scratch_bytes = 0;
   char err[512] = {0};
 };
 
@@ -103,6 +107,60 @@ int fixed_dispatch(hg_handle* h, int order, int dim, const hg::FixedParams& p, c
   return launch_fixed<8, 7>(h, p, s);
 }
 
+// Saved-step area of the deferred event refinement for N trajectories of
+// dimension D: count (256 B), list (N ints), record ((15 D + 3) x N doubles).
+long long refine_area_bytes(int N, int D) {
+  auto up = [](long long x) { return (x + 255) & ~255LL; };
+  return 256 + up((long long)N * 4) + up((15LL * D + 3) * (long long)N * 8);
+}
+
+void refine_area_carve(int N, char* base, hg::DopParams& p) {
+  auto up = [](long long x) { return (x + 255) & ~255LL; };
+  p.refine_count = (int*)base;
+  p.refine_list = (int*)(base + 256);
+  p.rec = (double*)(base + 256 + up((long long)N * 4));
+  p.rec_ld = N;
+}
+
+// Terminal events (one hit) are refined after the integration, in lock step.
+bool defer_refine(const hg::DopParams& p) { return p.ev_index >= 0 && p.max_hits == 1; }
+
+template <int G>
+int launch_refine(hg_handle* h, hg::DopParams p, cudaStream_t s) {
+  const int kBlock = h->block;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hg::refine_kernel<G>, kBlock, 0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int tpb = (kBlock / 32) * hg::Layout<G>::TPW;
+  const int need = (p.N + tpb - 1) / tpb;
+  const int cap = per_sm * h->sm_count;
+  const int grid = need < cap ? need : cap;
+  if (grid < 1) return HG_OK;
+  p.stride = grid * tpb;
+  hg::refine_kernel<G><<<grid, kBlock, 0, s>>>(p);
+  return check_launch(h, "refine_kernel");
+}
+
+int refine_pending(hg_handle* h, const hg::DopParams& p, int dim, cudaStream_t s) {
+  if (!p.rec) return HG_OK;
+  return dim == 6 ? launch_refine<1>(h, p, s) : launch_refine<7>(h, p, s);
+}
+
+int ensure_scratch(hg_handle* h, long long bytes) {
+  if (bytes <= h->scratch_bytes) return HG_OK;
+  if (h->scratch) cudaFree(h->scratch);
+  h->scratch = nullptr;
+  h->scratch_bytes = 0;
+  const long long want = bytes + bytes / 4;
+  if (cudaMalloc(&h->scratch, (size_t)want) != cudaSuccess) {
+    h->scratch = nullptr;
+    return fail(h, HG_ERR_CUDA, "cudaMalloc of %lld bytes of refinement scratch failed", want);
+  }
+  h->scratch_bytes = want;
+  return HG_OK;
+}
+
 template <int G>
 int launch_dop853(hg_handle* h, hg::DopParams p, cudaStream_t s) {
   if (p.N <= 0) return HG_OK;
@@ -125,6 +183,17 @@ int launch_dop853(hg_handle* h, hg::DopParams p, cudaStream_t s) {
   return check_launch(h, "dop853_kernel");
 }
 
+// Lanes per 6-dim DOP853 trajectory when the caller did not choose: the
+// largest group whose warps still fit one per SM sub-partition (the longest
+// trajectory sets the time and its per-step latency falls with the group
+// size), single lanes once even those oversubscribe.
+int auto_lanes_d6(const hg_handle* h, int N) {
+  const long long smsp = 4LL * h->sm_count;
+  if ((N + 4LL) / 5 <= smsp) return 6;
+  if ((N + 15LL) / 16 <= smsp) return 2;
+  return 1;
+}
+
 __global__ void seg_init_kernel(int N, int* list, int* count, int* status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < N) {
@@ -142,9 +211,10 @@ struct SegWs {
   double* err_prev;
   double* prev_pow;
   int* q;
+  char* refine;  // saved crossing steps (refine_area_bytes)
 };
 
-long long seg_ws_layout(int N, char* base, SegWs* w) {
+long long seg_ws_layout(int N, int D, char* base, SegWs* w) {
   auto up = [](long long x) { return (x + 255) & ~255LL; };
   long long off = 0;
   const long long ni = up((long long)N * 4), nd = up((long long)N * 8);
@@ -162,21 +232,28 @@ long long seg_ws_layout(int N, char* base, SegWs* w) {
   off += nd;
   if (w) w->q = (int*)(base + off);
   off += ni;
+  if (w) w->refine = base + off;
+  off += refine_area_bytes(N, D);
   return off;
 }
 
+// One segment over the live list list[a] (at most n_live entries): every
+// live trajectory advances by up to seg_steps attempted steps; those still
+// running are appended to list[a ^ 1].
 template <int G>
-int launch_dop853_seg(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_steps, int max_segments, int resume,
-                      cudaStream_t s) {
+int launch_segment(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_steps, int a, int n_live, cudaStream_t s) {
   const int kBlock = h->block;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hg::dop853_kernel<G>, kBlock, 0) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
   const int tpb = (kBlock / 32) * hg::Layout<G>::TPW;
-  const int need = (p.N + tpb - 1) / tpb;
+  const int need = (n_live + tpb - 1) / tpb;
   const int cap = per_sm * h->sm_count;
   const int grid = need < cap ? need : cap;
+  const int b = a ^ 1;
+  if (cudaMemsetAsync(w.count + b, 0, sizeof(int), s) != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset");
+  if (grid < 1) return HG_OK;
   p.stride = grid * tpb;
   p.next_traj = nullptr;
   p.seg = 1;
@@ -185,20 +262,28 @@ int launch_dop853_seg(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_ste
   p.ws_err_prev = w.err_prev;
   p.ws_prev_pow = w.prev_pow;
   p.ws_q = w.q;
+  p.active_in = w.list[a];
+  p.n_in = w.count + a;
+  p.active_out = w.list[b];
+  p.n_out = w.count + b;
+  hg::dop853_kernel<G><<<grid, kBlock, 0, s>>>(p);
+  return check_launch(h, "dop853_kernel (segment)");
+}
+
+int seg_init(hg_handle* h, const hg::DopParams& p, const SegWs& w, cudaStream_t s) {
+  seg_init_kernel<<<(p.N + 255) / 256, 256, 0, s>>>(p.N, w.list[0], w.count, p.status);
+  return check_launch(h, "seg_init_kernel");
+}
+
+template <int G>
+int launch_dop853_seg(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_steps, int max_segments, int resume,
+                      cudaStream_t s) {
   if (!resume) {
-    seg_init_kernel<<<(p.N + 255) / 256, 256, 0, s>>>(p.N, w.list[0], w.count, p.status);
-    const int rc = check_launch(h, "seg_init_kernel");
+    const int rc = seg_init(h, p, w, s);
     if (rc != HG_OK) return rc;
   }
   for (int sgm = 0; sgm < max_segments; ++sgm) {
-    const int a = sgm & 1, b = a ^ 1;
-    if (cudaMemsetAsync(w.count + b, 0, sizeof(int), s) != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset");
-    p.active_in = w.list[a];
-    p.n_in = w.count + a;
-    p.active_out = w.list[b];
-    p.n_out = w.count + b;
-    hg::dop853_kernel<G><<<grid, kBlock, 0, s>>>(p);
-    const int rc = check_launch(h, "dop853_kernel (segment)");
+    const int rc = launch_segment<G>(h, p, w, seg_steps, sgm & 1, p.N, s);
     if (rc != HG_OK) return rc;
   }
   if (max_segments & 1) {  // leave the live list in list[0] for a resume
@@ -207,6 +292,31 @@ int launch_dop853_seg(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_ste
       return fail(h, HG_ERR_CUDA, "memcpy");
   }
   return HG_OK;
+}
+
+// Layout of the next segment of a 6-dim batch with n_live trajectories
+// left: the group size with the least time per step, where one warp's step
+// takes lat(G) (measured on GB300 for the longest manifold trajectory:
+// 75.4, 46.9 and 30.2 us for G = 1, 2, 6) and warps beyond one per SM
+// sub-partition share its FP64 pipe.
+int sched_lanes_d6(const hg_handle* h, int n_live) {
+  if (h->lanes_d6 != 0) return h->lanes_d6;
+  const double smsp = 4.0 * h->sm_count;
+  const int gs[3] = {1, 2, 6};
+  const int tpw[3] = {32, 16, 5};
+  const double lat[3] = {1.0, 0.622, 0.400};
+  int best = 0;
+  double best_cost = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    const double warps = (double)((n_live + tpw[i] - 1) / tpw[i]);
+    const double load = warps / smsp;
+    const double cost = lat[i] * (load > 1.0 ? load : 1.0);
+    if (i == 0 || cost < best_cost) {
+      best = i;
+      best_cost = cost;
+    }
+  }
+  return gs[best];
 }
 
 __global__ void fp64_probe_kernel(double* out, int iters, double a, double b) {
@@ -261,6 +371,8 @@ int hg_create(const hg_config* cfg, hg_handle** out) {
 int hg_destroy(hg_handle* h) {
   if (!h) return HG_OK;
   if (h->counters) cudaFree(h->counters);
+  if (h->host_count) cudaFreeHost(h->host_count);
+  if (h->scratch) cudaFree(h->scratch);
   delete h;
   return HG_OK;
 }
@@ -375,20 +487,35 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
   const int rc = dop853_setup(h, mu, dim, N, y0, ld, t0_arr, tmax_arr, t0, tmax, opts, ev, n_samples,
                               sample_last_only, y_samples, y_end, t_end, hit_t, hit_y, n_hits, n_accept, n_reject,
                               status, p);
-  if (rc != HG_OK) return rc;
+  if (rc != HG_OK || N == 0) return rc;
   cudaStream_t s = (cudaStream_t)stream;
+  if (defer_refine(p)) {
+    int e = ensure_scratch(h, refine_area_bytes(N, dim));
+    if (e != HG_OK) return e;
+    refine_area_carve(N, h->scratch, p);
+    if (cudaMemsetAsync(p.refine_count, 0, sizeof(int), s) != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset");
+  }
+  int rc2;
   if (dim == 6) {
     int lanes = h->lanes_d6;
-    // auto: pairs while two lanes per trajectory still fit one warp per SM
-    // sub-partition (shortest per-step latency), single lanes beyond
-    if (lanes == 0) lanes = (2LL * N <= 4LL * 32 * h->sm_count) ? 2 : 1;
-    if (lanes == 2) return launch_dop853<2>(h, p, s);
-    return launch_dop853<1>(h, p, s);
+    if (lanes == 0) lanes = auto_lanes_d6(h, N);
+    if (lanes == 6)
+      rc2 = launch_dop853<6>(h, p, s);
+    else if (lanes == 2)
+      rc2 = launch_dop853<2>(h, p, s);
+    else
+      rc2 = launch_dop853<1>(h, p, s);
+  } else {
+    rc2 = launch_dop853<7>(h, p, s);
   }
-  return launch_dop853<7>(h, p, s);
+  if (rc2 != HG_OK) return rc2;
+  return refine_pending(h, p, dim, s);
 }
 
-long long hg_dop853_segmented_workspace_bytes(int N) { return N < 0 ? -1 : seg_ws_layout(N, nullptr, nullptr); }
+long long hg_dop853_segmented_workspace_bytes(int N, int dim) {
+  if (N < 0 || (dim != 6 && dim != 42)) return -1;
+  return seg_ws_layout(N, dim, nullptr, nullptr);
+}
 
 int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N, const double* y0, long long ld,
                                   const double* t0_arr, const double* tmax_arr, double t0, double tmax,
@@ -402,8 +529,8 @@ int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N, const
   if (N > 0 && (!y_end || !t_end || !n_accept || !n_reject || !status))
     return fail(h, HG_ERR_ARGS, "segmented runs keep their state in y_end/t_end/n_accept/n_reject/status");
   if (ev && ev->index >= 0 && N > 0 && !n_hits) return fail(h, HG_ERR_ARGS, "n_hits is required with an event");
-  if (!workspace || workspace_bytes < seg_ws_layout(N, nullptr, nullptr))
-    return fail(h, HG_ERR_ARGS, "workspace smaller than hg_dop853_segmented_workspace_bytes(N)");
+  if (!workspace || workspace_bytes < seg_ws_layout(N, dim, nullptr, nullptr))
+    return fail(h, HG_ERR_ARGS, "workspace smaller than hg_dop853_segmented_workspace_bytes(N, dim)");
   // argument checks and parameter setup shared with the single-pass entry
   hg::DopParams p;
   memset(&p, 0, sizeof(p));
@@ -411,15 +538,91 @@ int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N, const
                         y_samples, y_end, t_end, hit_t, hit_y, n_hits, n_accept, n_reject, status, p);
   if (rc != HG_OK || N == 0) return rc;
   SegWs w;
-  seg_ws_layout(N, (char*)workspace, &w);
+  seg_ws_layout(N, dim, (char*)workspace, &w);
   cudaStream_t s = (cudaStream_t)stream;
+  // crossings of this call are refined at its end
+  if (defer_refine(p)) {
+    refine_area_carve(N, w.refine, p);
+    if (cudaMemsetAsync(p.refine_count, 0, sizeof(int), s) != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset");
+  }
   if (dim == 6) {
     int lanes = h->lanes_d6;
-    if (lanes == 0) lanes = (2LL * N <= 4LL * 32 * h->sm_count) ? 2 : 1;
-    if (lanes == 2) return launch_dop853_seg<2>(h, p, w, seg_steps, max_segments, resume, s);
-    return launch_dop853_seg<1>(h, p, w, seg_steps, max_segments, resume, s);
+    if (lanes == 0) lanes = auto_lanes_d6(h, N);
+    if (lanes == 6)
+      rc = launch_dop853_seg<6>(h, p, w, seg_steps, max_segments, resume, s);
+    else if (lanes == 2)
+      rc = launch_dop853_seg<2>(h, p, w, seg_steps, max_segments, resume, s);
+    else
+      rc = launch_dop853_seg<1>(h, p, w, seg_steps, max_segments, resume, s);
+  } else {
+    rc = launch_dop853_seg<7>(h, p, w, seg_steps, max_segments, resume, s);
   }
-  return launch_dop853_seg<7>(h, p, w, seg_steps, max_segments, resume, s);
+  if (rc != HG_OK) return rc;
+  return refine_pending(h, p, dim, s);
+}
+
+int hg_propagate_dop853_scheduled(hg_handle* h, double mu, int dim, int N, const double* y0, long long ld,
+                                  const double* t0_arr, const double* tmax_arr, double t0, double tmax,
+                                  const hg_dop853_opts* opts, const hg_event* ev, int n_samples,
+                                  int sample_last_only, double* y_samples, double* y_end, double* t_end,
+                                  double* hit_t, double* hit_y, int* n_hits, int* n_accept, int* n_reject,
+                                  int* status, void* workspace, long long workspace_bytes, void* stream) {
+  if (!h) return HG_ERR_ARGS;
+  if (N > 0 && (!y_end || !t_end || !n_accept || !n_reject || !status))
+    return fail(h, HG_ERR_ARGS, "scheduled runs keep their state in y_end/t_end/n_accept/n_reject/status");
+  if (ev && ev->index >= 0 && N > 0 && !n_hits) return fail(h, HG_ERR_ARGS, "n_hits is required with an event");
+  if (!workspace || workspace_bytes < seg_ws_layout(N, dim, nullptr, nullptr))
+    return fail(h, HG_ERR_ARGS, "workspace smaller than hg_dop853_segmented_workspace_bytes(N, dim)");
+  hg::DopParams p;
+  memset(&p, 0, sizeof(p));
+  int rc = dop853_setup(h, mu, dim, N, y0, ld, t0_arr, tmax_arr, t0, tmax, opts, ev, n_samples, sample_last_only,
+                        y_samples, y_end, t_end, hit_t, hit_y, n_hits, n_accept, n_reject, status, p);
+  if (rc != HG_OK || N == 0) return rc;
+  if (!h->host_count) {
+    if (cudaHostAlloc(&h->host_count, sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+      h->host_count = nullptr;
+      return fail(h, HG_ERR_CUDA, "cudaHostAlloc failed");
+    }
+  }
+  SegWs w;
+  seg_ws_layout(N, dim, (char*)workspace, &w);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (defer_refine(p)) {
+    refine_area_carve(N, w.refine, p);
+    if (cudaMemsetAsync(p.refine_count, 0, sizeof(int), s) != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset");
+  }
+  rc = seg_init(h, p, w, s);
+  if (rc != HG_OK) return rc;
+  // every segment finishes its trajectories or advances each by seg_steps
+  // attempted steps, and no trajectory exceeds max_steps: this bounds the loop
+  const long long seg = h->seg_steps;
+  const long long max_iter = p.max_steps / seg + 2;
+  int n_live = N, a = 0;
+  for (long long it = 0; it < max_iter && n_live > 0; ++it) {
+    if (dim == 6) {
+      const int g = sched_lanes_d6(h, n_live);
+      if (g == 6)
+        rc = launch_segment<6>(h, p, w, (int)seg, a, n_live, s);
+      else if (g == 2)
+        rc = launch_segment<2>(h, p, w, (int)seg, a, n_live, s);
+      else
+        rc = launch_segment<1>(h, p, w, (int)seg, a, n_live, s);
+    } else {
+      rc = launch_segment<7>(h, p, w, (int)seg, a, n_live, s);
+    }
+    if (rc != HG_OK) return rc;
+    a ^= 1;
+    cudaError_t e = cudaMemcpyAsync(h->host_count, w.count + a, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(h, HG_ERR_CUDA, "segment: %s", cudaGetErrorString(e));
+    n_live = *h->host_count;
+  }
+  if (n_live > 0) return fail(h, HG_ERR_CUDA, "scheduled DOP853 did not finish within its step bound");
+  rc = refine_pending(h, p, dim, s);
+  if (rc != HG_OK) return rc;
+  const cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(h, HG_ERR_CUDA, "refine: %s", cudaGetErrorString(e));
+  return HG_OK;
 }
 
 int hg_set_tuning(hg_handle* h, int key, int value) {
@@ -430,8 +633,13 @@ int hg_set_tuning(hg_handle* h, int key, int value) {
       h->block = value;
       return HG_OK;
     case HG_TUNE_DOP853_LANES_D6:
-      if (value < 0 || value > 2) return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 1 or 2");
+      if (value != 0 && value != 1 && value != 2 && value != 6)
+        return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 1, 2 or 6");
       h->lanes_d6 = value;
+      return HG_OK;
+    case HG_TUNE_SEG_STEPS:
+      if (value < 1 || value > 1000000) return fail(h, HG_ERR_ARGS, "segment steps must be in [1, 1e6]");
+      h->seg_steps = value;
       return HG_OK;
     default:
       return fail(h, HG_ERR_ARGS, "unknown tuning key %d", key);
@@ -442,6 +650,7 @@ int hg_get_tuning(hg_handle* h, int key, int* value) {
   if (!h || !value) return HG_ERR_ARGS;
   if (key == HG_TUNE_BLOCK_THREADS) *value = h->block;
   else if (key == HG_TUNE_DOP853_LANES_D6) *value = h->lanes_d6;
+  else if (key == HG_TUNE_SEG_STEPS) *value = h->seg_steps;
   else return fail(h, HG_ERR_ARGS, "unknown tuning key %d", key);
   return HG_OK;
 }

@@ -276,6 +276,62 @@ struct Layout<2> {
   }
 };
 
+// G = 6 (6-dim state, lowest-latency layout): six lanes own one trajectory,
+// lane `role` holds component `role`, five trajectories per warp (lanes 30
+// and 31 idle).  The right-hand side splits the six quotients of rhs6 over
+// the six lanes: lane (b, a) with b = role / 3 the primary and a = role % 3
+// the axis forms the numerator of axis a over r_b^3 (each primary's lanes
+// compute its distance redundantly, in parallel); the acceleration lanes
+// 3..5 fetch the first primary's quotient of their axis and combine.  Every
+// operation and its operands are the ones rhs6 uses, so the bits are too;
+// the per-step FP64 critical path is about 0.55x that of G = 2.
+template <>
+struct Layout<6> {
+  static constexpr int D = 6;
+  static constexpr int NC = 1;
+  static constexpr int TPW = 5;
+  int role;        // component 0..5
+  int base;        // first lane of the group
+  unsigned gmask;  // the six lanes
+  __device__ __forceinline__ int comp(int) const { return role; }
+  __device__ __forceinline__ int owner(int c) const { return c; }
+  __device__ __forceinline__ int local(int) const { return 0; }
+  __device__ __forceinline__ void rhs(const double (&v)[1], double mu, const Dir& dir, double (&dv)[1]) const {
+    const double x = __shfl_sync(gmask, v[0], base);
+    const double y = __shfl_sync(gmask, v[0], base + 1);
+    const double z = __shfl_sync(gmask, v[0], base + 2);
+    // lanes 0..2: their derivative is the velocity of lane role + 3; lanes
+    // 3 and 4: the Coriolis term needs vy (lane 4) and vx (lane 3)
+    const int src = role < 3 ? role + 3 : (role == 3 ? 4 : 3);
+    const double u = __shfl_sync(gmask, v[0], base + src);
+    const bool b0 = role < 3;
+    const int ax = b0 ? role : role - 3;
+    const double omu = 1.0 - mu;
+    const double cb = b0 ? mu : -omu;  // x + mu | x - (1 - mu)
+    const double a1 = b0 ? mu : -1.0;  // x-numerator: (x + a1) + a2
+    const double a2 = b0 ? 0.0 : mu;
+    const double t = x + cb;
+    const double yy = y * y;
+    const double zz = z * z;
+    const double r = sqrt((t * t + yy) + zz);
+    const double rc = r * (r * r);
+    const double ir = hg_rcp_rn(rc);
+    const double nx = (x + a1) + a2;
+    const double nb = ax == 0 ? nx : (ax == 1 ? y : z);
+    const double m = b0 ? (ax == 2 ? -omu : omu) : mu;
+    const double q = hg_div_rn(m * nb, rc, ir);
+    // first primary's quotient of this lane's axis (lanes 3..5 use it)
+    const double pq = __shfl_sync(gmask, q, base + ax);
+    const double c2 = role == 3 ? 2.0 : -2.0;
+    const double xy = role == 3 ? x : y;
+    const double acc_xy = ((c2 * u + xy) - pq) - q;
+    const double acc_z = pq - q;
+    double d = role < 3 ? u : (role == 5 ? acc_z : acc_xy);
+    if (role >= dir.neg_lo && role < dir.neg_hi) d = -d;
+    dv[0] = d;
+  }
+};
+
 // numpy float64 dot order of the host the reference fixtures come from:
 // sequential fused accumulation for n < 16, a 32-element blocked sum plus a
 // fused tail for n = 42.  v is the full vector (identical in every lane).
@@ -343,6 +399,21 @@ struct Gather<2> {
   }
 };
 
+template <>
+struct Gather<6> {
+  // every lane runs the sequential fused accumulation over the six
+  // broadcast components
+  __device__ __forceinline__ double dot(const Layout<6>& L, const double (&v)[1]) const {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const double c = __shfl_sync(L.gmask, v[0], L.base + i);
+      s = fma(c, c, s);
+    }
+    return s;
+  }
+};
+
 // v[r] for a runtime r without dynamic register indexing.
 template <int NC>
 __device__ __forceinline__ double pick(const double (&v)[NC], int r) {
@@ -374,44 +445,61 @@ __device__ __forceinline__ double select_initial_step(double d0, double d1, doub
   if (h < min_step) h = min_step;
   return h;
 }
-// PI controller (order 8): beta = 1/9, alpha = 0.4*beta; reject exponent 1/8.
-// err_pow_alpha caches err_prev**alpha from the previous accepted step.
-__device__ __forceinline__ double pi_accept_factor(double err_norm, double err_prev, double& next_prev_pow) {
+// exp(e * (Lh + Ll)) rounded once: the composition hg_pow uses after its
+// logarithm (two_prod of the exponent with the double-double log).
+__device__ __forceinline__ double exp_scaled(double e, double Lh, double Ll) {
+  double th, pe, Th, Tl;
+  hg_two_prod(e, Lh, th, pe);
+  hg_fast_two_sum(th, fma(e, Ll, pe), Th, Tl);
+  return hg_exp_dd(Th, Tl);
+}
+
+// PI step-size factor after an attempted step (integrators/utils.py
+// step-size control, order 8): an accepted step scales h by
+// 0.9 * err^-beta * err_prev^alpha (beta = 1/9, alpha = 0.4 beta;
+// err_prev^alpha was computed at the previous accepted step and is carried
+// in prev_pow), a rejected one by 0.9 * err^(-1/8); factors are clamped to
+// [0.2, 10].  Accepting and rejecting lanes share the logarithm, so a warp
+// whose trajectories disagree runs one transcendental sequence, not two; in
+// a group of lanes the two exponentials run on two lanes at once.  Every
+// power is the correctly rounded one hg_pow gives.  Zero, NaN and
+// err >= 1e300 take no logarithm: their factors are the clamp bounds (a
+// rejected err >= 1e300 gives 0.9 * err^(-1/8) < 0.2).
+template <int G>
+__device__ __forceinline__ double pi_factor(const Layout<G>& L, bool accepted, double err, double err_prev,
+                                            double& prev_pow) {
   const double beta = 1.0 / (8.0 + 1.0);
   const double alpha = 0.4 * beta;
-  double factor;
-  if (err_norm == 0.0) {
-    factor = 10.0;
-    next_prev_pow = 0.0;
-  } else {
+  const double rexp = 1.0 / 8.0;
+  const bool regular = err > 0.0 && err < 1e300;
+  double p1 = 0.0, pa = 0.0;
+  if (regular) {
     double Lh, Ll;
-    hg_log_dd(err_norm, Lh, Ll);
-    double th, pe, Th, Tl;
-    hg_two_prod(-beta, Lh, th, pe);
-    hg_fast_two_sum(th, fma(-beta, Ll, pe), Th, Tl);
-    const double p1 = hg_exp_dd(Th, Tl);
-    hg_two_prod(alpha, Lh, th, pe);
-    hg_fast_two_sum(th, fma(alpha, Ll, pe), Th, Tl);
-    const double pa = hg_exp_dd(Th, Tl);
-    if (err_prev < 0.0)
-      factor = 0.9 * p1;
-    else
-      factor = (0.9 * p1) * next_prev_pow;
-    next_prev_pow = pa;
+    hg_log_dd(err, Lh, Ll);
+    const double e1 = accepted ? -beta : -rexp;
+    if constexpr (G == 1) {
+      p1 = exp_scaled(e1, Lh, Ll);
+      pa = exp_scaled(alpha, Lh, Ll);
+    } else {
+      const double v = exp_scaled(L.role == 0 ? e1 : alpha, Lh, Ll);
+      p1 = __shfl_sync(L.gmask, v, L.base);
+      pa = __shfl_sync(L.gmask, v, L.base + 1);
+    }
   }
-  if (!(factor == factor)) factor = 10.0;
-  if (factor < 0.2) factor = 0.2;
-  if (factor > 10.0) factor = 10.0;
-  return factor;
-}
-__device__ __forceinline__ double pi_reject_factor(double err_norm) {
-  const double err_exp = 1.0 / 8.0;
   double factor;
-  if (err_norm <= 0.0)
-    factor = 0.2;
-  else
-    factor = 0.9 * hg_pow(err_norm, -err_exp);
-  if (!(factor == factor)) factor = 0.2;
+  if (accepted) {
+    if (err == 0.0) {
+      factor = 10.0;
+      prev_pow = 0.0;
+    } else {
+      factor = err_prev < 0.0 ? 0.9 * p1 : (0.9 * p1) * prev_pow;
+      prev_pow = pa;
+      if (!(factor == factor)) factor = 10.0;
+    }
+  } else {
+    factor = regular ? 0.9 * p1 : 0.2;
+    if (!(factor == factor)) factor = 0.2;
+  }
   if (factor < 0.2) factor = 0.2;
   if (factor > 10.0) factor = 10.0;
   return factor;
@@ -721,6 +809,13 @@ struct DopParams {
   double* ws_err_prev;
   double* ws_prev_pow;
   int* ws_q;
+  // Deferred refinement of terminal crossings (rec != null, max_hits == 1):
+  // the crossing step is saved (save_step) and refine_kernel computes hit_t /
+  // hit_y for every trajectory in refine_list[0 .. *refine_count).
+  double* rec;
+  long long rec_ld;
+  int* refine_list;
+  int* refine_count;
 };
 
 #define HG_RUNNING (-1)
@@ -868,17 +963,11 @@ struct DopLane {
   }
 };
 
+// Lane -> (group, role) for one launch; false for the idle lanes of a warp.
 template <int G>
-__global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
-  constexpr int D = Layout<G>::D;
-  constexpr int NC = Layout<G>::NC;
+__device__ __forceinline__ bool setup_layout(Layout<G>& L, Gather<G>& gat, double* sm_gather, int& traj) {
   const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  Layout<G> L;
-  Gather<G> gat;
-  int traj;
-  __shared__ double sm_gather[(G == 7) ? 4 * 4 * 42 : 1];  // 4 warps x 4 groups
   if constexpr (G == 1) {
     L.role = 6;
     traj = warp * 32 + lane;
@@ -888,36 +977,167 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
     L.base = g * 2;
     L.gmask = 0x3u << L.base;
     traj = warp * 16 + g;
+  } else if constexpr (G == 6) {
+    if (lane >= 30) return false;
+    const int g = lane / 6;
+    L.role = lane % 6;
+    L.base = g * 6;
+    L.gmask = 0x3Fu << L.base;
+    traj = warp * 5 + g;
   } else {
-    if (lane >= 28) return;
+    if (lane >= 28) return false;
     const int g = lane / 7;
     L.role = lane % 7;
     L.base = g * 7;
     L.gmask = 0x7Fu << L.base;
     traj = warp * 4 + g;
-    gat.slot = sm_gather + (wib * 4 + g) * 42;
+    gat.slot = sm_gather + ((threadIdx.x >> 5) * 4 + g) * 42;
   }
-  const bool leader = (G == 1) || (G == 2 && L.role == 0) || (G == 7 && L.role == 6);
-  const bool has_event = p.ev_index >= 0 && p.max_hits > 0;
-  // event component: which lane of the group holds it, and where
-  int ev_r = 0;
-  bool ev_mine = false;
-  int ev_src = lane;
-  if (has_event) {
-    ev_r = L.local(p.ev_index);
+  return true;
+}
+
+template <int G>
+__device__ __forceinline__ bool is_leader(const Layout<G>& L) {
+  return (G == 1) || ((G == 2 || G == 6) && L.role == 0) || (G == 7 && L.role == 6);
+}
+
+// Where the event component lives in a group: its register index r on the
+// owning lane (mine), and the owning lane, which broadcasts g to the group.
+template <int G>
+struct EvCtx {
+  int r = 0;
+  bool mine = false;
+  int src = 0;
+  unsigned gmask = 0;
+  __device__ __forceinline__ EvCtx(const Layout<G>& L, int index) {
+    if (index < 0) return;
+    r = L.local(index);
     if constexpr (G == 1) {
-      ev_mine = true;
+      mine = true;
     } else {
-      ev_mine = (L.role == L.owner(p.ev_index));
-      ev_src = L.base + L.owner(p.ev_index);
+      mine = (L.role == L.owner(index));
+      src = L.base + L.owner(index);
+      gmask = L.gmask;
     }
   }
-  auto bcast_ev = [&](double v) -> double {
+  __device__ __forceinline__ double bcast(double v) const {
     if constexpr (G == 1)
       return v;
     else
-      return __shfl_sync(L.gmask, v, ev_src);
-  };
+      return __shfl_sync(gmask, v, src);
+  }
+};
+
+// _dop853_refine_in_step: bisection for the crossing on the step's dense
+// interpolant (rows F, step size h, g at the step start g_left); returns the
+// crossing as a fraction x of the step.
+template <int G>
+__device__ __forceinline__ double refine_in_step(const EvCtx<G>& ev, const double (&y)[Layout<G>::NC],
+                                                 const double (&F)[7][Layout<G>::NC], double h, double g_left,
+                                                 const DopParams& p) {
+  constexpr int NC = Layout<G>::NC;
+  double fe[7];
+#pragma unroll
+  for (int i = 0; i < 7; ++i) fe[i] = pick<NC>(F[i], ev.r);
+  const double ye = pick<NC>(y, ev.r);
+  double a = 0.0, b = 1.0;
+  double x_hit = -1.0;
+  for (int it = 0; it < 128; ++it) {
+    const double mid = 0.5 * (a + b);
+    const double g_mid = ev.bcast(ev.mine ? (DopLane<G>::eval_row(ye, fe, mid) - p.ev_offset) : 0.0);
+    if (fabs(g_mid) <= p.gtol) {
+      x_hit = mid;
+      break;
+    }
+    if (crossed_direction(g_left, g_mid, p.ev_dir)) {
+      b = mid;
+    } else {
+      a = mid;
+      g_left = g_mid;
+    }
+    if ((b - a) * fabs(h) <= p.xtol) break;
+  }
+  if (x_hit < 0.0) x_hit = b;
+  return x_hit;
+}
+
+// Saved step of a terminal crossing (deferred refinement), structure of
+// arrays with stride rec_ld: y (D), y_new (D), k[0..12] (13 D), h, t, g_left.
+template <int G>
+__device__ __forceinline__ void save_step(const Layout<G>& L, const DopParams& p, int traj, bool leader,
+                                          const double (&y)[Layout<G>::NC], const double (&yh)[Layout<G>::NC],
+                                          const double (&k)[13][Layout<G>::NC], double h, double t, double g_left) {
+  constexpr int D = Layout<G>::D;
+  constexpr int NC = Layout<G>::NC;
+  double* r = p.rec + traj;
+  const long long ld = p.rec_ld;
+#pragma unroll
+  for (int d = 0; d < NC; ++d) {
+    const int c = L.comp(d);
+    r[c * ld] = y[d];
+    r[(D + c) * ld] = yh[d];
+#pragma unroll
+    for (int j = 0; j < 13; ++j) r[(2 * D + j * D + c) * ld] = k[j][d];
+  }
+  if (leader) {
+    r[(15 * D) * ld] = h;
+    r[(15 * D + 1) * ld] = t;
+    r[(15 * D + 2) * ld] = g_left;
+    p.refine_list[atomicAdd(p.refine_count, 1)] = traj;
+  }
+}
+
+// Refinement of the saved terminal crossings, all lanes in lock step: the
+// same dense cache, bisection and interpolation as the inline path.
+template <int G>
+__global__ void __launch_bounds__(128) refine_kernel(DopParams p) {
+  constexpr int D = Layout<G>::D;
+  constexpr int NC = Layout<G>::NC;
+  Layout<G> L;
+  Gather<G> gat;
+  int slot;
+  __shared__ double sm_gather[(G == 7) ? 4 * 4 * 42 : 1];
+  if (!setup_layout<G>(L, gat, sm_gather, slot)) return;
+  const bool leader = is_leader<G>(L);
+  const EvCtx<G> ev(L, p.ev_index);
+  const int n = *p.refine_count;
+  for (; slot < n; slot += p.stride) {
+    const int traj = p.refine_list[slot];
+    const double* r = p.rec + traj;
+    const long long ld = p.rec_ld;
+    double y[NC], yh[NC], k[13][NC];
+#pragma unroll
+    for (int d = 0; d < NC; ++d) {
+      const int c = L.comp(d);
+      y[d] = r[c * ld];
+      yh[d] = r[(D + c) * ld];
+#pragma unroll
+      for (int j = 0; j < 13; ++j) k[j][d] = r[(2 * D + j * D + c) * ld];
+    }
+    const double h = r[(15 * D) * ld];
+    const double t = r[(15 * D + 1) * ld];
+    const double g_left = r[(15 * D + 2) * ld];
+    double F[7][NC];
+    DopLane<G>::dense_cache(L, y, yh, h, p.mu, p.dir, k, F);
+    const double x_hit = refine_in_step<G>(ev, y, F, h, g_left, p);
+    if (leader) p.hit_t[traj] = t + x_hit * h;
+#pragma unroll
+    for (int d = 0; d < NC; ++d) p.hit_y[(long long)L.comp(d) * p.ld + traj] = DopLane<G>::eval1(y[d], F, d, x_hit);
+  }
+}
+
+template <int G>
+__global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
+  constexpr int D = Layout<G>::D;
+  constexpr int NC = Layout<G>::NC;
+  Layout<G> L;
+  Gather<G> gat;
+  int traj;
+  __shared__ double sm_gather[(G == 7) ? 4 * 4 * 42 : 1];  // 4 warps x 4 groups
+  if (!setup_layout<G>(L, gat, sm_gather, traj)) return;
+  const bool leader = is_leader<G>(L);
+  const bool has_event = p.ev_index >= 0 && p.max_hits > 0;
+  const EvCtx<G> ev(L, has_event ? p.ev_index : -1);
 
   int slot = traj;
   while (true) {
@@ -942,7 +1162,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
     // on resume this is bitwise k[12] of the last accepted step
     L.rhs(y, p.mu, p.dir, k[0]);
     double g_prev = 0.0;
-    if (has_event) g_prev = bcast_ev(ev_mine ? (pick<NC>(y, ev_r) - p.ev_offset) : 0.0);
+    if (has_event) g_prev = ev.bcast(ev.mine ? (pick<NC>(y, ev.r) - p.ev_offset) : 0.0);
     double h, t, err_prev, prev_pow;
     int acc, rej, hits, q_next;
     const bool dense = p.m >= 2;
@@ -1012,7 +1232,9 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
         else
           err_norm = (fabs(h) * n5) / sqrt((n5 + 0.01 * n3) * (double)D);
       }
-      if (err_norm <= 1.0) {
+      const bool accepted = err_norm <= 1.0;
+      bool fin = true;
+      if (accepted) {
         ++acc;
         const double t_new = t + h;
         bool stop = false;
@@ -1034,45 +1256,28 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
           }
         }
         if (has_event) {
-          const double g_new = bcast_ev(ev_mine ? (pick<NC>(yh, ev_r) - p.ev_offset) : 0.0);
+          const double g_new = ev.bcast(ev.mine ? (pick<NC>(yh, ev.r) - p.ev_offset) : 0.0);
           if (event_crossed(g_prev, g_new, p.ev_dir)) {
-            // _dop853_refine_in_step with the step size h
-            double F[7][NC];
-            DopLane<G>::dense_cache(L, y, yh, h, p.mu, p.dir, k, F);
-            double fe[7];
+            if (p.rec) {
+              // terminal crossing: keep the step for refine_kernel
+              save_step<G>(L, p, traj, leader, y, yh, k, h, t, g_prev);
+            } else {
+              // _dop853_refine_in_step with the step size h
+              double F[7][NC];
+              DopLane<G>::dense_cache(L, y, yh, h, p.mu, p.dir, k, F);
+              const double x_hit = refine_in_step<G>(ev, y, F, h, g_prev, p);
+              p.hit_t[(long long)hits * p.ld + traj] = t + x_hit * h;
+              double* o = p.hit_y + (long long)hits * D * p.ld;
 #pragma unroll
-            for (int i = 0; i < 7; ++i) fe[i] = pick<NC>(F[i], ev_r);
-            const double ye = pick<NC>(y, ev_r);
-            double a = 0.0, b = 1.0;
-            double g_left = g_prev;
-            double x_hit = -1.0;
-            for (int it = 0; it < 128; ++it) {
-              const double mid = 0.5 * (a + b);
-              const double g_mid = bcast_ev(ev_mine ? (DopLane<G>::eval_row(ye, fe, mid) - p.ev_offset) : 0.0);
-              if (fabs(g_mid) <= p.gtol) {
-                x_hit = mid;
-                break;
-              }
-              if (crossed_direction(g_left, g_mid, p.ev_dir)) {
-                b = mid;
-              } else {
-                a = mid;
-                g_left = g_mid;
-              }
-              if ((b - a) * fabs(h) <= p.xtol) break;
+              for (int d = 0; d < NC; ++d)
+                o[(long long)L.comp(d) * p.ld + traj] = DopLane<G>::eval1(y[d], F, d, x_hit);
             }
-            if (x_hit < 0.0) x_hit = b;
-            p.hit_t[(long long)hits * p.ld + traj] = t + x_hit * h;
-            double* o = p.hit_y + (long long)hits * D * p.ld;
-#pragma unroll
-            for (int d = 0; d < NC; ++d) o[(long long)L.comp(d) * p.ld + traj] = DopLane<G>::eval1(y[d], F, d, x_hit);
             ++hits;
             if (hits >= p.max_hits) stop = true;
           }
           g_prev = g_new;
         }
         t = t_new;
-        bool fin = true;
 #pragma unroll
         for (int d = 0; d < NC; ++d) {
           y[d] = yh[d];
@@ -1080,7 +1285,11 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
           fin = fin && finite_bits(yh[d]);
         }
         if (stop) break;
-        h = h * pi_accept_factor(err_norm, err_prev, prev_pow);
+      } else {
+        ++rej;
+      }
+      h = h * pi_factor<G>(L, accepted, err_norm, err_prev, prev_pow);
+      if (accepted) {
         err_prev = err_norm;
         if constexpr (G > 1) fin = __all_sync(L.gmask, fin);
         if (!fin) {
@@ -1088,8 +1297,6 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
           break;
         }
       } else {
-        ++rej;
-        h = h * pi_reject_factor(err_norm);
         h = clamp_step(h, p.max_step, p.min_step);
       }
     }

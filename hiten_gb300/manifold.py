@@ -117,11 +117,11 @@ def compute(x0, period, mu, stable=True, direction=1, step=0.02, integration_fra
 
 
 def propagate_to_plane(seeds_arr, mu, tf=8.0, forward=-1, plane_index=0, plane_offset=None, rtol=1e-12,
-                       atol=1e-12, max_hits=1, device=None):
+                       atol=1e-12, max_hits=1, device=None, **kw):
     """DOP853 from every seed to |t| = tf or the first crossing of
     y[plane_index] = plane_offset (default x = 1 - mu), as a terminal event."""
     if plane_offset is None:
         plane_offset = 1.0 - mu
     ev = P.EventSpec(index=plane_index, offset=float(plane_offset), direction=0, max_hits=max_hits)
     return P.propagate_dop853(seeds_arr, 0.0, float(tf), mu, rtol=rtol, atol=atol, max_step=1e4, fwd=forward,
-                              flip=(0, 6), event=ev, device=device)
+                              flip=(0, 6), event=ev, device=device, **kw)

@@ -137,7 +137,8 @@ class Dop853Result:
 
 def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min_step=None,
                      max_steps=100_000, fwd=1, flip=None, event=None, n_samples=0, sample_last_only=False,
-                     device=None, stream=None, segmented=False, seg_steps=16, max_segments=8):
+                     device=None, stream=None, segmented=False, seg_steps=16, max_segments=8,
+                     scheduled=False):
     """Adaptive DOP853 for N states from t0 to tmax (scalars or (N,) arrays).
 
     Mirrors integrators/rk.py:2375-2549 / :2678-2803 step for step.
@@ -146,7 +147,9 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
     ``segmented``: run in launches of at most ``seg_steps`` attempted steps per
     trajectory (``max_segments`` launches per asynchronous call, repeated until
     every trajectory finished), compacting the live trajectories between
-    launches; results are bit-identical.
+    launches; results are bit-identical.  ``scheduled``: host-scheduled
+    segments (``hg_propagate_dop853_scheduled``): the layout of each segment
+    follows the number of trajectories still running; synchronous.
     """
     dev = _device(device)
     y0 = torch.as_tensor(y0, dtype=torch.float64)
@@ -193,10 +196,14 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
             C.byref(evp) if evp is not None else None, int(n_samples), 1 if sample_last_only else 0, _ptr(samples),
             _ptr(y_end), _ptr(t_end), _ptr(hit_t), _ptr(hit_y), _ptr(n_hits), _ptr(n_acc), _ptr(n_rej), _ptr(status))
     with torch.cuda.device(dev):
-        if not segmented:
+        if scheduled:
+            ws_bytes = int(H.lib.hg_dop853_segmented_workspace_bytes(N, dim))
+            ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
+            H.check(H.lib.hg_propagate_dop853_scheduled(*args, _ptr(ws), ws_bytes, st))
+        elif not segmented:
             H.check(H.lib.hg_propagate_dop853(*args, st))
         else:
-            ws_bytes = int(H.lib.hg_dop853_segmented_workspace_bytes(N))
+            ws_bytes = int(H.lib.hg_dop853_segmented_workspace_bytes(N, dim))
             ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
             segs = int(max_segments)
             resume = 0
@@ -231,22 +238,26 @@ def fp64_peak_tflops(device=None):
 
 class tuning:
     """Set the launch shape of the device's handle (results are unchanged):
-    ``lanes_d6`` in {0 (auto), 1, 2} lanes per 6-dim DOP853 trajectory,
-    ``block`` in {32, 64, 128} threads per block.  Usable as a context
-    manager (restores the previous values on exit) or as a plain call."""
+    ``lanes_d6`` in {0 (auto), 1, 2, 6} lanes per 6-dim DOP853 trajectory,
+    ``block`` in {32, 64, 128} threads per block, ``seg_steps`` attempted
+    steps per segment of the scheduled driver.  Usable as a context manager
+    (restores the previous values on exit) or as a plain call."""
 
-    def __init__(self, lanes_d6=None, block=None, device=None):
+    _KEYS = (("lanes_d6", _lib.HG_TUNE_DOP853_LANES_D6), ("block", _lib.HG_TUNE_BLOCK_THREADS),
+             ("seg_steps", _lib.HG_TUNE_SEG_STEPS))
+
+    def __init__(self, lanes_d6=None, block=None, device=None, seg_steps=None):
         dev = _device(device)
         self.H = _lib.handle(dev.index or 0)
-        self.old = (self.H.get_tuning(_lib.HG_TUNE_DOP853_LANES_D6), self.H.get_tuning(_lib.HG_TUNE_BLOCK_THREADS))
-        if lanes_d6 is not None:
-            self.H.set_tuning(_lib.HG_TUNE_DOP853_LANES_D6, lanes_d6)
-        if block is not None:
-            self.H.set_tuning(_lib.HG_TUNE_BLOCK_THREADS, block)
+        self.old = {k: self.H.get_tuning(key) for k, key in self._KEYS}
+        new = {"lanes_d6": lanes_d6, "block": block, "seg_steps": seg_steps}
+        for k, key in self._KEYS:
+            if new[k] is not None:
+                self.H.set_tuning(key, new[k])
 
     def __enter__(self):
         return self
 
     def __exit__(self, *exc):
-        self.H.set_tuning(_lib.HG_TUNE_DOP853_LANES_D6, self.old[0])
-        self.H.set_tuning(_lib.HG_TUNE_BLOCK_THREADS, self.old[1])
+        for k, key in self._KEYS:
+            self.H.set_tuning(key, self.old[k])

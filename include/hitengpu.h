@@ -138,11 +138,12 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N,
  * captured in a CUDA graph.  State persists in the outputs (y_end, t_end,
  * n_accept, n_reject, n_hits, status -- all required; status = -1 marks a
  * trajectory still running) and in `workspace` (caller device memory of at
- * least hg_dop853_segmented_workspace_bytes(N) bytes); resume = 1 continues
+ * least hg_dop853_segmented_workspace_bytes(N, dim) bytes; -1 for an invalid
+ * N or dim); resume = 1 continues
  * a previous call's unfinished trajectories.  Results are bit-identical to
  * hg_propagate_dop853.
  * Replaces: as hg_propagate_dop853 (execution schedule only). */
-long long hg_dop853_segmented_workspace_bytes(int N);
+long long hg_dop853_segmented_workspace_bytes(int N, int dim);
 int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N,
                                   const double* y0, long long ld,
                                   const double* t0_arr, const double* tmax_arr,
@@ -153,6 +154,30 @@ int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N,
                                   double* hit_t, double* hit_y, int* n_hits,
                                   int* n_accept, int* n_reject, int* status,
                                   int seg_steps, int max_segments, int resume,
+                                  void* workspace, long long workspace_bytes,
+                                  void* stream);
+
+/* hg_propagate_dop853 run as host-scheduled segments: each segment advances
+ * every live trajectory by up to HG_TUNE_SEG_STEPS attempted steps, the
+ * trajectories still running are compacted into a dense list, and the host
+ * reads their count back before the next segment.  For a 6-dim system the
+ * layout of each segment (1, 2 or 6 lanes per trajectory) is chosen from that
+ * count unless HG_TUNE_DOP853_LANES_D6 fixes it: wide layouts for the few
+ * long trajectories at the end of an uneven batch cut the per-step latency
+ * that bounds it.  Synchronous: returns when every trajectory has finished
+ * (it synchronizes `stream` once per segment).  Same arguments and state
+ * requirements as hg_propagate_dop853_segmented; results are bit-identical
+ * to hg_propagate_dop853.
+ * Replaces: as hg_propagate_dop853 (execution schedule only). */
+int hg_propagate_dop853_scheduled(hg_handle* h, double mu, int dim, int N,
+                                  const double* y0, long long ld,
+                                  const double* t0_arr, const double* tmax_arr,
+                                  double t0, double tmax,
+                                  const hg_dop853_opts* opts, const hg_event* ev,
+                                  int n_samples, int sample_last_only, double* y_samples,
+                                  double* y_end, double* t_end,
+                                  double* hit_t, double* hit_y, int* n_hits,
+                                  int* n_accept, int* n_reject, int* status,
                                   void* workspace, long long workspace_bytes,
                                   void* stream);
 
@@ -213,13 +238,17 @@ int hg_trajectory_filters(int N, int m, const double* samples, long long ld, dou
 /* Launch-shape tuning of a handle (set by hiten_gb300.autotune).
  * HG_TUNE_BLOCK_THREADS: threads per block, 32 (default), 64 or 128.
  * HG_TUNE_DOP853_LANES_D6: lanes per 6-dim DOP853 trajectory: 1 (one
- * trajectory per lane: least total work), 2 (lane pairs: about half the
- * per-step latency, for batches too small to fill the GPU, where the
- * longest trajectory sets the time), 0 = automatic (the default).
+ * trajectory per lane: least total work), 2 (lane pairs: 0.62x the per-step
+ * latency), 6 (one component per lane: 0.40x), for batches too small to
+ * fill the GPU, where the longest trajectory sets the time; 0 = automatic
+ * (the default).
+ * HG_TUNE_SEG_STEPS: attempted steps per segment of
+ * hg_propagate_dop853_scheduled (default 16).
  * Results are bit-identical for every setting.
  * Replaces: nothing (no reference counterpart; launch shape only). */
 #define HG_TUNE_BLOCK_THREADS 1
 #define HG_TUNE_DOP853_LANES_D6 2
+#define HG_TUNE_SEG_STEPS 3
 int hg_set_tuning(hg_handle* h, int key, int value);
 int hg_get_tuning(hg_handle* h, int key, int* value);
 

@@ -37,7 +37,7 @@ def _same(a, b, with_event=False, samples=False):
         assert np.array_equal(_np(a.samples), _np(b.samples))
 
 
-@pytest.mark.parametrize("lanes", [1, 2])
+@pytest.mark.parametrize("lanes", [1, 2, 6])
 @pytest.mark.parametrize("seg_steps,max_segments", SEGS)
 def test_segmented_manifold_event(gpu, lanes, seg_steps, max_segments):
     rng = np.random.default_rng(11)
@@ -94,3 +94,35 @@ def dev_oracle(oracle):
     oracle.set_mode(oracle.MODE_DEVICE)
     yield oracle
     oracle.set_mode(oracle.MODE_PYTHON)
+
+
+@pytest.mark.parametrize("seg_steps", [1, 4, 16])
+@pytest.mark.parametrize("lanes", [0, 1, 2, 6])
+def test_scheduled_layout_switching(gpu, seg_steps, lanes):
+    """A batch wide enough that the automatic policy passes through every
+    layout (1 -> 2 -> 6 lanes) as trajectories finish; bits as single pass."""
+    rng = np.random.default_rng(5)
+    n = 12000 if seg_steps > 1 else 3500
+    y0 = W.HALO_L1_AZ02_X0 + rng.uniform(-1e-4, 1e-4, (n, 6)) * np.logspace(-3, 0, n)[:, None]
+    tmax = rng.uniform(1.0, 8.0, n)
+    ev = gpu.EventSpec(index=0, offset=1 - MU, direction=0, max_hits=1)
+    ref = gpu.propagate_dop853(y0, 0.0, tmax, MU, fwd=-1, flip=(0, 6), event=ev)
+    with gpu.tuning(lanes_d6=lanes, seg_steps=seg_steps):
+        sch = gpu.propagate_dop853(y0, 0.0, tmax, MU, fwd=-1, flip=(0, 6), event=ev, scheduled=True)
+    _same(ref, sch, with_event=True)
+
+
+def test_scheduled_stm_dense_and_max_steps(gpu):
+    x0 = W.HALO_L1_AZ02_X0
+    y0 = np.array([stm_state(x0 + d) for d in np.linspace(-1e-4, 1e-4, 9)[:, None] * np.eye(6)[0]])
+    T = W.HALO_L1_AZ02_T
+    ref = gpu.propagate_dop853(y0, 0.0, T, MU, fwd=-1, flip=(36, 42), n_samples=40)
+    with gpu.tuning(seg_steps=3):
+        sch = gpu.propagate_dop853(y0, 0.0, T, MU, fwd=-1, flip=(36, 42), n_samples=40, scheduled=True)
+    _same(ref, sch, samples=True)
+    y6 = W.section_states(40, seed=3)
+    ref = gpu.propagate_dop853(y6, 0.0, 20.0, MU, rtol=1e-11, atol=1e-11, max_steps=7)
+    with gpu.tuning(seg_steps=2):
+        sch = gpu.propagate_dop853(y6, 0.0, 20.0, MU, rtol=1e-11, atol=1e-11, max_steps=7, scheduled=True)
+    _same(ref, sch)
+    assert np.all(_np(sch.status) == 1)
