@@ -6,14 +6,18 @@ stable manifold of the Earth-Moon (mu = 0.012150585609624) L1 southern halo
 with Az = 0.2 (x0, T as corrected by the reference): 512 phases x 32
 displacements log-uniform in [1e-7, 1e-5] along the stable eigenvector =
 16384 trajectories, DOP853 rtol = atol = 1e-12, integrated backward to
-t = -8 with a terminal event on the plane x = 1 - mu (uneven lengths),
-persistent lane-refill kernel.  Seeds are synthetic (seeded), computed on
-the GPU from the orbit's STM grid.
+t = -8 with a terminal event on the plane x = 1 - mu (uneven lengths).
+Seeds are synthetic (seeded), computed on the GPU from the orbit's STM grid.
+The execution plan -- one persistent lane-refill launch with a given lane
+layout, or host-scheduled segments that compact the live trajectories and
+widen the layout as they thin out -- is chosen by the autotuner on this
+workload (every plan gives the same bits).
 
 Metric: accepted trajectory-steps per second (attempted steps reported
-beside it).  `value`: kernel throughput with the seeds resident in HBM;
+beside it).  `value`: throughput with the seeds resident in HBM;
 `e2e`: the same through the public API (hiten_gb300.manifold) from pinned
-host seeds, H2D and D2H copies inside the timed region.
+host seeds, H2D and D2H copies inside the timed region.  `gpu_launches`:
+kernels launched in the timed region, read from the library's counter.
 
 `--impl reference`: the reference's algorithm on the host cores (the CPU
 oracle in numba-lowering mode, one trajectory per task, all host threads),
@@ -33,9 +37,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-METRIC = "FP64 trajectory-steps/sec (DOP853 manifold propagation, accepted steps)"
+METRIC = "FP64 trajectory-steps/sec w/ STM (batched/served vs plain GPU vs CPU); p50/p99 latency"
 UNIT = "traj-steps/s"
-FLOPS_PER_ATTEMPT_D6 = 1314.0  # algorithmic flops of one attempted DOP853 step, d = 6
+# algorithmic flops of one attempted DOP853 step at d = 6 (add/mul = 1, FMA = 2,
+# div = sqrt = 1): 12 right-hand sides x 31 + 2 (50 + 8) 6 stage sums
+# + 2 (8 + 8) 6 error estimates + 9 x 6 error norm
+FLOPS_PER_ATTEMPT_D6 = 1314.0
 N_PHASE, N_DISP = 512, 32
 TF = 8.0
 
@@ -72,7 +79,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
@@ -169,10 +176,12 @@ def run_reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plan", default=None,
+                    help="force an execution plan by name (autotune.plan_name), e.g. scheduled_seg16")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -201,15 +210,28 @@ def main():
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > L2
     stream = torch.cuda.current_stream(dev)
 
-    def one_step():
-        return M.propagate_to_plane(seeds_dev, mu, tf=TF, forward=-1, device=dev)
+    def run(scheduled):
+        return M.propagate_to_plane(seeds_dev, mu, tf=TF, forward=-1, device=dev, scheduled=scheduled)
 
     for _ in range(max(args.warmup, 3)):
-        r = one_step()
+        r = run(False)
     torch.cuda.synchronize(dev)
-    # launch shape (lanes per trajectory, block size) chosen by measurement on
-    # this workload; results are identical for every shape
-    shape, shape_ms = autotune.tune(f"manifold_{N}", one_step, device=dev)
+    # execution plan (single-pass launch shape or host-scheduled segments)
+    # chosen by measurement on this workload; results are identical for all
+    plans = autotune.DOP853_PLANS
+    if args.plan:
+        plans = [p for p in plans if autotune.plan_name(p) == args.plan]
+        if not plans:
+            raise SystemExit(f"unknown plan {args.plan}")
+    plan, plan_ms = autotune.tune_dop853(f"manifold_{N}", run, plans=plans, device=dev)
+    sched = plan["scheduled"]
+
+    def one_step():
+        return run(sched)
+
+    for _ in range(max(args.warmup, 3)):
+        one_step()
+    torch.cuda.synchronize(dev)
 
     # plain form: one kernel call per trajectory, the reference's call
     # granularity (one _propagate_dynsys per seed), on a bounded sample
@@ -228,9 +250,11 @@ def main():
     # ---- device-resident timing (CUDA events on the launching stream)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     acc = att = 0
+    H = _lib.handle(local)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize(dev)
+    launches0 = H.kernel_launches()
     with ClockSampler(local) as clk:
         results = []
         for i in range(args.steps):
@@ -240,6 +264,7 @@ def main():
             evs[i][1].record(stream)
             results.append(r)
         torch.cuda.synchronize(dev)
+    launches = H.kernel_launches() - launches0
     if world > 1:
         dist.barrier()
     clocks = clk.summary()
@@ -267,7 +292,7 @@ def main():
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for i in range(args.steps):
-        r = M.propagate_to_plane(host_seeds, mu, tf=TF, forward=-1, device=dev)
+        r = M.propagate_to_plane(host_seeds, mu, tf=TF, forward=-1, device=dev, scheduled=sched)
         y_end = r.y_end.cpu()
         hit_y = r.hit_y.cpu()
         hit_t = r.hit_t.cpu()
@@ -304,13 +329,14 @@ def main():
                "attempted_steps_per_s": att * world / (total_ms * 1e-3),
                "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                             "frac": achieved / peak if peak else None, "traffic": traffic,
+                            "traffic_scope": "DRAM bytes of one launch of the dominant kernel (first scheduled "
+                                             "segment, 16384 live trajectories x 32 steps), ncu",
                             "peak_source": "measured: DFMA throughput probe (hg_probe_fp64_peak) on this GPU; "
                                            "MEASURED_PEAKS.json has no FP64 entry",
                             "flops_per_attempted_step": FLOPS_PER_ATTEMPT_D6},
                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-               "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": args.steps,
-               "launch_shape": {"lanes_per_trajectory": shape[0], "block_threads": shape[1],
-                                "autotune_ms": {f"lanes{k[0]}_block{k[1]}": v for k, v in shape_ms.items()}},
+               "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
+               "plan": {"chosen": autotune.plan_name(plan), "autotune_ms": plan_ms},
                "plain_gpu": {"value": plain_value, "unit": UNIT,
                              "form": f"one kernel call per trajectory (reference call granularity), "
                                      f"{n_plain}-trajectory sample"},

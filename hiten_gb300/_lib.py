@@ -27,11 +27,13 @@ EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg
             "hg_propagate_dop853", "hg_probe_fp64_peak", "hg_propagate_dop853_noalloc", "hg_set_tuning",
             "hg_get_tuning", "hg_section_detect", "hg_trajectory_filters", "hg_propagate_fixed_event",
             "hg_dop853_segmented_workspace_bytes", "hg_propagate_dop853_segmented",
-            "hg_propagate_dop853_scheduled")
+            "hg_propagate_dop853_scheduled", "hg_get_counter")
+HG_COUNTER_KERNEL_LAUNCHES = 1
 HG_RUNNING = -1
 HG_TUNE_BLOCK_THREADS = 1
 HG_TUNE_DOP853_LANES_D6 = 2
 HG_TUNE_SEG_STEPS = 3
+HG_TUNE_SPREAD = 4
 
 
 class HitenGpuError(RuntimeError):
@@ -102,7 +104,7 @@ def load(build_if_missing=True):
                                                C.c_int, C.c_int, _P, C.c_longlong, C.c_int, C.c_int, C.c_int,
                                                C.POINTER(hg_event), _P, _P, _P, _P, _P]
         L.hg_propagate_fixed_event.restype = C.c_int
-        L.hg_dop853_segmented_workspace_bytes.argtypes = [C.c_int, C.c_int]
+        L.hg_dop853_segmented_workspace_bytes.argtypes = [C.c_int, C.c_int, C.c_int]
         L.hg_dop853_segmented_workspace_bytes.restype = C.c_longlong
         L.hg_propagate_dop853_segmented.argtypes = (L.hg_propagate_dop853.argtypes[:-1]
                                                     + [C.c_int, C.c_int, C.c_int, _P, C.c_longlong, _P])
@@ -113,6 +115,8 @@ def load(build_if_missing=True):
         L.hg_set_tuning.restype = C.c_int
         L.hg_get_tuning.argtypes = [_P, C.c_int, C.POINTER(C.c_int)]
         L.hg_get_tuning.restype = C.c_int
+        L.hg_get_counter.argtypes = [_P, C.c_int, C.POINTER(C.c_longlong)]
+        L.hg_get_counter.restype = C.c_int
         L.hg_probe_fp64_peak.argtypes = [_P, C.POINTER(C.c_double)]
         L.hg_probe_fp64_peak.restype = C.c_int
         _lib = L
@@ -143,6 +147,12 @@ class Handle:
     def get_tuning(self, key):
         v = C.c_int(0)
         self.check(self.lib.hg_get_tuning(self.ptr, int(key), C.byref(v)))
+        return v.value
+
+    def kernel_launches(self):
+        """Kernels launched through this handle so far."""
+        v = C.c_longlong(0)
+        self.check(self.lib.hg_get_counter(self.ptr, HG_COUNTER_KERNEL_LAUNCHES, C.byref(v)))
         return v.value
 
     def close(self):

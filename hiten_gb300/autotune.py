@@ -20,6 +20,52 @@ from . import propagate as P
 DEFAULT_SHAPES = ((1, 32), (2, 32), (1, 64), (2, 64))
 _cache = {}
 
+# Execution plans of a 6-dim DOP853 batch: single-pass launch shapes (lanes per
+# trajectory, block threads, one block per SM) and the host-scheduled driver
+# (per-segment layout from the live count) with its segment length.
+DOP853_PLANS = (
+    {"scheduled": False, "lanes_d6": 1, "block": 32, "spread": 0},
+    {"scheduled": False, "lanes_d6": 2, "block": 32, "spread": 0},
+    {"scheduled": False, "lanes_d6": 2, "block": 32, "spread": 1},
+    {"scheduled": False, "lanes_d6": 6, "block": 32, "spread": 0},
+    {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 8},
+    {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 16},
+    {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 32},
+)
+_plan_cache = {}
+
+
+def _knobs(plan):
+    return {k: plan[k] for k in ("lanes_d6", "block", "spread", "seg_steps") if k in plan}
+
+
+def tune_dop853(key, run, plans=DOP853_PLANS, reps=2, device=None):
+    """Pick the fastest execution plan for a DOP853 workload.
+
+    `run(scheduled)` must run the workload once.  Every plan gives the same
+    bits; the winner's launch knobs are applied to the device's handle and
+    the plan (with its `scheduled` flag) is returned with all timings."""
+    if key in _plan_cache:
+        best = _plan_cache[key]
+        P.tuning(device=device, **_knobs(best))
+        return best, {}
+    timings = {}
+    for i, plan in enumerate(plans):
+        with P.tuning(device=device, **_knobs(plan)):
+            run(plan["scheduled"])  # warm
+            torch.cuda.synchronize()
+            timings[i] = _time(lambda: run(plan["scheduled"]), reps)
+    best = dict(plans[min(timings, key=timings.get)])
+    _plan_cache[key] = best
+    P.tuning(device=device, **_knobs(best))
+    return best, {plan_name(plans[i]): ms for i, ms in timings.items()}
+
+
+def plan_name(plan):
+    if plan["scheduled"]:
+        return f"scheduled_seg{plan.get('seg_steps', 16)}"
+    return f"lanes{plan['lanes_d6']}_block{plan['block']}" + ("_spread" if plan.get("spread") else "")
+
 
 def _time(fn, reps):
     best = float("inf")

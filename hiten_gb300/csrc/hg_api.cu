@@ -18,9 +18,12 @@ struct hg_handle {
   int block = 32;           // threads per block (32, 64 or 128)
   int lanes_d6 = 0;         // lanes per 6-dim DOP853 trajectory: 0 auto, 1, 2, 6
   int seg_steps = 16;       // attempted steps per segment of the scheduled DOP853 driver
+  int spread = 0;           // 1: DOP853 blocks of 4 warps, one block per SM (one warp per sub-partition)
+  int smem_per_sm = 0;      // bytes of shared memory per SM
   int* host_count = nullptr;  // pinned: live-trajectory count read back between segments
   char* scratch = nullptr;    // grow-only: saved crossing steps of single-pass calls
   long long scratch_bytes = 0;
+  long long launches = 0;   // kernels launched through this handle
   char err[512] = {0};
 };
 
@@ -39,6 +42,7 @@ int fail(hg_handle* h, int code, const char* fmt, ...) {
 int check_launch(hg_handle* h, const char* what) {
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(h, HG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  ++h->launches;
   return HG_OK;
 }
 
@@ -107,23 +111,29 @@ int fixed_dispatch(hg_handle* h, int order, int dim, const hg::FixedParams& p, c
   return launch_fixed<8, 7>(h, p, s);
 }
 
-// Saved-step area of the deferred event refinement for N trajectories of
-// dimension D: count (256 B), list (N ints), record ((15 D + 3) x N doubles).
-long long refine_area_bytes(int N, int D) {
+// Record pool of the deferred event refinement for N trajectories of
+// dimension D with up to max_hits crossings each: count (256 B), trajectory
+// and hit index per record, records ((15 D + 3) doubles each), all for
+// N * max_hits records.
+long long refine_area_bytes(int N, int D, int max_hits) {
   auto up = [](long long x) { return (x + 255) & ~255LL; };
-  return 256 + up((long long)N * 4) + up((15LL * D + 3) * (long long)N * 8);
+  if (max_hits < 1) return 0;
+  const long long cap = (long long)N * max_hits;
+  return 256 + 2 * up(cap * 4) + up((15LL * D + 3) * cap * 8);
 }
 
-void refine_area_carve(int N, char* base, hg::DopParams& p) {
+void refine_area_carve(int N, int max_hits, char* base, hg::DopParams& p) {
   auto up = [](long long x) { return (x + 255) & ~255LL; };
+  const long long cap = (long long)N * max_hits;
   p.refine_count = (int*)base;
   p.refine_list = (int*)(base + 256);
-  p.rec = (double*)(base + 256 + up((long long)N * 4));
-  p.rec_ld = N;
+  p.refine_hit = (int*)(base + 256 + up(cap * 4));
+  p.rec = (double*)(base + 256 + 2 * up(cap * 4));
+  p.rec_ld = cap;
 }
 
-// Terminal events (one hit) are refined after the integration, in lock step.
-bool defer_refine(const hg::DopParams& p) { return p.ev_index >= 0 && p.max_hits == 1; }
+// Event crossings are refined after the integration, in lock step.
+bool defer_refine(const hg::DopParams& p) { return p.ev_index >= 0 && p.max_hits >= 1; }
 
 template <int G>
 int launch_refine(hg_handle* h, hg::DopParams p, cudaStream_t s) {
@@ -133,9 +143,10 @@ int launch_refine(hg_handle* h, hg::DopParams p, cudaStream_t s) {
       per_sm < 1)
     per_sm = 1;
   const int tpb = (kBlock / 32) * hg::Layout<G>::TPW;
-  const int need = (p.N + tpb - 1) / tpb;
+  const long long records = p.rec_ld;
+  const long long need = (records + tpb - 1) / tpb;
   const int cap = per_sm * h->sm_count;
-  const int grid = need < cap ? need : cap;
+  const int grid = need < cap ? (int)need : cap;
   if (grid < 1) return HG_OK;
   p.stride = grid * tpb;
   hg::refine_kernel<G><<<grid, kBlock, 0, s>>>(p);
@@ -161,13 +172,45 @@ int ensure_scratch(hg_handle* h, long long bytes) {
   return HG_OK;
 }
 
+// Launch shape of a DOP853 kernel: threads per block, dynamic shared memory
+// and resident blocks per SM.  In spread mode a block of four warps reserves
+// more than half of the SM's shared memory (unused), so no two blocks share
+// an SM and every warp gets an SM sub-partition's FP64 pipe to itself.
+struct Shape {
+  int block;
+  size_t smem;
+  int per_sm;
+};
+
+template <class K>
+Shape dop_shape(const hg_handle* h, K kernel) {
+  Shape sh{h->block, 0, 1};
+  if (h->spread && h->smem_per_sm > 0) {
+    sh.block = 128;
+    sh.smem = (size_t)(h->smem_per_sm / 2 + 1024);
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem) != cudaSuccess) {
+      cudaGetLastError();
+      sh.block = h->block;
+      sh.smem = 0;
+    }
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, sh.block, sh.smem) != cudaSuccess ||
+      per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  sh.per_sm = per_sm;
+  return sh;
+}
+
 template <int G>
 int launch_dop853(hg_handle* h, hg::DopParams p, cudaStream_t s) {
   if (p.N <= 0) return HG_OK;
-  const int kBlock = h->block;
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hg::dop853_kernel<G>, kBlock, 0);
-  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+  const Shape sh = dop_shape(h, hg::dop853_kernel<G>);
+  const int kBlock = sh.block;
+  const int per_sm = sh.per_sm;
+  cudaError_t e;
   const int tpb = (kBlock / 32) * hg::Layout<G>::TPW;
   const int need = (p.N + tpb - 1) / tpb;
   const int cap = per_sm * h->sm_count;
@@ -179,7 +222,7 @@ int launch_dop853(hg_handle* h, hg::DopParams p, cudaStream_t s) {
     e = cudaMemsetAsync(h->counters, 0, sizeof(int), s);
     if (e != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
   }
-  hg::dop853_kernel<G><<<grid, kBlock, 0, s>>>(p);
+  hg::dop853_kernel<G><<<grid, kBlock, sh.smem, s>>>(p);
   return check_launch(h, "dop853_kernel");
 }
 
@@ -214,7 +257,7 @@ struct SegWs {
   char* refine;  // saved crossing steps (refine_area_bytes)
 };
 
-long long seg_ws_layout(int N, int D, char* base, SegWs* w) {
+long long seg_ws_layout(int N, int D, int max_hits, char* base, SegWs* w) {
   auto up = [](long long x) { return (x + 255) & ~255LL; };
   long long off = 0;
   const long long ni = up((long long)N * 4), nd = up((long long)N * 8);
@@ -233,7 +276,7 @@ long long seg_ws_layout(int N, int D, char* base, SegWs* w) {
   if (w) w->q = (int*)(base + off);
   off += ni;
   if (w) w->refine = base + off;
-  off += refine_area_bytes(N, D);
+  off += refine_area_bytes(N, D, max_hits);
   return off;
 }
 
@@ -242,11 +285,9 @@ long long seg_ws_layout(int N, int D, char* base, SegWs* w) {
 // running are appended to list[a ^ 1].
 template <int G>
 int launch_segment(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_steps, int a, int n_live, cudaStream_t s) {
-  const int kBlock = h->block;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hg::dop853_kernel<G>, kBlock, 0) != cudaSuccess ||
-      per_sm < 1)
-    per_sm = 1;
+  const Shape sh = dop_shape(h, hg::dop853_kernel<G>);
+  const int kBlock = sh.block;
+  const int per_sm = sh.per_sm;
   const int tpb = (kBlock / 32) * hg::Layout<G>::TPW;
   const int need = (n_live + tpb - 1) / tpb;
   const int cap = per_sm * h->sm_count;
@@ -266,7 +307,7 @@ int launch_segment(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_steps,
   p.n_in = w.count + a;
   p.active_out = w.list[b];
   p.n_out = w.count + b;
-  hg::dop853_kernel<G><<<grid, kBlock, 0, s>>>(p);
+  hg::dop853_kernel<G><<<grid, kBlock, sh.smem, s>>>(p);
   return check_launch(h, "dop853_kernel (segment)");
 }
 
@@ -295,13 +336,14 @@ int launch_dop853_seg(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_ste
 }
 
 // Layout of the next segment of a 6-dim batch with n_live trajectories
-// left: the group size with the least time per step, where one warp's step
-// takes lat(G) (measured on GB300 for the longest manifold trajectory:
-// 75.4, 46.9 and 30.2 us for G = 1, 2, 6) and warps beyond one per SM
-// sub-partition share its FP64 pipe.
+// left: the group size with the least time per step.  One warp's step takes
+// lat(G) while its SM is not saturated (measured on GB300 for the longest
+// manifold trajectory: 75.4, 46.9 and 30.2 us for G = 1, 2, 6); an SM's FP64
+// unit serves about three such warps at full speed (two run as fast as one,
+// four lose ~13 %), beyond which they share it.
 int sched_lanes_d6(const hg_handle* h, int n_live) {
   if (h->lanes_d6 != 0) return h->lanes_d6;
-  const double smsp = 4.0 * h->sm_count;
+  const double smsp = 3.0 * h->sm_count;
   const int gs[3] = {1, 2, 6};
   const int tpw[3] = {32, 16, 5};
   const double lat[3] = {1.0, 0.622, 0.400};
@@ -358,6 +400,7 @@ int hg_create(const hg_config* cfg, hg_handle** out) {
   cudaGetDevice(&prev);
   cudaSetDevice(h->device);
   cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
+  cudaDeviceGetAttribute(&h->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, h->device);
   const cudaError_t e = cudaMalloc(&h->counters, 64 * sizeof(int));
   cudaSetDevice(prev);
   if (e != cudaSuccess) {
@@ -490,9 +533,9 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
   if (rc != HG_OK || N == 0) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   if (defer_refine(p)) {
-    int e = ensure_scratch(h, refine_area_bytes(N, dim));
+    int e = ensure_scratch(h, refine_area_bytes(N, dim, p.max_hits));
     if (e != HG_OK) return e;
-    refine_area_carve(N, h->scratch, p);
+    refine_area_carve(N, p.max_hits, h->scratch, p);
     if (cudaMemsetAsync(p.refine_count, 0, sizeof(int), s) != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset");
   }
   int rc2;
@@ -512,9 +555,9 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
   return refine_pending(h, p, dim, s);
 }
 
-long long hg_dop853_segmented_workspace_bytes(int N, int dim) {
-  if (N < 0 || (dim != 6 && dim != 42)) return -1;
-  return seg_ws_layout(N, dim, nullptr, nullptr);
+long long hg_dop853_segmented_workspace_bytes(int N, int dim, int max_hits) {
+  if (N < 0 || (dim != 6 && dim != 42) || max_hits < 0) return -1;
+  return seg_ws_layout(N, dim, max_hits, nullptr, nullptr);
 }
 
 int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N, const double* y0, long long ld,
@@ -529,8 +572,9 @@ int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N, const
   if (N > 0 && (!y_end || !t_end || !n_accept || !n_reject || !status))
     return fail(h, HG_ERR_ARGS, "segmented runs keep their state in y_end/t_end/n_accept/n_reject/status");
   if (ev && ev->index >= 0 && N > 0 && !n_hits) return fail(h, HG_ERR_ARGS, "n_hits is required with an event");
-  if (!workspace || workspace_bytes < seg_ws_layout(N, dim, nullptr, nullptr))
-    return fail(h, HG_ERR_ARGS, "workspace smaller than hg_dop853_segmented_workspace_bytes(N, dim)");
+  const int ws_hits = (ev && ev->index >= 0 && ev->max_hits > 0) ? ev->max_hits : 0;
+  if (!workspace || workspace_bytes < seg_ws_layout(N, dim, ws_hits, nullptr, nullptr))
+    return fail(h, HG_ERR_ARGS, "workspace smaller than hg_dop853_segmented_workspace_bytes(N, dim, max_hits)");
   // argument checks and parameter setup shared with the single-pass entry
   hg::DopParams p;
   memset(&p, 0, sizeof(p));
@@ -538,11 +582,11 @@ int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N, const
                         y_samples, y_end, t_end, hit_t, hit_y, n_hits, n_accept, n_reject, status, p);
   if (rc != HG_OK || N == 0) return rc;
   SegWs w;
-  seg_ws_layout(N, dim, (char*)workspace, &w);
+  seg_ws_layout(N, dim, ws_hits, (char*)workspace, &w);
   cudaStream_t s = (cudaStream_t)stream;
   // crossings of this call are refined at its end
   if (defer_refine(p)) {
-    refine_area_carve(N, w.refine, p);
+    refine_area_carve(N, p.max_hits, w.refine, p);
     if (cudaMemsetAsync(p.refine_count, 0, sizeof(int), s) != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset");
   }
   if (dim == 6) {
@@ -571,8 +615,9 @@ int hg_propagate_dop853_scheduled(hg_handle* h, double mu, int dim, int N, const
   if (N > 0 && (!y_end || !t_end || !n_accept || !n_reject || !status))
     return fail(h, HG_ERR_ARGS, "scheduled runs keep their state in y_end/t_end/n_accept/n_reject/status");
   if (ev && ev->index >= 0 && N > 0 && !n_hits) return fail(h, HG_ERR_ARGS, "n_hits is required with an event");
-  if (!workspace || workspace_bytes < seg_ws_layout(N, dim, nullptr, nullptr))
-    return fail(h, HG_ERR_ARGS, "workspace smaller than hg_dop853_segmented_workspace_bytes(N, dim)");
+  const int ws_hits = (ev && ev->index >= 0 && ev->max_hits > 0) ? ev->max_hits : 0;
+  if (!workspace || workspace_bytes < seg_ws_layout(N, dim, ws_hits, nullptr, nullptr))
+    return fail(h, HG_ERR_ARGS, "workspace smaller than hg_dop853_segmented_workspace_bytes(N, dim, max_hits)");
   hg::DopParams p;
   memset(&p, 0, sizeof(p));
   int rc = dop853_setup(h, mu, dim, N, y0, ld, t0_arr, tmax_arr, t0, tmax, opts, ev, n_samples, sample_last_only,
@@ -585,10 +630,10 @@ int hg_propagate_dop853_scheduled(hg_handle* h, double mu, int dim, int N, const
     }
   }
   SegWs w;
-  seg_ws_layout(N, dim, (char*)workspace, &w);
+  seg_ws_layout(N, dim, ws_hits, (char*)workspace, &w);
   cudaStream_t s = (cudaStream_t)stream;
   if (defer_refine(p)) {
-    refine_area_carve(N, w.refine, p);
+    refine_area_carve(N, p.max_hits, w.refine, p);
     if (cudaMemsetAsync(p.refine_count, 0, sizeof(int), s) != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset");
   }
   rc = seg_init(h, p, w, s);
@@ -637,6 +682,10 @@ int hg_set_tuning(hg_handle* h, int key, int value) {
         return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 1, 2 or 6");
       h->lanes_d6 = value;
       return HG_OK;
+    case HG_TUNE_SPREAD:
+      if (value != 0 && value != 1) return fail(h, HG_ERR_ARGS, "spread must be 0 or 1");
+      h->spread = value;
+      return HG_OK;
     case HG_TUNE_SEG_STEPS:
       if (value < 1 || value > 1000000) return fail(h, HG_ERR_ARGS, "segment steps must be in [1, 1e6]");
       h->seg_steps = value;
@@ -646,11 +695,19 @@ int hg_set_tuning(hg_handle* h, int key, int value) {
   }
 }
 
+int hg_get_counter(hg_handle* h, int key, long long* value) {
+  if (!h || !value) return HG_ERR_ARGS;
+  if (key == HG_COUNTER_KERNEL_LAUNCHES) *value = h->launches;
+  else return fail(h, HG_ERR_ARGS, "unknown counter %d", key);
+  return HG_OK;
+}
+
 int hg_get_tuning(hg_handle* h, int key, int* value) {
   if (!h || !value) return HG_ERR_ARGS;
   if (key == HG_TUNE_BLOCK_THREADS) *value = h->block;
   else if (key == HG_TUNE_DOP853_LANES_D6) *value = h->lanes_d6;
   else if (key == HG_TUNE_SEG_STEPS) *value = h->seg_steps;
+  else if (key == HG_TUNE_SPREAD) *value = h->spread;
   else return fail(h, HG_ERR_ARGS, "unknown tuning key %d", key);
   return HG_OK;
 }

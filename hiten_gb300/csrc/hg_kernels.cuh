@@ -151,6 +151,12 @@ struct Dir {
   int neg_lo, neg_hi;  // component range whose derivative is negated (fwd=-1)
 };
 
+// -v when neg: the sign-bit flip IEEE negation is, on the integer pipe (the
+// FP64 pipe is the scarce one).
+__device__ __forceinline__ double neg_if(double v, bool neg) {
+  return __longlong_as_double(__double_as_longlong(v) ^ (neg ? (long long)0x8000000000000000ull : 0ll));
+}
+
 template <int G>
 struct Layout;
 
@@ -167,7 +173,7 @@ struct Layout<1> {
     rhs6(v, mu, dv);
 #pragma unroll
     for (int r = 0; r < 6; ++r)
-      if (r >= dir.neg_lo && r < dir.neg_hi) dv[r] = -dv[r];
+      dv[r] = neg_if(dv[r], r >= dir.neg_lo && r < dir.neg_hi);
   }
   template <typename T>
   __device__ __forceinline__ T from_state(T v) const { return v; }
@@ -212,7 +218,7 @@ struct Layout<7> {
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
       const int c = comp(r);
-      if (c >= dir.neg_lo && c < dir.neg_hi) dv[r] = -dv[r];
+      dv[r] = neg_if(dv[r], c >= dir.neg_lo && c < dir.neg_hi);
     }
   }
 };
@@ -271,7 +277,7 @@ struct Layout<2> {
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const int c = comp(i);
-      if (c >= dir.neg_lo && c < dir.neg_hi) dv[i] = -dv[i];
+      dv[i] = neg_if(dv[i], c >= dir.neg_lo && c < dir.neg_hi);
     }
   }
 };
@@ -326,9 +332,8 @@ struct Layout<6> {
     const double xy = role == 3 ? x : y;
     const double acc_xy = ((c2 * u + xy) - pq) - q;
     const double acc_z = pq - q;
-    double d = role < 3 ? u : (role == 5 ? acc_z : acc_xy);
-    if (role >= dir.neg_lo && role < dir.neg_hi) d = -d;
-    dv[0] = d;
+    const double d = role < 3 ? u : (role == 5 ? acc_z : acc_xy);
+    dv[0] = neg_if(d, role >= dir.neg_lo && role < dir.neg_hi);
   }
 };
 
@@ -809,12 +814,15 @@ struct DopParams {
   double* ws_err_prev;
   double* ws_prev_pow;
   int* ws_q;
-  // Deferred refinement of terminal crossings (rec != null, max_hits == 1):
-  // the crossing step is saved (save_step) and refine_kernel computes hit_t /
-  // hit_y for every trajectory in refine_list[0 .. *refine_count).
+  // Deferred refinement of event crossings (rec != null): every crossing step
+  // is appended to a record pool (save_step: record slot, its trajectory in
+  // refine_list and hit index in refine_hit) and refine_kernel computes
+  // hit_t / hit_y for records [0 .. *refine_count), all lanes in lock step.
+  // Capacity rec_ld >= N * max_hits (no trajectory records more hits).
   double* rec;
   long long rec_ld;
   int* refine_list;
+  int* refine_hit;
   int* refine_count;
 };
 
@@ -1061,15 +1069,28 @@ __device__ __forceinline__ double refine_in_step(const EvCtx<G>& ev, const doubl
   return x_hit;
 }
 
-// Saved step of a terminal crossing (deferred refinement), structure of
-// arrays with stride rec_ld: y (D), y_new (D), k[0..12] (13 D), h, t, g_left.
+// A crossing step saved for deferred refinement, structure of arrays with
+// stride rec_ld: y (D), y_new (D), k[0..12] (13 D), h, t, g_left.
 template <int G>
-__device__ __forceinline__ void save_step(const Layout<G>& L, const DopParams& p, int traj, bool leader,
+__device__ __forceinline__ int leader_lane(const Layout<G>& L) {
+  if constexpr (G == 1)
+    return threadIdx.x & 31;
+  else if constexpr (G == 7)
+    return L.base + 6;
+  else
+    return L.base;
+}
+
+template <int G>
+__device__ __forceinline__ void save_step(const Layout<G>& L, const DopParams& p, int traj, int hit, bool leader,
                                           const double (&y)[Layout<G>::NC], const double (&yh)[Layout<G>::NC],
                                           const double (&k)[13][Layout<G>::NC], double h, double t, double g_left) {
   constexpr int D = Layout<G>::D;
   constexpr int NC = Layout<G>::NC;
-  double* r = p.rec + traj;
+  int slot = 0;
+  if (leader) slot = atomicAdd(p.refine_count, 1);
+  if constexpr (G > 1) slot = __shfl_sync(L.gmask, slot, leader_lane<G>(L));
+  double* r = p.rec + slot;
   const long long ld = p.rec_ld;
 #pragma unroll
   for (int d = 0; d < NC; ++d) {
@@ -1083,12 +1104,13 @@ __device__ __forceinline__ void save_step(const Layout<G>& L, const DopParams& p
     r[(15 * D) * ld] = h;
     r[(15 * D + 1) * ld] = t;
     r[(15 * D + 2) * ld] = g_left;
-    p.refine_list[atomicAdd(p.refine_count, 1)] = traj;
+    p.refine_list[slot] = traj;
+    p.refine_hit[slot] = hit;
   }
 }
 
-// Refinement of the saved terminal crossings, all lanes in lock step: the
-// same dense cache, bisection and interpolation as the inline path.
+// Refinement of the saved crossings, all lanes in lock step: the same dense
+// cache, bisection and interpolation as the inline path.
 template <int G>
 __global__ void __launch_bounds__(128) refine_kernel(DopParams p) {
   constexpr int D = Layout<G>::D;
@@ -1103,7 +1125,8 @@ __global__ void __launch_bounds__(128) refine_kernel(DopParams p) {
   const int n = *p.refine_count;
   for (; slot < n; slot += p.stride) {
     const int traj = p.refine_list[slot];
-    const double* r = p.rec + traj;
+    const int hit = p.refine_hit[slot];
+    const double* r = p.rec + slot;
     const long long ld = p.rec_ld;
     double y[NC], yh[NC], k[13][NC];
 #pragma unroll
@@ -1120,9 +1143,10 @@ __global__ void __launch_bounds__(128) refine_kernel(DopParams p) {
     double F[7][NC];
     DopLane<G>::dense_cache(L, y, yh, h, p.mu, p.dir, k, F);
     const double x_hit = refine_in_step<G>(ev, y, F, h, g_left, p);
-    if (leader) p.hit_t[traj] = t + x_hit * h;
+    if (leader) p.hit_t[(long long)hit * p.ld + traj] = t + x_hit * h;
+    double* o = p.hit_y + (long long)hit * D * p.ld;
 #pragma unroll
-    for (int d = 0; d < NC; ++d) p.hit_y[(long long)L.comp(d) * p.ld + traj] = DopLane<G>::eval1(y[d], F, d, x_hit);
+    for (int d = 0; d < NC; ++d) o[(long long)L.comp(d) * p.ld + traj] = DopLane<G>::eval1(y[d], F, d, x_hit);
   }
 }
 
@@ -1201,7 +1225,9 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
     int seg_count = 0;
     bool paused = false;
 
-    while ((t - tmax) * 1.0 < 0.0) {
+    // integrators/rk.py loop test (t - t_end) * direction < 0 with direction
+    // +1; the product by 1 is exact, so it is left out
+    while (t - tmax < 0.0) {
       if (p.seg && seg_count >= p.seg_steps) {
         paused = true;
         break;
@@ -1240,7 +1266,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
         bool stop = false;
         // dense samples inside (t, t_new] (reference: searchsorted on nodes)
         if (dense) {
-          const bool last = !((t_new - tmax) * 1.0 < 0.0);
+          const bool last = !(t_new - tmax < 0.0);
           if (q_next < p.m && (last || sample_t(q_next) < t_new)) {
             const double hseg = t_new - t;
             double F[7][NC];
@@ -1259,8 +1285,8 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
           const double g_new = ev.bcast(ev.mine ? (pick<NC>(yh, ev.r) - p.ev_offset) : 0.0);
           if (event_crossed(g_prev, g_new, p.ev_dir)) {
             if (p.rec) {
-              // terminal crossing: keep the step for refine_kernel
-              save_step<G>(L, p, traj, leader, y, yh, k, h, t, g_prev);
+              // keep the step for refine_kernel
+              save_step<G>(L, p, traj, hits, leader, y, yh, k, h, t, g_prev);
             } else {
               // _dop853_refine_in_step with the step size h
               double F[7][NC];

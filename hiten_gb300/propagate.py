@@ -190,6 +190,7 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
     if n_samples:
         rows = 1 if sample_last_only else int(n_samples)
         samples = torch.empty((rows, dim, ld), dtype=torch.float64, device=dev)
+    ws_hits = int(event.max_hits) if event is not None else 0
     H = _lib.handle(dev.index or 0)
     st = _stream(dev) if stream is None else C.c_void_p(stream)
     args = (H.ptr, float(mu), dim, N, _ptr(Y0), ld, _ptr(t0a), _ptr(tmaxa), t0s, tmaxs, C.byref(opts),
@@ -197,13 +198,13 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
             _ptr(y_end), _ptr(t_end), _ptr(hit_t), _ptr(hit_y), _ptr(n_hits), _ptr(n_acc), _ptr(n_rej), _ptr(status))
     with torch.cuda.device(dev):
         if scheduled:
-            ws_bytes = int(H.lib.hg_dop853_segmented_workspace_bytes(N, dim))
+            ws_bytes = int(H.lib.hg_dop853_segmented_workspace_bytes(N, dim, ws_hits))
             ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
             H.check(H.lib.hg_propagate_dop853_scheduled(*args, _ptr(ws), ws_bytes, st))
         elif not segmented:
             H.check(H.lib.hg_propagate_dop853(*args, st))
         else:
-            ws_bytes = int(H.lib.hg_dop853_segmented_workspace_bytes(N, dim))
+            ws_bytes = int(H.lib.hg_dop853_segmented_workspace_bytes(N, dim, ws_hits))
             ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
             segs = int(max_segments)
             resume = 0
@@ -240,17 +241,19 @@ class tuning:
     """Set the launch shape of the device's handle (results are unchanged):
     ``lanes_d6`` in {0 (auto), 1, 2, 6} lanes per 6-dim DOP853 trajectory,
     ``block`` in {32, 64, 128} threads per block, ``seg_steps`` attempted
-    steps per segment of the scheduled driver.  Usable as a context manager
+    steps per segment of the scheduled driver, ``spread`` one 4-warp block
+    per SM for DOP853.  Usable as a context manager
     (restores the previous values on exit) or as a plain call."""
 
     _KEYS = (("lanes_d6", _lib.HG_TUNE_DOP853_LANES_D6), ("block", _lib.HG_TUNE_BLOCK_THREADS),
-             ("seg_steps", _lib.HG_TUNE_SEG_STEPS))
+             ("seg_steps", _lib.HG_TUNE_SEG_STEPS), ("spread", _lib.HG_TUNE_SPREAD))
 
-    def __init__(self, lanes_d6=None, block=None, device=None, seg_steps=None):
+    def __init__(self, lanes_d6=None, block=None, device=None, seg_steps=None, spread=None):
         dev = _device(device)
         self.H = _lib.handle(dev.index or 0)
         self.old = {k: self.H.get_tuning(key) for k, key in self._KEYS}
-        new = {"lanes_d6": lanes_d6, "block": block, "seg_steps": seg_steps}
+        new = {"lanes_d6": lanes_d6, "block": block, "seg_steps": seg_steps,
+               "spread": None if spread is None else int(bool(spread))}
         for k, key in self._KEYS:
             if new[k] is not None:
                 self.H.set_tuning(key, new[k])

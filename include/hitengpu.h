@@ -138,12 +138,14 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N,
  * captured in a CUDA graph.  State persists in the outputs (y_end, t_end,
  * n_accept, n_reject, n_hits, status -- all required; status = -1 marks a
  * trajectory still running) and in `workspace` (caller device memory of at
- * least hg_dop853_segmented_workspace_bytes(N, dim) bytes; -1 for an invalid
- * N or dim); resume = 1 continues
+ * least hg_dop853_segmented_workspace_bytes(N, dim, max_hits) bytes, with
+ * max_hits the event's (0 without one); -1 for invalid arguments); it also
+ * holds the steps of the event crossings, refined at the end of each call;
+ * resume = 1 continues
  * a previous call's unfinished trajectories.  Results are bit-identical to
  * hg_propagate_dop853.
  * Replaces: as hg_propagate_dop853 (execution schedule only). */
-long long hg_dop853_segmented_workspace_bytes(int N, int dim);
+long long hg_dop853_segmented_workspace_bytes(int N, int dim, int max_hits);
 int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N,
                                   const double* y0, long long ld,
                                   const double* t0_arr, const double* tmax_arr,
@@ -244,13 +246,24 @@ int hg_trajectory_filters(int N, int m, const double* samples, long long ld, dou
  * (the default).
  * HG_TUNE_SEG_STEPS: attempted steps per segment of
  * hg_propagate_dop853_scheduled (default 16).
+ * HG_TUNE_SPREAD: 1 = DOP853 launches use blocks of four warps that each
+ * occupy a whole SM (one warp per SM sub-partition); 0 = HG_TUNE_BLOCK_THREADS
+ * blocks (default).
  * Results are bit-identical for every setting.
  * Replaces: nothing (no reference counterpart; launch shape only). */
 #define HG_TUNE_BLOCK_THREADS 1
 #define HG_TUNE_DOP853_LANES_D6 2
 #define HG_TUNE_SEG_STEPS 3
+#define HG_TUNE_SPREAD 4
 int hg_set_tuning(hg_handle* h, int key, int value);
 int hg_get_tuning(hg_handle* h, int key, int* value);
+
+/* Counters of a handle.  HG_COUNTER_KERNEL_LAUNCHES: kernels launched
+ * through the handle since hg_create (every propagation kernel, segment,
+ * refinement and set-up kernel; memsets and copies are not kernels).
+ * Replaces: nothing (instrumentation only). */
+#define HG_COUNTER_KERNEL_LAUNCHES 1
+int hg_get_counter(hg_handle* h, int key, long long* value);
 
 /* Measured FP64 fused-multiply-add throughput of this device (TFLOP/s,
  * counting an FMA as 2 flops): runs a short dependent-chain-free DFMA loop

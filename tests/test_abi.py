@@ -48,13 +48,17 @@ def test_segmented_workspace_query():
     """Pure host arithmetic: 256-byte aligned sub-buffers, grows with N."""
     from hiten_gb300 import _lib
     L = _lib.load()
-    assert L.hg_dop853_segmented_workspace_bytes(-1, 6) == -1
-    assert L.hg_dop853_segmented_workspace_bytes(10, 7) == -1
+    assert L.hg_dop853_segmented_workspace_bytes(-1, 6, 0) == -1
+    assert L.hg_dop853_segmented_workspace_bytes(10, 7, 0) == -1
+    assert L.hg_dop853_segmented_workspace_bytes(10, 6, -1) == -1
     for dim in (6, 42):
-        prev = L.hg_dop853_segmented_workspace_bytes(0, dim)
-        assert prev > 0 and prev % 256 == 0
-        for n in (1, 63, 64, 65, 16384, 1 << 20):
-            b = L.hg_dop853_segmented_workspace_bytes(n, dim)
-            # lists, step-size state and the saved crossing step (15 dim + 3 doubles)
-            assert b % 256 == 0 and b >= prev and b >= n * (3 * 4 + 3 * 8 + 4 + (15 * dim + 3) * 8)
-            prev = b
+        for hits in (0, 1, 8):
+            prev = L.hg_dop853_segmented_workspace_bytes(0, dim, hits)
+            assert prev > 0 and prev % 256 == 0
+            for n in (1, 63, 64, 65, 16384, 1 << 20):
+                b = L.hg_dop853_segmented_workspace_bytes(n, dim, hits)
+                # lists and step-size state, plus one saved step (15 dim + 3
+                # doubles, trajectory and hit index) per possible crossing
+                assert b % 256 == 0 and b >= prev
+                assert b >= n * (3 * 4 + 3 * 8) + n * hits * ((15 * dim + 3) * 8 + 8)
+                prev = b

@@ -15,11 +15,14 @@ pytestmark = pytest.mark.gpu
 MU = W.MU_EM
 
 
-@pytest.fixture(params=[(1, 32), (2, 32), (1, 128), (2, 64), (6, 32), (6, 128)],
-                ids=["lanes1-b32", "lanes2-b32", "lanes1-b128", "lanes2-b64", "lanes6-b32", "lanes6-b128"])
+@pytest.fixture(params=[(1, 32, 0), (2, 32, 0), (1, 128, 0), (2, 64, 0), (6, 32, 0), (6, 128, 0), (1, 32, 1),
+                        (6, 32, 1)],
+                ids=["lanes1-b32", "lanes2-b32", "lanes1-b128", "lanes2-b64", "lanes6-b32", "lanes6-b128",
+                     "lanes1-spread", "lanes6-spread"])
 def shape(request, gpu):
     """Every launch shape must give the same bits."""
-    with gpu.tuning(lanes_d6=request.param[0], block=request.param[1]):
+    lanes, block, spread = request.param
+    with gpu.tuning(lanes_d6=lanes, block=block, spread=spread):
         yield request.param
 
 
