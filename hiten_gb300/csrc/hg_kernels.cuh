@@ -192,13 +192,91 @@ struct Layout<7> {
   __device__ __forceinline__ int comp(int r) const { return role < 6 ? 6 * r + role : 36 + r; }
   template <typename T>
   __device__ __forceinline__ T from_state(T v) const { return __shfl_sync(gmask, v, base + 6); }
+  __device__ __forceinline__ double from(double v, int r) const { return __shfl_sync(gmask, v, base + r); }
+
+  // hessian42 with its work spread over the group.  Lane b*3 + k (b = primary,
+  // k < 3) takes one power pair r^3, r^5 of its primary (hg_pow15_25), one
+  // reciprocal and two of the twelve quotients:
+  //   0: mu2/r3, t1/r3     1: y/r3, z/r3     2: mu2/r5, (mu2 t1)/r5
+  //   3: mu/R3,  t2/R3     4: y/R3, z/R3     5: mu/R5,  (mu t2)/R5
+  // (lane 6 repeats lane 0's work).  The quotients are exchanged, lanes 0..5
+  // form xx, yy, zz, ax, ay, az with one common expression
+  // ((p + a u) + b w) + c whose operands reproduce hessian42's exactly
+  // (x - m == x + (-m), (-a) u == -(a u), -0 + v == v), and those six are
+  // exchanged again.  Same operations on the same operands: same bits.
+  __device__ __forceinline__ Hess hessian_split(double x, double y, double z, double vx, double vy,
+                                                double mu) const {
+    const double mu2 = 1.0 - mu;
+    const double t1 = x + mu;
+    const double t2 = x - mu2;
+    const double ys = y * y;
+    const double zs = z * z;
+    const double t1s = t1 * t1;
+    const double t2s = t2 * t2;
+    const bool b2 = role >= 3 && role < 6;
+    const int k = b2 ? role - 3 : (role == 6 ? 0 : role);
+    const double rr = ((b2 ? t2s : t1s) + ys) + zs;
+    double p3, p5;
+    hg_pow15_25(rr, p3, p5);
+    const double den = k == 2 ? p5 : p3;
+    const double inv = hg_rcp_rn(den);
+    const double m = b2 ? mu : mu2;
+    const double tt = b2 ? t2 : t1;
+    const double mt = m * tt;
+    const double n0 = k == 1 ? y : m;
+    const double n1 = k == 0 ? tt : (k == 1 ? z : mt);
+    const double q0 = hg_div_rn(n0, den, inv);
+    const double q1 = hg_div_rn(n1, den, inv);
+    // exchange: qa, qb, the r^3 terms of c3, the r^5 terms of sxy
+    const double qa = from(q0, 2), qb = from(q0, 5);
+    const double c3a = from(q0, 0), c3b = from(q0, 3);
+    const double sxa = from(q1, 2), sxb = from(q1, 5);
+    // acceleration lanes 3/4/5 read the x/y/z quotients of both primaries
+    const int ua = role == 3 ? 0 : 1, wa = role == 3 ? 3 : 4;
+    const double u0 = from(q0, ua), u1 = from(q1, ua), w0 = from(q0, wa), w1 = from(q1, wa);
+    const double a3 = qa * 3.0;
+    const double b3 = qb * 3.0;
+    const double c3 = c3a + c3b;
+    // role 0 xx, 1 yy, 2 zz, 3 ax, 4 ay, 5 az (6: xx again)
+    const bool acc = b2;
+    const int e = role == 6 ? 0 : role;
+    double P, A, U, B, W, Cc;
+    if (!acc) {
+      P = e == 2 ? -0.0 : 1.0;
+      A = a3;
+      U = e == 0 ? t1s : (e == 1 ? ys : zs);
+      B = b3;
+      W = e == 0 ? t2s : (e == 1 ? ys : zs);
+      Cc = -c3;
+    } else {
+      P = e == 3 ? x : (e == 4 ? y : -0.0);
+      A = -mu2;
+      U = e == 3 ? u1 : (e == 4 ? u0 : u1);  // t1/r3 | y/r3 | z/r3
+      B = -mu;
+      W = e == 3 ? w1 : (e == 4 ? w0 : w1);  // t2/R3 | y/R3 | z/R3
+      Cc = e == 3 ? 2.0 * vy : (e == 4 ? -2.0 * vx : -0.0);
+    }
+    const double form = ((P + A * U) + B * W) + Cc;
+    Hess H;
+    H.xx = from(form, 0);
+    H.yy = from(form, 1);
+    H.zz = from(form, 2);
+    H.ax = from(form, 3);
+    H.ay = from(form, 4);
+    H.az = from(form, 5);
+    const double sxy = sxa + sxb;
+    H.xy = (3.0 * y) * sxy;
+    H.xz = (3.0 * z) * sxy;
+    H.yz = ((3.0 * y) * z) * (qa + qb);
+    return H;
+  }
   __device__ __forceinline__ void rhs(const double (&v)[6], double mu, const Dir& dir, double (&dv)[6]) const {
     const double x = from_state(v[0]);
     const double y = from_state(v[1]);
     const double z = from_state(v[2]);
     const double vx = from_state(v[3]);
     const double vy = from_state(v[4]);
-    const Hess H = hessian42(x, y, z, vx, vy, mu);
+    const Hess H = hessian_split(x, y, z, vx, vy, mu);
     if (role < 6) {
       // rows of F(x) @ Phi[:, j] (dynamics/rtbp.py:204-209), zero terms skipped
       dv[0] = v[3];
