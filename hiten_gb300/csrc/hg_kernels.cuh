@@ -2,15 +2,20 @@
 //
 // Execution model.  GB300 issues FP64 at a small fraction of its FP32 rate,
 // so the kernels are bound by the FP64 pipe, not by HBM: state and Runge-
-// Kutta stages live in registers, HBM sees only initial states and sampled
-// outputs.  Two lane layouts:
+// Kutta stages live in registers, HBM sees only initial states, sampled
+// outputs and saved event steps.  Lane layouts (Layout<G>):
 //   * G = 1  (6-dim state): one lane owns one trajectory.
+//   * G = 2  (6-dim): a lane pair (position / velocity halves).
+//   * G = 6  (6-dim): six lanes, one component each.
 //   * G = 7  (42-dim state + STM): a group of 7 lanes owns one trajectory;
 //            lane j < 6 holds STM column j (components 6r+j, r = 0..5), lane 6
 //            holds the state (components 36..41).  Column j of dPhi = F(x)Phi
 //            needs only the state, which the state lane broadcasts by shuffle
-//            at every stage; every lane of the group computes the Hessian of
-//            the effective potential from it.  Four groups fill lanes 0..27.
+//            at every stage; the group shares the Hessian's work.  Four
+//            groups fill lanes 0..27.
+// Wider groups cut the per-step latency of one trajectory (what bounds a
+// batch whose longest trajectories run alone at the end); narrower ones
+// spend the least FP64 work per step.
 // Group-wide decisions (accept/reject, events) use values that every lane of
 // the group computes identically, so control flow stays group-uniform.
 //
