@@ -173,6 +173,141 @@ def run_reference_arm(args):
     print(json.dumps(out))
 
 
+def whole_job_rate(local_units, local_seconds, device=None):
+    """(units of all ranks / the slowest rank's seconds, that time).  Ranks are
+    replicas with no data-path exchange; only these two numbers cross ranks."""
+    import torch
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        u = torch.tensor([float(local_units)], dtype=torch.float64, device=device)
+        s = torch.tensor([float(local_seconds)], dtype=torch.float64, device=device)
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        dist.all_reduce(s, op=dist.ReduceOp.MAX)
+        return float(u.item()) / float(s.item()), float(s.item())
+    return float(local_units) / float(local_seconds), float(local_seconds)
+
+
+def _event_ms(fn, reps):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    ts, r = [], None
+    for _ in range(reps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        r = fn()
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    return statistics.median(ts), r
+
+
+def _line(name, metric, value, unit, ms, cfg, **extra):
+    out = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "ms_per_step": ms, "higher_is_better": True,
+           "dtype": "f64", "data": "synthetic", "config": dict(workload=name, **cfg)}
+    out.update(extra)
+    print(json.dumps(out))
+
+
+def bench_fixed_stm(args):
+    """Fixed-step RK8 with the 42-dim variational system: 1024 states (STM = I), t in [0, 3], 3000 steps,
+    every 100th state written."""
+    import torch
+    from hiten_gb300 import propagate as P
+    from hiten_gb300 import workloads as W
+    dev = torch.device("cuda", 0)
+    y = torch.as_tensor(W.stm_fixed_batch(1024, seed=0), device=dev)
+    t = np.linspace(0.0, 3.0, 3001)
+    ms, _ = _event_ms(lambda: P.propagate_fixed(y, t, W.MU_EM, order=8, out_every=100, device=dev), args.steps)
+    steps = 1024 * 3000
+    _line("RK8 + STM, 1024 states x 3000 steps (42-dim)", METRIC, steps / (ms * 1e-3), UNIT, ms,
+          {"states": 1024, "steps": 3000, "dim": 42},
+          roofline={"achieved_tflops": 7870 * steps / (ms * 1e-3) / 1e12, "flops_per_step": 7870})
+
+
+def bench_section(args):
+    """Synodic section: 65536 Jacobi-matched states near L1/L2, DOP853 1e-11 to t = 20, up to 8 y = 0
+    crossings (direction -1) each; single pass and host-scheduled plans (same bits)."""
+    import torch
+    from hiten_gb300 import propagate as P
+    from hiten_gb300 import workloads as W
+    dev = torch.device("cuda", 0)
+    y = torch.as_tensor(W.section_states(65536, seed=0), device=dev)
+    ev = P.EventSpec(index=1, offset=0.0, direction=-1, max_hits=8)
+    res = {}
+    for plan, kw in (("single", {}), ("scheduled", {"scheduled": True})):
+        ms, r = _event_ms(lambda: P.propagate_dop853(y, 0.0, 20.0, W.MU_EM, rtol=1e-11, atol=1e-11, event=ev,
+                                                     device=dev, **kw), max(2, args.steps // 4))
+        res[plan] = (ms, int(r.n_accept.sum()), int(r.n_accept.sum() + r.n_reject.sum()), float(r.n_hits.float().mean()))
+    best = min(res, key=lambda k: res[k][0])
+    ms, acc, att, hits = res[best]
+    _line("synodic section, 65536 states, DOP853 1e-11 to t=20, <= 8 crossings", METRIC, acc / (ms * 1e-3), UNIT, ms,
+          {"states": 65536, "max_hits": 8, "plan": best},
+          plans_ms={k: v[0] for k, v in res.items()}, mean_hits=hits,
+          roofline={"achieved_tflops": FLOPS_PER_ATTEMPT_D6 * att / (ms * 1e-3) / 1e12})
+
+
+def bench_correct(args):
+    """Batched halo correction: 2048 third-order guesses (half L1, half L2, Az ~ U[0.01, 0.4]), single
+    shooting on the half-period y = 0 crossing to ||r|| < 1e-12."""
+    import torch
+    from hiten_gb300 import corrector, halo
+    from hiten_gb300 import workloads as W
+    mu = W.MU_EM
+    pt, az, zen = W.halo_guess_params(2048, seed=0)
+    g = np.concatenate([halo.third_order_guess(mu, 1, az[pt == 1], zen[pt == 1]),
+                        halo.third_order_guess(mu, 2, az[pt == 2], zen[pt == 2])])
+    corrector.correct_halo(g[:64], mu)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(max(1, args.steps // 4)):
+        t0 = time.perf_counter()
+        res = corrector.correct_halo(g, mu)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    s = statistics.median(ts)
+    _line("halo correction, 2048 guesses (L1/L2, Az 0.01-0.4)", "orbits corrected/s", len(g) / s, "orbits/s",
+          s * 1e3, {"orbits": len(g)}, converged=int((res.status == 0).sum()),
+          iterations_hist=np.bincount(res.iterations).tolist(), gpu_launches=res.launches)
+
+
+def bench_serving(args):
+    """Serving mix: seeded Poisson stream (200 req/s for 1 s) of manifold (64-4096 seeds), correction
+    (1-256 guesses) and synodic (1k-32k states) requests; continuous batching vs the same stream run
+    sequentially in the plain form (one single-pass call per request)."""
+    import torch
+    from hiten_gb300 import serving
+    from hiten_gb300 import workloads as W
+    mu = W.MU_EM
+    dev = torch.device("cuda", 0)
+    seeds = make_seeds(dev)
+    serving.run_sequential(serving.poisson_requests(200.0, 0.05, mu, seed=2, manifold_seeds=seeds,
+                                                    size_scale=0.05), mu)
+    def stream(burst=False):
+        reqs = serving.poisson_requests(200.0, 1.0, mu, seed=1, manifold_seeds=seeds)
+        if burst:  # every request present at t = 0: throughput without waiting for arrivals
+            for r in reqs:
+                r.arrival = 0.0
+        return reqs
+
+    eng = serving.ServingEngine(mu, max_concurrent=6)
+    served = eng.serve(stream()).summary()
+    served_burst = eng.serve(stream(burst=True)).summary()
+    eng.close()
+    seq = serving.run_sequential(stream(), mu).summary()
+    seq_burst = serving.run_sequential(stream(burst=True), mu).summary()
+    _line("serving mix, Poisson 200 req/s x 1 s (manifold / correct / synodic)", METRIC,
+          served_burst["traj_steps_per_s"], UNIT, served_burst["wall_s"] * 1e3, {"rate_hz": 200, "window_s": 1.0},
+          served_poisson=served, sequential_plain_poisson=seq, served_burst=served_burst,
+          sequential_plain_burst=seq_burst,
+          speedup_vs_plain=served_burst["traj_steps_per_s"] / seq_burst["traj_steps_per_s"])
+
+
+EXTRA = {"fixed_stm": bench_fixed_stm, "section": bench_section, "correct": bench_correct,
+         "serving": bench_serving}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -182,9 +317,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plan", default=None,
                     help="force an execution plan by name (autotune.plan_name), e.g. scheduled_seg16")
+    ap.add_argument("--workload", default="manifold", choices=["manifold"] + sorted(EXTRA),
+                    help="manifold (the headline); the others print one secondary line each")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.workload != "manifold":
+        return EXTRA[args.workload](args)
 
     import torch
     import torch.distributed as dist
@@ -272,12 +411,9 @@ def main():
     for r in results:
         acc += int(r.n_accept.sum().item())
         att += int(r.n_accept.sum().item() + r.n_reject.sum().item())
-    total_ms = sum(times_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = acc * world / (total_ms * 1e-3)
+    value, total_s = whole_job_rate(acc, sum(times_ms) * 1e-3, device=dev)
+    total_ms = total_s * 1e3
+    att_rate, _ = whole_job_rate(att, sum(times_ms) * 1e-3, device=dev)
     kernel_ms = total_ms / args.steps
     flops = FLOPS_PER_ATTEMPT_D6 * att / args.steps
     peak = P.fp64_peak_tflops(dev)
@@ -300,12 +436,7 @@ def main():
         e2e_acc += int(n_acc.sum())
         d2h = (y_end.numel() + hit_y.numel() + hit_t.numel()) * 8 + n_acc.numel() * 4
     torch.cuda.synchronize(dev)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = e2e_acc * world / e2e_s
+    e2e_value, e2e_s = whole_job_rate(e2e_acc, time.perf_counter() - t0, device=dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -326,7 +457,7 @@ def main():
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(world),
-               "attempted_steps_per_s": att * world / (total_ms * 1e-3),
+               "attempted_steps_per_s": att_rate,
                "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                             "frac": achieved / peak if peak else None, "traffic": traffic,
                             "traffic_scope": "DRAM bytes of one launch of the dominant kernel (first scheduled "

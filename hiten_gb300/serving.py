@@ -53,18 +53,27 @@ class Request:
         return BYTES_PER_TRAJ[self.kind] * len(self.payload)
 
 
-def _solve(kind, x, mu, device):
-    """Run one batch of one kind; returns host arrays per trajectory."""
+# Merged batches at least this wide run as host-scheduled segments (the
+# layout widens as their trajectories finish); narrower ones fit the GPU in
+# one launch of the widest layout.
+SCHEDULE_MIN = 4096
+
+
+def _solve(kind, x, mu, device, batched=True):
+    """Run one batch of one kind; returns host arrays per trajectory.
+    `batched` = False is the plain form: one single-pass call, no scheduling."""
+    sched = batched and len(x) >= SCHEDULE_MIN
     if kind == "manifold":
         ev = P.EventSpec(index=0, offset=1.0 - mu, direction=0, max_hits=1)
         r = P.propagate_dop853(x, 0.0, 8.0, mu, rtol=1e-12, atol=1e-12, max_step=1e4, fwd=-1, flip=(0, 6),
-                               event=ev, device=device)
+                               event=ev, device=device, scheduled=sched)
         return {"y_end": r.y_end.cpu().numpy(), "t_end": r.t_end.cpu().numpy(), "n_hits": r.n_hits.cpu().numpy(),
                 "hit_t": r.hit_t.cpu().numpy(), "hit_y": r.hit_y.cpu().numpy(), "n_accept": r.n_accept.cpu().numpy(),
                 "status": r.status.cpu().numpy()}
     if kind == "synodic":
         ev = P.EventSpec(index=1, offset=0.0, direction=-1, max_hits=8)
-        r = P.propagate_dop853(x, 0.0, 20.0, mu, rtol=1e-11, atol=1e-11, max_step=1e4, event=ev, device=device)
+        r = P.propagate_dop853(x, 0.0, 20.0, mu, rtol=1e-11, atol=1e-11, max_step=1e4, event=ev, device=device,
+                               scheduled=sched)
         return {"y_end": r.y_end.cpu().numpy(), "n_hits": r.n_hits.cpu().numpy(), "hit_t": r.hit_t.cpu().numpy(),
                 "hit_y": r.hit_y.cpu().numpy(), "n_accept": r.n_accept.cpu().numpy(), "status": r.status.cpu().numpy()}
     if kind == "correct":
@@ -184,7 +193,7 @@ def run_sequential(requests, mu, device=None, t0=None):
         if wait > 0:
             time.sleep(wait)
         r.admitted = time.perf_counter()
-        r.result = _solve(r.kind, r.payload, mu, dev)
+        r.result = _solve(r.kind, r.payload, mu, dev, batched=False)
         torch.cuda.synchronize(dev)
         r.done = time.perf_counter()
         stats.n += 1
