@@ -24,6 +24,7 @@ STM integration and one batched event integration per Armijo level, over the
 orbits still active.  The small 2x2 linear algebra runs in numpy exactly as
 the reference does (stacked LAPACK calls give the same bits as single calls).
 """
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -87,21 +88,35 @@ class GpuShootingBackend:
         return r.samples[0, :, :36].cpu().numpy().reshape(-1, 6, 6)
 
 
+def _libm_pow(a, e):
+    """Elementwise C `pow`: what the reference's numpy-scalar `**` computes
+    (numpy's array `**` takes other paths: `x*x` for 2, SIMD kernels for
+    fractional exponents, which differ in the last bit)."""
+    flat = np.ascontiguousarray(a, dtype=np.float64).ravel()
+    return np.fromiter((math.pow(v, e) for v in flat.tolist()), dtype=np.float64, count=flat.size).reshape(a.shape)
+
+
 def halo_quadratic_term(x_ev, Phi, mu):
-    """types/services/orbits.py:917-948, per orbit, with the same numpy
-    scalar arithmetic as the reference."""
+    """types/services/orbits.py:917-948 for a batch of orbits: the same
+    expression tree as the reference's per-orbit numpy scalar code, with its
+    powers through C `pow` and every +, -, *, / elementwise (identical to the
+    scalar operations)."""
+    x, y, z, vx, vy = (np.ascontiguousarray(x_ev[:, i]) for i in range(5))
+    mu2 = 1 - mu
+    y2 = _libm_pow(y, 2)
+    z2 = _libm_pow(z, 2)
+    rho_1 = 1 / _libm_pow((_libm_pow(x + mu, 2) + y2) + z2, 1.5)
+    rho_2 = 1 / _libm_pow((_libm_pow(x - mu2, 2) + y2) + z2, 1.5)
+    omega_x = (-((mu2 * (x + mu)) * rho_1) - ((mu * (x - mu2)) * rho_2)) + x
+    DDx = 2 * vy + omega_x
+    DDz = -((mu2 * z) * rho_1) - ((mu * z) * rho_2)
+    small = np.abs(vy) < 1e-9
+    vy = np.where(small, np.where(vy != 0, np.sign(vy) * 1e-9, 1e-9), vy)
+    # [[DDx], [DDz]] @ Phi[[1], (0, 4)] / vy: a rank-one product, one multiply per entry
+    p = Phi[:, 1, [0, 4]]
     out = np.empty((x_ev.shape[0], 2, 2))
-    for i in range(x_ev.shape[0]):
-        x, y, z, vx, vy, vz = x_ev[i]
-        mu2 = 1 - mu
-        rho_1 = 1 / (((x + mu) ** 2 + y ** 2 + z ** 2) ** 1.5)
-        rho_2 = 1 / (((x - mu2) ** 2 + y ** 2 + z ** 2) ** 1.5)
-        omega_x = -(mu2 * (x + mu) * rho_1) - (mu * (x - mu2) * rho_2) + x
-        DDx = 2 * vy + omega_x
-        DDz = -(mu2 * z * rho_1) - (mu * z * rho_2)
-        if abs(vy) < 1e-9:
-            vy = np.sign(vy) * 1e-9 if vy != 0 else 1e-9
-        out[i] = np.array([[DDx], [DDz]]) @ Phi[i][[1], :][:, (0, 4)] / vy
+    out[:, 0, :] = DDx[:, None] * p / vy[:, None]
+    out[:, 1, :] = DDz[:, None] * p / vy[:, None]
     return out
 
 
@@ -198,22 +213,26 @@ def correct_halo(guesses, mu, options=None, backend=None, device=None):
             rt, nt, tt, xt, ft = residual(trial, active[idx])
             # an evaluation without a crossing is a failed residual: try a smaller step
             ok = ft & (nt <= (1.0 - o.armijo_c * alpha[idx]) * rn[idx])
-            for j, i in enumerate(idx):
-                if ok[j]:
-                    new[0][i], new[1][i], new[2][i], new[3][i], new[4][i] = trial[j], nt[j], rt[j], tt[j], xt[j]
-                    pending[i] = False
-                    continue
-                if ft[j] and nt[j] < best[1][i]:
-                    best[0][i], best[1][i], best[2][i] = trial[j], nt[j], alpha[i]
-                    best[3][i], best[4][i], best[5][i] = rt[j], tt[j], xt[j]
-                alpha[i] *= o.alpha_reduction
-                if alpha[i] < o.min_alpha:
-                    pending[i] = False
-                    if best[2][i] > 0:
-                        new[0][i], new[1][i], new[2][i], new[3][i], new[4][i] = (best[0][i], best[1][i], best[3][i],
-                                                                                 best[4][i], best[5][i])
-                    else:
-                        failed[i] = True
+            # accepted trials
+            a_i = idx[ok]
+            for dst, src in zip(new, (trial, nt, rt, tt, xt)):
+                dst[a_i] = src[ok]
+            pending[a_i] = False
+            # rejected ones: remember the best finite trial, halve alpha
+            rej = ~ok
+            r_i = idx[rej]
+            better = ft[rej] & (nt[rej] < best[1][r_i])
+            b_i = r_i[better]
+            best[2][b_i] = alpha[b_i]
+            for dst, src in zip((best[0], best[1], best[3], best[4], best[5]), (trial, nt, rt, tt, xt)):
+                dst[b_i] = src[rej][better]
+            alpha[r_i] *= o.alpha_reduction
+            s_i = r_i[alpha[r_i] < o.min_alpha]
+            pending[s_i] = False
+            g_i = s_i[best[2][s_i] > 0]
+            for dst, src in zip(new, (best[0], best[1], best[3], best[4], best[5])):
+                dst[g_i] = src[g_i]
+            failed[s_i[best[2][s_i] <= 0]] = True
         status[active[failed]] = STATUS_LINE_SEARCH
         iters[active[failed]] = k
         keep = ~failed
