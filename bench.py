@@ -236,7 +236,7 @@ def bench_section(args):
     y = torch.as_tensor(W.section_states(65536, seed=0), device=dev)
     ev = P.EventSpec(index=1, offset=0.0, direction=-1, max_hits=8)
     res = {}
-    for plan, kw in (("single", {}), ("scheduled", {"scheduled": True})):
+    for plan, kw in (("single", {"scheduled": False}), ("scheduled", {"scheduled": True})):
         ms, r = _event_ms(lambda: P.propagate_dop853(y, 0.0, 20.0, W.MU_EM, rtol=1e-11, atol=1e-11, event=ev,
                                                      device=dev, **kw), max(2, args.steps // 4))
         res[plan] = (ms, int(r.n_accept.sum()), int(r.n_accept.sum() + r.n_reject.sum()), float(r.n_hits.float().mean()))

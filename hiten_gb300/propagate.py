@@ -15,6 +15,9 @@ import torch
 from . import _lib
 
 EPS = float(np.finfo(float).eps)
+# 6-dim DOP853 batches at least this wide run as host-scheduled segments by
+# default: their long tail then runs in the widest lane layout
+SCHEDULE_MIN = 4096
 
 
 def _device(device):
@@ -138,7 +141,7 @@ class Dop853Result:
 def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min_step=None,
                      max_steps=100_000, fwd=1, flip=None, event=None, n_samples=0, sample_last_only=False,
                      device=None, stream=None, segmented=False, seg_steps=16, max_segments=8,
-                     scheduled=False):
+                     scheduled=None):
     """Adaptive DOP853 for N states from t0 to tmax (scalars or (N,) arrays).
 
     Mirrors integrators/rk.py:2375-2549 / :2678-2803 step for step.
@@ -149,7 +152,9 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
     every trajectory finished), compacting the live trajectories between
     launches; results are bit-identical.  ``scheduled``: host-scheduled
     segments (``hg_propagate_dop853_scheduled``): the layout of each segment
-    follows the number of trajectories still running; synchronous.
+    follows the number of trajectories still running; synchronous.  The
+    default (None) schedules 6-dim batches of at least SCHEDULE_MIN states
+    and runs everything else as one asynchronous launch.
     """
     dev = _device(device)
     y0 = torch.as_tensor(y0, dtype=torch.float64)
@@ -157,6 +162,8 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
     Y0 = _to_soa(y0, dim, dev)
     N = Y0.shape[1]
     ld = max(N, 1)
+    if scheduled is None:
+        scheduled = (not segmented) and dim == 6 and N >= SCHEDULE_MIN
     if min_step is None:
         min_step = 10.0 * EPS
     t0a = tmaxa = None

@@ -53,16 +53,10 @@ class Request:
         return BYTES_PER_TRAJ[self.kind] * len(self.payload)
 
 
-# Merged batches at least this wide run as host-scheduled segments (the
-# layout widens as their trajectories finish); narrower ones fit the GPU in
-# one launch of the widest layout.
-SCHEDULE_MIN = 4096
-
-
 def _solve(kind, x, mu, device, batched=True):
     """Run one batch of one kind; returns host arrays per trajectory.
     `batched` = False is the plain form: one single-pass call, no scheduling."""
-    sched = batched and len(x) >= SCHEDULE_MIN
+    sched = batched and len(x) >= P.SCHEDULE_MIN
     if kind == "manifold":
         ev = P.EventSpec(index=0, offset=1.0 - mu, direction=0, max_hits=1)
         r = P.propagate_dop853(x, 0.0, 8.0, mu, rtol=1e-12, atol=1e-12, max_step=1e4, fwd=-1, flip=(0, 6),

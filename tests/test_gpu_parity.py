@@ -173,11 +173,13 @@ def test_max_steps_status(gpu):
     assert np.all(_np(res.n_accept) + _np(res.n_reject) == 3)
 
 
-def test_lane_refill_matches_oracle(gpu, shape, dev_oracle):
-    """More trajectories than resident lanes: finished lanes take new ones."""
+@pytest.mark.parametrize("scheduled", [False, None], ids=["single-pass-refill", "default-plan"])
+def test_lane_refill_matches_oracle(gpu, shape, dev_oracle, scheduled):
+    """More trajectories than resident lanes: finished lanes take new ones
+    (single pass), or the default plan for a batch this wide (scheduled)."""
     y0 = W.section_states(60000, seed=4)
     ev = gpu.EventSpec(index=1, offset=0.0, direction=-1, max_hits=2)
-    res = gpu.propagate_dop853(y0, 0.0, 0.6, MU, rtol=1e-11, atol=1e-11, event=ev)
+    res = gpu.propagate_dop853(y0, 0.0, 0.6, MU, rtol=1e-11, atol=1e-11, event=ev, scheduled=scheduled)
     idx = np.random.default_rng(0).choice(60000, 300, replace=False)
     ref = dev_oracle.dop853_event_batch(y0[idx], 0.0, 0.6, MU, 1, 0.0, -1, 2, rtol=1e-11, atol=1e-11,
                                         max_step=1e4)
