@@ -17,6 +17,7 @@ struct hg_handle {
   int* counters = nullptr;  // scratch: lane-refill counters
   int block = 32;           // threads per block (32, 64 or 128)
   int lanes_d6 = 0;         // lanes per 6-dim DOP853 trajectory: 0 auto, 1, 2, 6
+  int lanes_d42 = 0;        // lanes per 42-dim trajectory (fixed RK and DOP853): 0 auto, 7, 14
   int seg_steps = 16;       // attempted steps per segment of the scheduled DOP853 driver
   int spread = 0;           // 1: DOP853 blocks of 4 warps, one block per SM (one warp per sub-partition)
   int smem_per_sm = 0;      // bytes of shared memory per SM
@@ -66,12 +67,30 @@ int launch_fixed(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
   const int tpb = (h->block / 32) * hg::Layout<G>::TPW;  // trajectories per block
   const int grid = (p.N + tpb - 1) / tpb;
   if (grid > 0) {
-    if (p.ev_index >= 0)
-      hg::fixed_rk_event_kernel<ORDER, G><<<grid, h->block, 0, s>>>(p);
-    else
+    if constexpr (G == 14) {
       hg::fixed_rk_kernel<ORDER, G><<<grid, h->block, 0, s>>>(p);
+    } else {
+      if (p.ev_index >= 0)
+        hg::fixed_rk_event_kernel<ORDER, G><<<grid, h->block, 0, s>>>(p);
+      else
+        hg::fixed_rk_kernel<ORDER, G><<<grid, h->block, 0, s>>>(p);
+    }
   }
   return check_launch(h, "fixed_rk_kernel");
+}
+
+// Lanes per 42-dim trajectory: 7 (an STM column per lane) or 14 (half a
+// column per lane: half the stage work per lane, twice the warps).  Unless
+// fixed by tuning, the one with the least time per step, where a warp's step
+// takes lat(G) (G = 14: 0.65 of G = 7) while its SM holds at most three
+// warps' FP64 demand, beyond which warps share the SM's FP64 unit.
+int lanes_d42(const hg_handle* h, int n) {
+  if (h->lanes_d42 != 0) return h->lanes_d42;
+  const double cap = 3.0 * h->sm_count;
+  const double w7 = (double)((n + 3) / 4), w14 = (double)((n + 1) / 2);
+  const double c7 = 1.0 * (w7 > cap ? w7 / cap : 1.0);
+  const double c14 = 0.65 * (w14 > cap ? w14 / cap : 1.0);
+  return c14 < c7 ? 14 : 7;
 }
 
 int fixed_common(hg_handle* h, double mu, int order, int dim, int N, const double* y0, long long ld_in,
@@ -105,6 +124,11 @@ int fixed_dispatch(hg_handle* h, int order, int dim, const hg::FixedParams& p, c
     if (order == 4) return launch_fixed<4, 1>(h, p, s);
     if (order == 6) return launch_fixed<6, 1>(h, p, s);
     return launch_fixed<8, 1>(h, p, s);
+  }
+  if (p.ev_index < 0 && lanes_d42(h, p.N) == 14) {
+    if (order == 4) return launch_fixed<4, 14>(h, p, s);
+    if (order == 6) return launch_fixed<6, 14>(h, p, s);
+    return launch_fixed<8, 14>(h, p, s);
   }
   if (order == 4) return launch_fixed<4, 7>(h, p, s);
   if (order == 6) return launch_fixed<6, 7>(h, p, s);
@@ -549,7 +573,7 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
     else
       rc2 = launch_dop853<1>(h, p, s);
   } else {
-    rc2 = launch_dop853<7>(h, p, s);
+    rc2 = lanes_d42(h, N) == 14 ? launch_dop853<14>(h, p, s) : launch_dop853<7>(h, p, s);
   }
   if (rc2 != HG_OK) return rc2;
   return refine_pending(h, p, dim, s);
@@ -599,7 +623,8 @@ int hg_propagate_dop853_segmented(hg_handle* h, double mu, int dim, int N, const
     else
       rc = launch_dop853_seg<1>(h, p, w, seg_steps, max_segments, resume, s);
   } else {
-    rc = launch_dop853_seg<7>(h, p, w, seg_steps, max_segments, resume, s);
+    rc = lanes_d42(h, N) == 14 ? launch_dop853_seg<14>(h, p, w, seg_steps, max_segments, resume, s)
+                               : launch_dop853_seg<7>(h, p, w, seg_steps, max_segments, resume, s);
   }
   if (rc != HG_OK) return rc;
   return refine_pending(h, p, dim, s);
@@ -652,6 +677,8 @@ int hg_propagate_dop853_scheduled(hg_handle* h, double mu, int dim, int N, const
         rc = launch_segment<2>(h, p, w, (int)seg, a, n_live, s);
       else
         rc = launch_segment<1>(h, p, w, (int)seg, a, n_live, s);
+    } else if (lanes_d42(h, n_live) == 14) {
+      rc = launch_segment<14>(h, p, w, (int)seg, a, n_live, s);
     } else {
       rc = launch_segment<7>(h, p, w, (int)seg, a, n_live, s);
     }
@@ -682,6 +709,10 @@ int hg_set_tuning(hg_handle* h, int key, int value) {
         return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 1, 2 or 6");
       h->lanes_d6 = value;
       return HG_OK;
+    case HG_TUNE_LANES_D42:
+      if (value != 0 && value != 7 && value != 14) return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 7 or 14");
+      h->lanes_d42 = value;
+      return HG_OK;
     case HG_TUNE_SPREAD:
       if (value != 0 && value != 1) return fail(h, HG_ERR_ARGS, "spread must be 0 or 1");
       h->spread = value;
@@ -708,6 +739,7 @@ int hg_get_tuning(hg_handle* h, int key, int* value) {
   else if (key == HG_TUNE_DOP853_LANES_D6) *value = h->lanes_d6;
   else if (key == HG_TUNE_SEG_STEPS) *value = h->seg_steps;
   else if (key == HG_TUNE_SPREAD) *value = h->spread;
+  else if (key == HG_TUNE_LANES_D42) *value = h->lanes_d42;
   else return fail(h, HG_ERR_ARGS, "unknown tuning key %d", key);
   return HG_OK;
 }

@@ -184,6 +184,85 @@ struct Layout<1> {
   __device__ __forceinline__ T from_state(T v) const { return v; }
 };
 
+// hessian42 with its work spread over a lane group: lane base + job does job
+// (0..5); L.from(v, r) reads lane base + r.  Lane b*3 + k (b = primary,
+// k < 3) takes one power pair r^3, r^5 of its primary (hg_pow15_25), one
+// reciprocal and two of the twelve quotients:
+//   0: mu2/r3, t1/r3     1: y/r3, z/r3     2: mu2/r5, (mu2 t1)/r5
+//   3: mu/R3,  t2/R3     4: y/R3, z/R3     5: mu/R5,  (mu t2)/R5
+// (further lanes repeat job 0).  The quotients are exchanged, lanes 0..5
+// form xx, yy, zz, ax, ay, az with one common expression
+// ((p + a u) + b w) + c whose operands reproduce hessian42's exactly
+// (x - m == x + (-m), (-a) u == -(a u), -0 + v == v), and those six are
+// exchanged again.  Same operations on the same operands: same bits.
+template <class LT>
+__device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, double y, double z, double vx, double vy,
+                                            double mu) {
+  const double mu2 = 1.0 - mu;
+  const double t1 = x + mu;
+  const double t2 = x - mu2;
+  const double ys = y * y;
+  const double zs = z * z;
+  const double t1s = t1 * t1;
+  const double t2s = t2 * t2;
+  const bool b2 = job >= 3;
+  const int k = b2 ? job - 3 : job;
+  const double rr = ((b2 ? t2s : t1s) + ys) + zs;
+  double p3, p5;
+  hg_pow15_25(rr, p3, p5);
+  const double den = k == 2 ? p5 : p3;
+  const double inv = hg_rcp_rn(den);
+  const double m = b2 ? mu : mu2;
+  const double tt = b2 ? t2 : t1;
+  const double mt = m * tt;
+  const double n0 = k == 1 ? y : m;
+  const double n1 = k == 0 ? tt : (k == 1 ? z : mt);
+  const double q0 = hg_div_rn(n0, den, inv);
+  const double q1 = hg_div_rn(n1, den, inv);
+  // exchange: qa, qb, the r^3 terms of c3, the r^5 terms of sxy
+  const double qa = L.from(q0, 2), qb = L.from(q0, 5);
+  const double c3a = L.from(q0, 0), c3b = L.from(q0, 3);
+  const double sxa = L.from(q1, 2), sxb = L.from(q1, 5);
+  // acceleration lanes 3/4/5 read the x/y/z quotients of both primaries
+  const int ua = job == 3 ? 0 : 1, wa = job == 3 ? 3 : 4;
+  const double u0 = L.from(q0, ua), u1 = L.from(q1, ua), w0 = L.from(q0, wa), w1 = L.from(q1, wa);
+  const double a3 = qa * 3.0;
+  const double b3 = qb * 3.0;
+  const double c3 = c3a + c3b;
+  // job 0 xx, 1 yy, 2 zz, 3 ax, 4 ay, 5 az
+  const bool acc = b2;
+  const int e = job;
+  double P, A, U, B, W, Cc;
+  if (!acc) {
+    P = e == 2 ? -0.0 : 1.0;
+    A = a3;
+    U = e == 0 ? t1s : (e == 1 ? ys : zs);
+    B = b3;
+    W = e == 0 ? t2s : (e == 1 ? ys : zs);
+    Cc = -c3;
+  } else {
+    P = e == 3 ? x : (e == 4 ? y : -0.0);
+    A = -mu2;
+    U = e == 3 ? u1 : (e == 4 ? u0 : u1);  // t1/r3 | y/r3 | z/r3
+    B = -mu;
+    W = e == 3 ? w1 : (e == 4 ? w0 : w1);  // t2/R3 | y/R3 | z/R3
+    Cc = e == 3 ? 2.0 * vy : (e == 4 ? -2.0 * vx : -0.0);
+  }
+  const double form = ((P + A * U) + B * W) + Cc;
+  Hess H;
+  H.xx = L.from(form, 0);
+  H.yy = L.from(form, 1);
+  H.zz = L.from(form, 2);
+  H.ax = L.from(form, 3);
+  H.ay = L.from(form, 4);
+  H.az = L.from(form, 5);
+  const double sxy = sxa + sxb;
+  H.xy = (3.0 * y) * sxy;
+  H.xz = (3.0 * z) * sxy;
+  H.yz = ((3.0 * y) * z) * (qa + qb);
+  return H;
+}
+
 template <>
 struct Layout<7> {
   static constexpr int D = 42;
@@ -199,89 +278,13 @@ struct Layout<7> {
   __device__ __forceinline__ T from_state(T v) const { return __shfl_sync(gmask, v, base + 6); }
   __device__ __forceinline__ double from(double v, int r) const { return __shfl_sync(gmask, v, base + r); }
 
-  // hessian42 with its work spread over the group.  Lane b*3 + k (b = primary,
-  // k < 3) takes one power pair r^3, r^5 of its primary (hg_pow15_25), one
-  // reciprocal and two of the twelve quotients:
-  //   0: mu2/r3, t1/r3     1: y/r3, z/r3     2: mu2/r5, (mu2 t1)/r5
-  //   3: mu/R3,  t2/R3     4: y/R3, z/R3     5: mu/R5,  (mu t2)/R5
-  // (lane 6 repeats lane 0's work).  The quotients are exchanged, lanes 0..5
-  // form xx, yy, zz, ax, ay, az with one common expression
-  // ((p + a u) + b w) + c whose operands reproduce hessian42's exactly
-  // (x - m == x + (-m), (-a) u == -(a u), -0 + v == v), and those six are
-  // exchanged again.  Same operations on the same operands: same bits.
-  __device__ __forceinline__ Hess hessian_split(double x, double y, double z, double vx, double vy,
-                                                double mu) const {
-    const double mu2 = 1.0 - mu;
-    const double t1 = x + mu;
-    const double t2 = x - mu2;
-    const double ys = y * y;
-    const double zs = z * z;
-    const double t1s = t1 * t1;
-    const double t2s = t2 * t2;
-    const bool b2 = role >= 3 && role < 6;
-    const int k = b2 ? role - 3 : (role == 6 ? 0 : role);
-    const double rr = ((b2 ? t2s : t1s) + ys) + zs;
-    double p3, p5;
-    hg_pow15_25(rr, p3, p5);
-    const double den = k == 2 ? p5 : p3;
-    const double inv = hg_rcp_rn(den);
-    const double m = b2 ? mu : mu2;
-    const double tt = b2 ? t2 : t1;
-    const double mt = m * tt;
-    const double n0 = k == 1 ? y : m;
-    const double n1 = k == 0 ? tt : (k == 1 ? z : mt);
-    const double q0 = hg_div_rn(n0, den, inv);
-    const double q1 = hg_div_rn(n1, den, inv);
-    // exchange: qa, qb, the r^3 terms of c3, the r^5 terms of sxy
-    const double qa = from(q0, 2), qb = from(q0, 5);
-    const double c3a = from(q0, 0), c3b = from(q0, 3);
-    const double sxa = from(q1, 2), sxb = from(q1, 5);
-    // acceleration lanes 3/4/5 read the x/y/z quotients of both primaries
-    const int ua = role == 3 ? 0 : 1, wa = role == 3 ? 3 : 4;
-    const double u0 = from(q0, ua), u1 = from(q1, ua), w0 = from(q0, wa), w1 = from(q1, wa);
-    const double a3 = qa * 3.0;
-    const double b3 = qb * 3.0;
-    const double c3 = c3a + c3b;
-    // role 0 xx, 1 yy, 2 zz, 3 ax, 4 ay, 5 az (6: xx again)
-    const bool acc = b2;
-    const int e = role == 6 ? 0 : role;
-    double P, A, U, B, W, Cc;
-    if (!acc) {
-      P = e == 2 ? -0.0 : 1.0;
-      A = a3;
-      U = e == 0 ? t1s : (e == 1 ? ys : zs);
-      B = b3;
-      W = e == 0 ? t2s : (e == 1 ? ys : zs);
-      Cc = -c3;
-    } else {
-      P = e == 3 ? x : (e == 4 ? y : -0.0);
-      A = -mu2;
-      U = e == 3 ? u1 : (e == 4 ? u0 : u1);  // t1/r3 | y/r3 | z/r3
-      B = -mu;
-      W = e == 3 ? w1 : (e == 4 ? w0 : w1);  // t2/R3 | y/R3 | z/R3
-      Cc = e == 3 ? 2.0 * vy : (e == 4 ? -2.0 * vx : -0.0);
-    }
-    const double form = ((P + A * U) + B * W) + Cc;
-    Hess H;
-    H.xx = from(form, 0);
-    H.yy = from(form, 1);
-    H.zz = from(form, 2);
-    H.ax = from(form, 3);
-    H.ay = from(form, 4);
-    H.az = from(form, 5);
-    const double sxy = sxa + sxb;
-    H.xy = (3.0 * y) * sxy;
-    H.xz = (3.0 * z) * sxy;
-    H.yz = ((3.0 * y) * z) * (qa + qb);
-    return H;
-  }
   __device__ __forceinline__ void rhs(const double (&v)[6], double mu, const Dir& dir, double (&dv)[6]) const {
     const double x = from_state(v[0]);
     const double y = from_state(v[1]);
     const double z = from_state(v[2]);
     const double vx = from_state(v[3]);
     const double vy = from_state(v[4]);
-    const Hess H = hessian_split(x, y, z, vx, vy, mu);
+    const Hess H = hessian_split(*this, role == 6 ? 0 : role, x, y, z, vx, vy, mu);
     if (role < 6) {
       // rows of F(x) @ Phi[:, j] (dynamics/rtbp.py:204-209), zero terms skipped
       dv[0] = v[3];
@@ -303,6 +306,50 @@ struct Layout<7> {
       const int c = comp(r);
       dv[r] = neg_if(dv[r], c >= dir.neg_lo && c < dir.neg_hi);
     }
+  }
+};
+
+// G = 14 (42-dim state + STM, latency layout): fourteen lanes own one
+// trajectory, two per STM column and two for the state; lane 2c + h holds
+// rows 3h..3h+2 of column c (components 6(3h + r) + c), lanes 12/13 the
+// position / velocity of the state.  The right-hand side: each lane reads its
+// partner's three components (lane ^ 1); position lanes' derivatives are
+// those components, velocity lanes form rows 3..5 of F(x) Phi[:, c] from
+// them and their own, the state's velocity lane takes the accelerations.  The
+// Hessian is shared as in G = 7 (jobs 0..5 on lanes 0..5).  Same operations
+// and operands as Layout<7>: same bits, at half the stage work per lane.
+template <>
+struct Layout<14> {
+  static constexpr int D = 42;
+  static constexpr int NC = 3;
+  static constexpr int TPW = 2;
+  int role;        // 2c + h (c < 6 STM column, c = 6 state; h = 0 rows 0..2, 1 rows 3..5)
+  int base;
+  unsigned gmask;
+  __device__ __forceinline__ int comp(int r) const {
+    const int c = role >> 1, h = role & 1;
+    return c < 6 ? 6 * (3 * h + r) + c : 36 + 3 * h + r;
+  }
+  __device__ __forceinline__ int owner(int c) const { return c >= 36 ? (c < 39 ? 12 : 13) : 2 * (c % 6) + (c / 6 >= 3); }
+  __device__ __forceinline__ int local(int c) const { return c >= 36 ? (c - 36) % 3 : (c / 6) % 3; }
+  __device__ __forceinline__ double from(double v, int r) const { return __shfl_sync(gmask, v, base + r); }
+  __device__ __forceinline__ void rhs(const double (&v)[3], double mu, const Dir& dir, double (&dv)[3]) const {
+    const double x = from(v[0], 12), y = from(v[1], 12), z = from(v[2], 12);
+    const double vx = from(v[0], 13), vy = from(v[1], 13);
+    const Hess H = hessian_split(*this, role < 6 ? role : 0, x, y, z, vx, vy, mu);
+    const int partner = role ^ 1;
+    const double q0 = from(v[0], partner), q1 = from(v[1], partner), q2 = from(v[2], partner);
+    // rows 3..5 of F(x) Phi[:, c] (dynamics/rtbp.py:204-209): q = rows 0..2, v = rows 3..5
+    const double r3 = ((H.xx * q0 + H.xy * q1) + H.xz * q2) + 2.0 * v[1];
+    const double r4 = ((H.xy * q0 + H.yy * q1) + H.yz * q2) + (-2.0) * v[0];
+    const double r5 = (H.xz * q0 + H.yz * q1) + H.zz * q2;
+    const bool pos = (role & 1) == 0, state = role >= 12;
+    double d0 = pos ? q0 : (state ? H.ax : r3);
+    double d1 = pos ? q1 : (state ? H.ay : r4);
+    double d2 = pos ? q2 : (state ? H.az : r5);
+    dv[0] = neg_if(d0, comp(0) >= dir.neg_lo && comp(0) < dir.neg_hi);
+    dv[1] = neg_if(d1, comp(1) >= dir.neg_lo && comp(1) < dir.neg_hi);
+    dv[2] = neg_if(d2, comp(2) >= dir.neg_lo && comp(2) < dir.neg_hi);
   }
 };
 
@@ -473,6 +520,18 @@ struct Gather<7> {
 };
 
 template <>
+struct Gather<14> {
+  double* slot;  // 42 doubles in shared memory
+  __device__ __forceinline__ double dot(const Layout<14>& L, const double (&v)[3]) const {
+    __syncwarp(L.gmask);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) slot[L.comp(r)] = v[r];
+    __syncwarp(L.gmask);
+    return np_dot_self<42>(slot);
+  }
+};
+
+template <>
 struct Gather<2> {
   // sequential fused accumulation over components 0..5: the position lane's
   // partial sum seeds the velocity lane's
@@ -623,36 +682,37 @@ __device__ __forceinline__ bool finite_bits(double a) {
 // Fixed-step RK kernels, integrators/rk.py:154-215 and :531-588
 // ---------------------------------------------------------------------------
 template <int ORDER, int G>
-__device__ __forceinline__ void rk_fixed_step(const Layout<G>& L, const double (&y)[6], double h, double mu,
-                                              const Dir& dir, double (&yn)[6]) {
+__device__ __forceinline__ void rk_fixed_step(const Layout<G>& L, const double (&y)[Layout<G>::NC], double h,
+                                              double mu, const Dir& dir, double (&yn)[Layout<G>::NC]) {
   using T = FixedTab<ORDER>;
-  double k[T::S][6];
+  constexpr int NC = Layout<G>::NC;
+  double k[T::S][NC];
   L.rhs(y, mu, dir, k[0]);
   static_for<T::S - 1>([&](auto ic) {
     constexpr int i = decltype(ic)::value + 1;
-    double ys[6];
+    double ys[NC];
 #pragma unroll
-    for (int d = 0; d < 6; ++d) ys[d] = y[d];
+    for (int d = 0; d < NC; ++d) ys[d] = y[d];
     static_for<i>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
       constexpr double a = T::a(i, j);
       if constexpr (a != 0.0) {
         const double c = h * a;
 #pragma unroll
-        for (int d = 0; d < 6; ++d) ys[d] = ys[d] + c * k[j][d];
+        for (int d = 0; d < NC; ++d) ys[d] = ys[d] + c * k[j][d];
       }
     });
     L.rhs(ys, mu, dir, k[i]);
   });
 #pragma unroll
-  for (int d = 0; d < 6; ++d) yn[d] = y[d];
+  for (int d = 0; d < NC; ++d) yn[d] = y[d];
   static_for<T::S>([&](auto jc) {
     constexpr int j = decltype(jc)::value;
     constexpr double b = T::b(j);
     if constexpr (b != 0.0) {
       const double c = h * b;
 #pragma unroll
-      for (int d = 0; d < 6; ++d) yn[d] = yn[d] + c * k[j][d];
+      for (int d = 0; d < NC; ++d) yn[d] = yn[d] + c * k[j][d];
     }
   });
 }
@@ -794,6 +854,7 @@ __global__ void __launch_bounds__(128) fixed_rk_event_kernel(FixedParams p) {
 
 template <int ORDER, int G>
 __global__ void __launch_bounds__(128) fixed_rk_kernel(FixedParams p) {
+  constexpr int NC = Layout<G>::NC;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   Layout<G> L;
@@ -801,6 +862,13 @@ __global__ void __launch_bounds__(128) fixed_rk_kernel(FixedParams p) {
   if constexpr (G == 1) {
     L.role = 6;
     traj = warp * 32 + lane;
+  } else if constexpr (G == 14) {
+    if (lane >= 28) return;
+    const int g = lane / 14;
+    L.role = lane % 14;
+    L.base = g * 14;
+    L.gmask = 0x3FFFu << L.base;
+    traj = warp * 2 + g;
   } else {
     if (lane >= 28) return;
     const int g = lane / 7;
@@ -810,34 +878,33 @@ __global__ void __launch_bounds__(128) fixed_rk_kernel(FixedParams p) {
     traj = warp * 4 + g;
   }
   if (traj >= p.N) return;
-  double y[6];
+  double y[NC];
 #pragma unroll
-  for (int r = 0; r < 6; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld_in + traj];
-  const int n_out = (p.n - 1) / p.out_every + 1;
-  (void)n_out;
+  for (int r = 0; r < NC; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld_in + traj];
 #pragma unroll
-  for (int r = 0; r < 6; ++r) p.out[(long long)L.comp(r) * p.ld_out + traj] = y[r];
+  for (int r = 0; r < NC; ++r) p.out[(long long)L.comp(r) * p.ld_out + traj] = y[r];
   const long long row = (long long)Layout<G>::D * p.ld_out;
   bool finite = true;
   for (int idx = 0; idx < p.n - 1; ++idx) {
     const double h = p.t_vals[idx + 1] - p.t_vals[idx];
-    double yn[6];
+    double yn[NC];
     rk_fixed_step<ORDER, G>(L, y, h, p.mu, p.dir, yn);
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
+    for (int r = 0; r < NC; ++r) {
       y[r] = yn[r];
       finite = finite && finite_bits(yn[r]);
     }
     if ((idx + 1) % p.out_every == 0) {
       double* o = p.out + (long long)((idx + 1) / p.out_every) * row;
 #pragma unroll
-      for (int r = 0; r < 6; ++r) o[(long long)L.comp(r) * p.ld_out + traj] = y[r];
+      for (int r = 0; r < NC; ++r) o[(long long)L.comp(r) * p.ld_out + traj] = y[r];
     }
   }
   if (p.status) {
-    if constexpr (G == 7) {
+    if constexpr (G > 1) {
       finite = __all_sync(L.gmask, finite);
-      if (L.role != 6) return;
+      // one lane of the group writes the status
+      if (L.role != (G == 7 ? 6 : 0)) return;
     }
     p.status[traj] = finite ? HG_OK : HG_NONFINITE;
   }
@@ -1075,6 +1142,14 @@ __device__ __forceinline__ bool setup_layout(Layout<G>& L, Gather<G>& gat, doubl
     L.base = g * 6;
     L.gmask = 0x3Fu << L.base;
     traj = warp * 5 + g;
+  } else if constexpr (G == 14) {
+    if (lane >= 28) return false;
+    const int g = lane / 14;
+    L.role = lane % 14;
+    L.base = g * 14;
+    L.gmask = 0x3FFFu << L.base;
+    traj = warp * 2 + g;
+    gat.slot = sm_gather + ((threadIdx.x >> 5) * 2 + g) * 42;
   } else {
     if (lane >= 28) return false;
     const int g = lane / 7;
@@ -1087,9 +1162,16 @@ __device__ __forceinline__ bool setup_layout(Layout<G>& L, Gather<G>& gat, doubl
   return true;
 }
 
+// Shared-memory doubles a block of up to four warps needs for the 42-vector
+// norm (one 42-double slot per lane group).
+template <int G>
+__host__ __device__ constexpr int gather_smem_doubles() {
+  return G == 7 ? 4 * 4 * 42 : (G == 14 ? 4 * 2 * 42 : 1);
+}
+
 template <int G>
 __device__ __forceinline__ bool is_leader(const Layout<G>& L) {
-  return (G == 1) || ((G == 2 || G == 6) && L.role == 0) || (G == 7 && L.role == 6);
+  return (G == 1) || ((G == 2 || G == 6 || G == 14) && L.role == 0) || (G == 7 && L.role == 6);
 }
 
 // Where the event component lives in a group: its register index r on the
@@ -1201,7 +1283,7 @@ __global__ void __launch_bounds__(128) refine_kernel(DopParams p) {
   Layout<G> L;
   Gather<G> gat;
   int slot;
-  __shared__ double sm_gather[(G == 7) ? 4 * 4 * 42 : 1];
+  __shared__ double sm_gather[gather_smem_doubles<G>()];
   if (!setup_layout<G>(L, gat, sm_gather, slot)) return;
   const bool leader = is_leader<G>(L);
   const EvCtx<G> ev(L, p.ev_index);
@@ -1240,7 +1322,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
   Layout<G> L;
   Gather<G> gat;
   int traj;
-  __shared__ double sm_gather[(G == 7) ? 4 * 4 * 42 : 1];  // 4 warps x 4 groups
+  __shared__ double sm_gather[gather_smem_doubles<G>()];  // 4 warps x 4 groups
   if (!setup_layout<G>(L, gat, sm_gather, traj)) return;
   const bool leader = is_leader<G>(L);
   const bool has_event = p.ev_index >= 0 && p.max_hits > 0;

@@ -246,6 +246,9 @@ int hg_trajectory_filters(int N, int m, const double* samples, long long ld, dou
  * (the default).
  * HG_TUNE_SEG_STEPS: attempted steps per segment of
  * hg_propagate_dop853_scheduled (default 16).
+ * HG_TUNE_LANES_D42: lanes per 42-dim trajectory (fixed RK without an event
+ * and DOP853): 7 (an STM column per lane), 14 (half a column per lane: 0.65x
+ * the per-step latency), 0 = automatic (the default).
  * HG_TUNE_SPREAD: 1 = DOP853 launches use blocks of four warps that each
  * occupy a whole SM (one warp per SM sub-partition); 0 = HG_TUNE_BLOCK_THREADS
  * blocks (default).
@@ -255,6 +258,7 @@ int hg_trajectory_filters(int N, int m, const double* samples, long long ld, dou
 #define HG_TUNE_DOP853_LANES_D6 2
 #define HG_TUNE_SEG_STEPS 3
 #define HG_TUNE_SPREAD 4
+#define HG_TUNE_LANES_D42 5
 int hg_set_tuning(hg_handle* h, int key, int value);
 int hg_get_tuning(hg_handle* h, int key, int* value);
 

@@ -15,14 +15,15 @@ pytestmark = pytest.mark.gpu
 MU = W.MU_EM
 
 
-@pytest.fixture(params=[(1, 32, 0), (2, 32, 0), (1, 128, 0), (2, 64, 0), (6, 32, 0), (6, 128, 0), (1, 32, 1),
-                        (6, 32, 1)],
-                ids=["lanes1-b32", "lanes2-b32", "lanes1-b128", "lanes2-b64", "lanes6-b32", "lanes6-b128",
-                     "lanes1-spread", "lanes6-spread"])
+@pytest.fixture(params=[(1, 32, 0, 7), (2, 32, 0, 14), (1, 128, 0, 14), (2, 64, 0, 7), (6, 32, 0, 14),
+                        (6, 128, 0, 7), (1, 32, 1, 14), (6, 32, 1, 7)],
+                ids=["lanes1-b32-d42x7", "lanes2-b32-d42x14", "lanes1-b128-d42x14", "lanes2-b64-d42x7",
+                     "lanes6-b32-d42x14", "lanes6-b128-d42x7", "lanes1-spread-d42x14", "lanes6-spread-d42x7"])
 def shape(request, gpu):
-    """Every launch shape must give the same bits."""
-    lanes, block, spread = request.param
-    with gpu.tuning(lanes_d6=lanes, block=block, spread=spread):
+    """Every launch shape must give the same bits (6-dim lanes, block, spread,
+    42-dim lanes)."""
+    lanes, block, spread, lanes42 = request.param
+    with gpu.tuning(lanes_d6=lanes, block=block, spread=spread, lanes_d42=lanes42):
         yield request.param
 
 
@@ -53,11 +54,13 @@ def test_fixed_matches_oracle_bitexact(gpu, shape, dev_oracle, order, dim):
     assert np.array_equal(out, ref.transpose(1, 0, 2))
 
 
-def test_fixed_rk8_stm_config_rows_bitexact(gpu, dev_oracle):
+@pytest.mark.parametrize("lanes42", [7, 14])
+def test_fixed_rk8_stm_config_rows_bitexact(gpu, dev_oracle, lanes42):
     """The 42-dim RK8 workload (t in [0,3], 3000 steps, every 100th state) on 16 states."""
     y0 = W.stm_fixed_batch(1024, seed=0)[:16]
     t = np.linspace(0.0, 3.0, 3001)
-    out = _np(gpu.propagate_fixed(y0, t, MU, order=8, out_every=100))
+    with gpu.tuning(lanes_d42=lanes42):
+        out = _np(gpu.propagate_fixed(y0, t, MU, order=8, out_every=100))
     ref, st = dev_oracle.fixed_rk_batch(8, y0, t, MU, out_every=100)
     assert np.array_equal(out, ref.transpose(1, 0, 2))
 

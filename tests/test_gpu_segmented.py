@@ -62,15 +62,19 @@ def test_segmented_multihit_ragged_tmax(gpu, seg_steps, max_segments):
     _same(ref, seg, with_event=True)
 
 
+@pytest.mark.parametrize("lanes42", [7, 14])
 @pytest.mark.parametrize("last_only", [False, True])
 @pytest.mark.parametrize("seg_steps,max_segments", [(1, 3), (5, 2), (40, 8)])
-def test_segmented_stm_dense(gpu, dev_oracle, last_only, seg_steps, max_segments):
+def test_segmented_stm_dense(gpu, dev_oracle, last_only, seg_steps, max_segments, lanes42):
     x0 = W.HALO_L1_AZ02_X0
     y0 = np.array([stm_state(x0 + d) for d in np.linspace(-1e-4, 1e-4, 9)[:, None] * np.eye(6)[0]])
     T = W.HALO_L1_AZ02_T
-    seg = gpu.propagate_dop853(y0, 0.0, T, MU, fwd=-1, flip=(36, 42), n_samples=40, sample_last_only=last_only,
-                               segmented=True, seg_steps=seg_steps, max_segments=max_segments)
-    ref = gpu.propagate_dop853(y0, 0.0, T, MU, fwd=-1, flip=(36, 42), n_samples=40, sample_last_only=last_only)
+    with gpu.tuning(lanes_d42=lanes42):
+        seg = gpu.propagate_dop853(y0, 0.0, T, MU, fwd=-1, flip=(36, 42), n_samples=40,
+                                   sample_last_only=last_only, segmented=True, seg_steps=seg_steps,
+                                   max_segments=max_segments)
+    with gpu.tuning(lanes_d42=7):
+        ref = gpu.propagate_dop853(y0, 0.0, T, MU, fwd=-1, flip=(36, 42), n_samples=40, sample_last_only=last_only)
     _same(ref, seg, samples=True)
     if not last_only:
         out = _np(seg.samples)
