@@ -35,6 +35,7 @@ HG_TUNE_DOP853_LANES_D6 = 2
 HG_TUNE_SEG_STEPS = 3
 HG_TUNE_SPREAD = 4
 HG_TUNE_LANES_D42 = 5
+HG_TUNE_SM_CAPACITY = 6
 
 
 class HitenGpuError(RuntimeError):

@@ -31,12 +31,14 @@ DOP853_PLANS = (
     {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 8},
     {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 16},
     {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 32},
+    {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 16, "sm_capacity": 4.5},
+    {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 32, "sm_capacity": 4.5},
 )
 _plan_cache = {}
 
 
 def _knobs(plan):
-    return {k: plan[k] for k in ("lanes_d6", "block", "spread", "seg_steps") if k in plan}
+    return {k: plan[k] for k in ("lanes_d6", "block", "spread", "seg_steps", "sm_capacity") if k in plan}
 
 
 def tune_dop853(key, run, plans=DOP853_PLANS, reps=2, device=None):
@@ -63,7 +65,8 @@ def tune_dop853(key, run, plans=DOP853_PLANS, reps=2, device=None):
 
 def plan_name(plan):
     if plan["scheduled"]:
-        return f"scheduled_seg{plan.get('seg_steps', 16)}"
+        cap = f"_cap{plan['sm_capacity']:g}" if "sm_capacity" in plan else ""
+        return f"scheduled_seg{plan.get('seg_steps', 16)}{cap}"
     return f"lanes{plan['lanes_d6']}_block{plan['block']}" + ("_spread" if plan.get("spread") else "")
 
 

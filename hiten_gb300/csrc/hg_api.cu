@@ -18,6 +18,7 @@ struct hg_handle {
   int block = 32;           // threads per block (32, 64 or 128)
   int lanes_d6 = 0;         // lanes per 6-dim DOP853 trajectory: 0 auto, 1, 2, 6
   int lanes_d42 = 0;        // lanes per 42-dim trajectory (fixed RK and DOP853): 0 auto, 7, 14
+  int sm_capacity_x10 = 30;  // warps' FP64 demand an SM serves at full speed, x10 (layout cost models)
   int seg_steps = 16;       // attempted steps per segment of the scheduled DOP853 driver
   int spread = 0;           // 1: DOP853 blocks of 4 warps, one block per SM (one warp per sub-partition)
   int smem_per_sm = 0;      // bytes of shared memory per SM
@@ -86,7 +87,7 @@ int launch_fixed(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
 // warps' FP64 demand, beyond which warps share the SM's FP64 unit.
 int lanes_d42(const hg_handle* h, int n) {
   if (h->lanes_d42 != 0) return h->lanes_d42;
-  const double cap = 3.0 * h->sm_count;
+  const double cap = 0.1 * h->sm_capacity_x10 * h->sm_count;
   const double w7 = (double)((n + 3) / 4), w14 = (double)((n + 1) / 2);
   const double c7 = 1.0 * (w7 > cap ? w7 / cap : 1.0);
   const double c14 = 0.65 * (w14 > cap ? w14 / cap : 1.0);
@@ -367,7 +368,7 @@ int launch_dop853_seg(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_ste
 // four lose ~13 %), beyond which they share it.
 int sched_lanes_d6(const hg_handle* h, int n_live) {
   if (h->lanes_d6 != 0) return h->lanes_d6;
-  const double smsp = 3.0 * h->sm_count;
+  const double smsp = 0.1 * h->sm_capacity_x10 * h->sm_count;
   const int gs[3] = {1, 2, 6};
   const int tpw[3] = {32, 16, 5};
   const double lat[3] = {1.0, 0.622, 0.400};
@@ -709,6 +710,10 @@ int hg_set_tuning(hg_handle* h, int key, int value) {
         return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 1, 2 or 6");
       h->lanes_d6 = value;
       return HG_OK;
+    case HG_TUNE_SM_CAPACITY:
+      if (value < 5 || value > 640) return fail(h, HG_ERR_ARGS, "capacity (tenths of warps per SM) must be in [5, 640]");
+      h->sm_capacity_x10 = value;
+      return HG_OK;
     case HG_TUNE_LANES_D42:
       if (value != 0 && value != 7 && value != 14) return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 7 or 14");
       h->lanes_d42 = value;
@@ -740,6 +745,7 @@ int hg_get_tuning(hg_handle* h, int key, int* value) {
   else if (key == HG_TUNE_SEG_STEPS) *value = h->seg_steps;
   else if (key == HG_TUNE_SPREAD) *value = h->spread;
   else if (key == HG_TUNE_LANES_D42) *value = h->lanes_d42;
+  else if (key == HG_TUNE_SM_CAPACITY) *value = h->sm_capacity_x10;
   else return fail(h, HG_ERR_ARGS, "unknown tuning key %d", key);
   return HG_OK;
 }

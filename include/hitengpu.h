@@ -249,6 +249,8 @@ int hg_trajectory_filters(int N, int m, const double* samples, long long ld, dou
  * HG_TUNE_LANES_D42: lanes per 42-dim trajectory (fixed RK without an event
  * and DOP853): 7 (an STM column per lane), 14 (half a column per lane: 0.65x
  * the per-step latency), 0 = automatic (the default).
+ * HG_TUNE_SM_CAPACITY: the layout cost models' FP64 capacity of an SM, in
+ * tenths of a warp's demand (default 30: three warps run at full speed).
  * HG_TUNE_SPREAD: 1 = DOP853 launches use blocks of four warps that each
  * occupy a whole SM (one warp per SM sub-partition); 0 = HG_TUNE_BLOCK_THREADS
  * blocks (default).
@@ -259,6 +261,7 @@ int hg_trajectory_filters(int N, int m, const double* samples, long long ld, dou
 #define HG_TUNE_SEG_STEPS 3
 #define HG_TUNE_SPREAD 4
 #define HG_TUNE_LANES_D42 5
+#define HG_TUNE_SM_CAPACITY 6
 int hg_set_tuning(hg_handle* h, int key, int value);
 int hg_get_tuning(hg_handle* h, int key, int* value);
 
