@@ -304,8 +304,39 @@ def bench_serving(args):
           speedup_vs_plain=served_burst["traj_steps_per_s"] / seq_burst["traj_steps_per_s"])
 
 
+def bench_continuation(args):
+    """Halo-family continuation: 64 families (corrected L1/L2 halos, Az 0.05-0.3) continued in z for 12
+    members each with the secant stepper; every round corrects the next member of all families in one
+    batched correction."""
+    import torch
+    from hiten_gb300 import continuation as Cn
+    from hiten_gb300 import corrector, halo
+    from hiten_gb300 import workloads as W
+    mu = W.MU_EM
+    rng = np.random.default_rng(3)
+    pts = np.repeat([1, 2], 32)
+    az = rng.uniform(0.05, 0.3, 64)
+    g = np.concatenate([halo.third_order_guess(mu, 1, az[:32], "southern"),
+                        halo.third_order_guess(mu, 2, az[32:], "southern")])
+    seed = corrector.correct_halo(g, mu)
+    ok = seed.status == 0
+    opts = Cn.ContinuationOptions(step=(0.002,), max_members=12)
+    Cn.continue_halo_families(seed.x0[ok][:4], seed.period[ok][:4], mu, options=opts)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = Cn.continue_halo_families(seed.x0[ok], seed.period[ok], mu, options=opts)
+    torch.cuda.synchronize()
+    s = time.perf_counter() - t0
+    members = sum(r.accepted_count - 1 for r in res)
+    _line("halo-family continuation, 64 families x 12 members (secant, z)", "family members/s", members / s,
+          "members/s", s * 1e3, {"families": int(ok.sum()), "members": 12,
+                                 "l1_families": int(np.sum(pts[ok] == 1)), "l2_families": int(np.sum(pts[ok] == 2))},
+          accepted=members, rejected=sum(r.rejected_count for r in res),
+          rounds=max(r.iterations for r in res))
+
+
 EXTRA = {"fixed_stm": bench_fixed_stm, "section": bench_section, "correct": bench_correct,
-         "serving": bench_serving}
+         "serving": bench_serving, "continuation": bench_continuation}
 
 
 def main():
