@@ -335,8 +335,41 @@ def bench_continuation(args):
           rounds=max(r.iterations for r in res))
 
 
+def bench_connections(args):
+    """Connections between two synthetic sections of 65536 points each (noisy closed curves on the
+    (y, vy) plane, as manifold cuts look), eps = 1e-4: the radius pairing in both directions and the
+    nearest neighbours of both sets (4 all-pairs searches of 4.3e9 pairs), then the host refinement."""
+    import torch
+    from hiten_gb300.connections import find_connections
+    n = 65536
+    rng = np.random.default_rng(5)
+
+    def curve(ph):
+        s = rng.uniform(0, 1, n)
+        return np.c_[0.1 * np.cos(2 * np.pi * s + ph) + rng.normal(0, 1e-4, n),
+                     0.3 * np.sin(2 * np.pi * s + ph) + rng.normal(0, 1e-4, n)]
+
+    pu, ps = curve(0.0), curve(0.3)
+    Xu = np.c_[np.full(n, 0.85), pu[:, 0], np.zeros(n), rng.normal(0, 1e-3, n), pu[:, 1], rng.normal(0, 1e-3, n)]
+    Xs = np.c_[np.full(n, 0.85), ps[:, 0], np.zeros(n), rng.normal(0, 1e-3, n), ps[:, 1], rng.normal(0, 1e-3, n)]
+    run = lambda: find_connections(pu, ps, Xu, Xs, eps=1e-4, dv_tol=1e-2, bal_tol=1e-4)
+    run()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(max(2, args.steps // 4)):
+        t0 = time.perf_counter()
+        res, meta = run()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    sec = statistics.median(ts)
+    pair_tests = 4.0 * n * n
+    _line("connections, 65536 x 65536 section points, eps 1e-4", "pair tests/s", pair_tests / sec, "pairs/s",
+          sec * 1e3, {"points_u": n, "points_s": n, "eps": 1e-4}, connections=len(res),
+          pairs_considered=meta.get("pairs_considered", 0))
+
+
 EXTRA = {"fixed_stm": bench_fixed_stm, "section": bench_section, "correct": bench_correct,
-         "serving": bench_serving, "continuation": bench_continuation}
+         "serving": bench_serving, "continuation": bench_continuation, "connections": bench_connections}
 
 
 def main():

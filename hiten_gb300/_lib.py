@@ -27,7 +27,7 @@ EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg
             "hg_propagate_dop853", "hg_probe_fp64_peak", "hg_propagate_dop853_noalloc", "hg_set_tuning",
             "hg_get_tuning", "hg_section_detect", "hg_trajectory_filters", "hg_propagate_fixed_event",
             "hg_dop853_segmented_workspace_bytes", "hg_propagate_dop853_segmented",
-            "hg_propagate_dop853_scheduled", "hg_get_counter")
+            "hg_propagate_dop853_scheduled", "hg_get_counter", "hg_radius_best", "hg_nearest_neighbor")
 HG_COUNTER_KERNEL_LAUNCHES = 1
 HG_RUNNING = -1
 HG_TUNE_BLOCK_THREADS = 1
@@ -117,6 +117,10 @@ def load(build_if_missing=True):
         L.hg_set_tuning.restype = C.c_int
         L.hg_get_tuning.argtypes = [_P, C.c_int, C.POINTER(C.c_int)]
         L.hg_get_tuning.restype = C.c_int
+        L.hg_radius_best.argtypes = [C.c_int, _P, _P, C.c_int, _P, _P, C.c_double, C.c_double, _P, _P, _P, _P]
+        L.hg_radius_best.restype = C.c_int
+        L.hg_nearest_neighbor.argtypes = [C.c_int, _P, _P, C.c_double, _P, _P]
+        L.hg_nearest_neighbor.restype = C.c_int
         L.hg_get_counter.argtypes = [_P, C.c_int, C.POINTER(C.c_longlong)]
         L.hg_get_counter.restype = C.c_int
         L.hg_probe_fp64_peak.argtypes = [_P, C.POINTER(C.c_double)]

@@ -1,0 +1,208 @@
+"""Heteroclinic / impulsive connections between two synodic sections.
+
+Mirrors connections/backends.py:410-540 (``_ConnectionsBackend.run``): pair
+the unstable-side section points with the stable-side ones within ``eps``,
+keep mutual nearest pairs, refine each on the segments to the points' own
+nearest neighbours (the closest points of two 2-D segments), interpolate
+the states there and classify the velocity jump.  The two all-pairs searches
+(radius pairing with each point's nearest partner, nearest neighbours within
+a set) run on the GPU (``hg_radius_best``, ``hg_nearest_neighbor``); the
+per-pair refinement is the reference's scalar arithmetic on the host.
+"""
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import propagate as P
+
+
+@dataclass
+class ConnectionResult:
+    """connections/types.py:60-120 (_ConnectionResult)."""
+
+    kind: str
+    delta_v: float
+    point2d: tuple
+    state_u: np.ndarray
+    state_s: np.ndarray
+    index_u: int
+    index_s: int
+    trajectory_index_u: int
+    trajectory_index_s: int
+
+
+class GpuSectionMatcher:
+    """The two all-pairs searches on the GPU."""
+
+    def __init__(self, device=None):
+        self.device = P._device(device)
+
+    def _xy(self, pts):
+        t = torch.as_tensor(np.ascontiguousarray(pts, dtype=np.float64), device=self.device)
+        return t[:, 0].contiguous(), t[:, 1].contiguous()
+
+    def radius_best(self, q, r, eps, coord_max):
+        L = _lib.load()
+        nq, nr = q.shape[0], r.shape[0]
+        qx, qy = self._xy(q)
+        rx, ry = self._xy(r)
+        cnt = torch.empty(nq, dtype=torch.int32, device=self.device)
+        bi = torch.empty(nq, dtype=torch.int32, device=self.device)
+        bd = torch.empty(nq, dtype=torch.float64, device=self.device)
+        st = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        with torch.cuda.device(self.device):
+            rc = L.hg_radius_best(nq, P._ptr(qx), P._ptr(qy), nr, P._ptr(rx), P._ptr(ry), float(eps), float(coord_max),
+                                  P._ptr(cnt), P._ptr(bi), P._ptr(bd), st)
+        if rc != _lib.HG_OK:
+            raise _lib.HitenGpuError(rc, "hg_radius_best failed")
+        return cnt.cpu().numpy().astype(np.int64), bi.cpu().numpy().astype(np.int64), bd.cpu().numpy()
+
+    def nearest(self, p, coord_max):
+        L = _lib.load()
+        n = p.shape[0]
+        x, y = self._xy(p)
+        out = torch.empty(n, dtype=torch.int32, device=self.device)
+        st = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        with torch.cuda.device(self.device):
+            rc = L.hg_nearest_neighbor(n, P._ptr(x), P._ptr(y), float(coord_max), P._ptr(out), st)
+        if rc != _lib.HG_OK:
+            raise _lib.HitenGpuError(rc, "hg_nearest_neighbor failed")
+        return out.cpu().numpy().astype(np.int64)
+
+
+def closest_points_on_segments_2d(a0x, a0y, a1x, a1y, b0x, b0y, b1x, b1y):
+    """connections/backends.py:237-320, the same scalar operations."""
+    ux = a1x - a0x
+    uy = a1y - a0y
+    vx = b1x - b0x
+    vy = b1y - b0y
+    wx = a0x - b0x
+    wy = a0y - b0y
+    A = ux * ux + uy * uy
+    B = ux * vx + uy * vy
+    Cc = vx * vx + vy * vy
+    D = ux * wx + uy * wy
+    E = vx * wx + vy * wy
+    den = A * Cc - B * B
+    s = 0.0
+    t = 0.0
+    if den > 0.0:
+        s = (B * E - Cc * D) / den
+        t = (A * E - B * D) / den
+    if s < 0.0:
+        s = 0.0
+        if Cc > 0.0:
+            t = E / Cc
+    elif s > 1.0:
+        s = 1.0
+        if Cc > 0.0:
+            t = (E + B) / Cc
+    if t < 0.0:
+        t = 0.0
+        if A > 0.0:
+            s = -D / A
+            if s < 0.0:
+                s = 0.0
+            elif s > 1.0:
+                s = 1.0
+    elif t > 1.0:
+        t = 1.0
+        if A > 0.0:
+            s = (B - D) / A
+            if s < 0.0:
+                s = 0.0
+            elif s > 1.0:
+                s = 1.0
+    return s, t, a0x + s * ux, a0y + s * uy, b0x + t * vx, b0y + t * vy
+
+
+def closest_points_on_segments_2d_batch(a0x, a0y, a1x, a1y, b0x, b0y, b1x, b1y):
+    """closest_points_on_segments_2d for arrays: the same expressions and the
+    same order of the clamping branches, elementwise."""
+    ux = a1x - a0x
+    uy = a1y - a0y
+    vx = b1x - b0x
+    vy = b1y - b0y
+    wx = a0x - b0x
+    wy = a0y - b0y
+    A = ux * ux + uy * uy
+    B = ux * vx + uy * vy
+    Cc = vx * vx + vy * vy
+    D = ux * wx + uy * wy
+    E = vx * wx + vy * wy
+    den = A * Cc - B * B
+    with np.errstate(divide="ignore", invalid="ignore"):
+        pos = den > 0.0
+        s = np.where(pos, (B * E - Cc * D) / den, 0.0)
+        t = np.where(pos, (A * E - B * D) / den, 0.0)
+        lo, hi = s < 0.0, s > 1.0
+        t = np.where(lo & (Cc > 0.0), E / Cc, t)
+        t = np.where(~lo & hi & (Cc > 0.0), (E + B) / Cc, t)
+        s = np.where(lo, 0.0, np.where(hi, 1.0, s))
+        tlo, thi = t < 0.0, t > 1.0
+        s_lo = np.clip(-D / A, 0.0, 1.0)
+        s_hi = np.clip((B - D) / A, 0.0, 1.0)
+        s = np.where(tlo & (A > 0.0), s_lo, s)
+        s = np.where(~tlo & thi & (A > 0.0), s_hi, s)
+        t = np.where(tlo, 0.0, np.where(thi, 1.0, t))
+    return s, t, a0x + s * ux, a0y + s * uy, b0x + t * vx, b0y + t * vy
+
+
+def find_connections(points_u, points_s, states_u, states_s, traj_indices_u=None, traj_indices_s=None, eps=1e-3,
+                     dv_tol=1e-3, bal_tol=1e-6, max_seg_len=1e9, matcher=None, device=None):
+    """Connections between the unstable-side section (points_u (N, 2),
+    states_u (N, 6)) and the stable-side one (points_s, states_s).
+    Returns (results sorted by delta_v, metadata)."""
+    pu = np.ascontiguousarray(points_u, dtype=np.float64).reshape(-1, 2)
+    ps = np.ascontiguousarray(points_s, dtype=np.float64).reshape(-1, 2)
+    Xu = np.asarray(states_u, dtype=np.float64)
+    Xs = np.asarray(states_s, dtype=np.float64)
+    if pu.size == 0 or ps.size == 0:
+        return [], {}
+    m = matcher or GpuSectionMatcher(device)
+    R = float(max(np.max(np.abs(pu)), np.max(np.abs(ps))))
+    cnt_u, best_u, d2_u = m.radius_best(pu, ps, eps, R)
+    total = int(cnt_u.sum())
+    if total == 0:
+        return [], {}
+    _, best_s, d2_s = m.radius_best(ps, pu, eps, R)
+    # mutual nearest pairs, in the order of the unstable-side index
+    cand = np.nonzero(cnt_u > 0)[0]
+    jb = best_u[cand]
+    keep = (best_s[jb] == cand) & (d2_s[jb] == d2_u[cand])
+    I, J = cand[keep], jb[keep]
+    if I.size == 0:
+        return [], {}
+    nn_u = m.nearest(pu, R) if pu.shape[0] >= 2 else np.full(pu.shape[0], -1, dtype=np.int64)
+    nn_s = m.nearest(ps, R) if ps.shape[0] >= 2 else np.full(ps.shape[0], -1, dtype=np.int64)
+    iu, js = nn_u[I], nn_s[J]
+    ok = ~((iu < 0) | (js < 0) | (iu == I) | (js == J))
+    iu_c, js_c = np.where(ok, iu, I), np.where(ok, js, J)
+    du = np.hypot(pu[iu_c, 0] - pu[I, 0], pu[iu_c, 1] - pu[I, 1])
+    ds = np.hypot(ps[js_c, 0] - ps[J, 0], ps[js_c, 1] - ps[J, 1])
+    ok &= ~((du > max_seg_len) | (ds > max_seg_len))
+    s, t, px, py, qx, qy = closest_points_on_segments_2d_batch(
+        pu[I, 0], pu[I, 1], pu[iu_c, 0], pu[iu_c, 1], ps[J, 0], ps[J, 1], ps[js_c, 0], ps[js_c, 1])
+    s = np.where(ok, s, 0.0)
+    t = np.where(ok, t, 0.0)
+    xu = np.where(ok[:, None], (1.0 - s)[:, None] * Xu[I] + s[:, None] * Xu[iu_c], Xu[I])
+    xs = np.where(ok[:, None], (1.0 - t)[:, None] * Xs[J] + t[:, None] * Xs[js_c], Xs[J])
+    ptx = np.where(ok, 0.5 * (px + qx), pu[I, 0])
+    pty = np.where(ok, 0.5 * (py + qy), pu[I, 1])
+    dvv = xu[:, 3:6] - xs[:, 3:6]
+    results = []
+    for k in range(I.size):
+        dv = float(np.linalg.norm(dvv[k]))  # numpy's norm, as the reference computes it
+        if dv <= dv_tol:
+            i, j = int(I[k]), int(J[k])
+            results.append(ConnectionResult(
+                kind="ballistic" if dv <= bal_tol else "impulsive", delta_v=dv,
+                point2d=(float(ptx[k]), float(pty[k])), state_u=xu[k].copy(), state_s=xs[k].copy(), index_u=i,
+                index_s=j, trajectory_index_u=int(traj_indices_u[i]) if traj_indices_u is not None else 0,
+                trajectory_index_s=int(traj_indices_s[j]) if traj_indices_s is not None else 0))
+    results.sort(key=lambda r: r.delta_v)
+    return results, {"pairs_considered": total, "accepted": len(results)}

@@ -237,6 +237,22 @@ int hg_section_detect(int N, int m, const double* samples, long long ld,
 int hg_trajectory_filters(int N, int m, const double* samples, long long ld, double mu,
                           double* min_r1, double* min_r2, double* max_rel_energy, void* stream);
 
+/* Section-point matching for connections (handle-free, asynchronous on
+ * `stream`; point sets as two coordinate arrays each).
+ * hg_radius_best: for each query point, the number of reference points
+ * within eps (dx*dx + dy*dy <= eps^2 in FP64) and the nearest of them
+ * (strict <, the lowest index wins ties; -1 if none).
+ * hg_nearest_neighbor: each point's nearest other point of the same set
+ * (strict <, lowest index on ties; -1 when n < 2).
+ * coord_max >= every |coordinate| involved: it sizes the FP32 pre-screen,
+ * whose margin provably keeps the FP64 results exact.
+ * Replaces: connections/backends.py:31-99 (_pair_counts, _radpair2d: counts
+ * and the pairs' per-query minimum used by _ConnectionsBackend.run :444-460)
+ * and :174-235 (_nearest_neighbor_2d). */
+int hg_radius_best(int nq, const double* qx, const double* qy, int nr, const double* rx, const double* ry,
+                   double eps, double coord_max, int* count, int* best_idx, double* best_d2, void* stream);
+int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_max, int* out, void* stream);
+
 /* Launch-shape tuning of a handle (set by hiten_gb300.autotune).
  * HG_TUNE_BLOCK_THREADS: threads per block, 32 (default), 64 or 128.
  * HG_TUNE_DOP853_LANES_D6: lanes per 6-dim DOP853 trajectory: 1 (one

@@ -1,0 +1,42 @@
+"""The connections host logic (hiten_gb300/connections.py) with the CPU
+oracle of its two all-pairs searches reproduces the reference's own
+_ConnectionsBackend.run results bit for bit (tests/golden/connections.npz:
+four seeded section clouds, one with duplicate points and distance ties,
+one with a single unstable-side point)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(os.path.join(GOLDEN, "connections.npz"))
+
+
+def _check(res, meta, gold, c):
+    n = len(gold[f"{c}/dv"])
+    assert len(res) == n
+    assert meta.get("pairs_considered", 0) == int(gold[f"{c}/pairs_considered"])
+    if n == 0:
+        return
+    assert np.array_equal(np.array([r.kind == "ballistic" for r in res]), gold[f"{c}/kind"])
+    assert np.array_equal(np.array([r.delta_v for r in res]), gold[f"{c}/dv"])
+    assert np.array_equal(np.array([r.point2d for r in res]), gold[f"{c}/point"])
+    assert np.array_equal(np.array([r.state_u for r in res]), gold[f"{c}/state_u"])
+    assert np.array_equal(np.array([r.state_s for r in res]), gold[f"{c}/state_s"])
+    idx = np.array([[r.index_u, r.index_s, r.trajectory_index_u, r.trajectory_index_s] for r in res])
+    assert np.array_equal(idx, gold[f"{c}/index"])
+
+
+@pytest.mark.parametrize("c", [0, 1, 2, 3])
+def test_connections_reproduce_reference(gold, c):
+    from oracle.connect import OracleSectionMatcher
+    from hiten_gb300.connections import find_connections
+    eps, dvt, bt = gold[f"{c}/params"]
+    res, meta = find_connections(gold[f"{c}/pu"], gold[f"{c}/ps"], gold[f"{c}/Xu"], gold[f"{c}/Xs"],
+                                 gold[f"{c}/tu"], gold[f"{c}/ts"], eps=eps, dv_tol=dvt, bal_tol=bt,
+                                 matcher=OracleSectionMatcher())
+    _check(res, meta, gold, c)
