@@ -36,6 +36,7 @@ HG_TUNE_SEG_STEPS = 3
 HG_TUNE_SPREAD = 4
 HG_TUNE_LANES_D42 = 5
 HG_TUNE_SM_CAPACITY = 6
+HG_TUNE_REFINE_POOL_MB = 7
 
 
 class HitenGpuError(RuntimeError):

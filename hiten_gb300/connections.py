@@ -10,7 +10,6 @@ a set) run on the GPU (``hg_radius_best``, ``hg_nearest_neighbor``); the
 per-pair refinement is the reference's scalar arithmetic on the host.
 """
 import ctypes as C
-import math
 from dataclasses import dataclass
 
 import numpy as np

@@ -19,6 +19,7 @@ struct hg_handle {
   int lanes_d6 = 0;         // lanes per 6-dim DOP853 trajectory: 0 auto, 1, 2, 6
   int lanes_d42 = 0;        // lanes per 42-dim trajectory (fixed RK and DOP853): 0 auto, 7, 14
   int sm_capacity_x10 = 30;  // warps' FP64 demand an SM serves at full speed, x10 (layout cost models)
+  long long refine_pool_max = 8LL << 30;  // largest record pool a single-pass call allocates (bytes)
   int seg_steps = 16;       // attempted steps per segment of the scheduled DOP853 driver
   int spread = 0;           // 1: DOP853 blocks of 4 warps, one block per SM (one warp per sub-partition)
   int smem_per_sm = 0;      // bytes of shared memory per SM
@@ -557,7 +558,9 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
                               status, p);
   if (rc != HG_OK || N == 0) return rc;
   cudaStream_t s = (cudaStream_t)stream;
-  if (defer_refine(p)) {
+  // crossings are refined after the integration through a record pool, or
+  // inline (same bits) when the pool would exceed refine_pool_max
+  if (defer_refine(p) && refine_area_bytes(N, dim, p.max_hits) <= h->refine_pool_max) {
     int e = ensure_scratch(h, refine_area_bytes(N, dim, p.max_hits));
     if (e != HG_OK) return e;
     refine_area_carve(N, p.max_hits, h->scratch, p);
@@ -710,6 +713,10 @@ int hg_set_tuning(hg_handle* h, int key, int value) {
         return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 1, 2 or 6");
       h->lanes_d6 = value;
       return HG_OK;
+    case HG_TUNE_REFINE_POOL_MB:
+      if (value < 0) return fail(h, HG_ERR_ARGS, "pool size must be >= 0 MB");
+      h->refine_pool_max = (long long)value << 20;
+      return HG_OK;
     case HG_TUNE_SM_CAPACITY:
       if (value < 5 || value > 640) return fail(h, HG_ERR_ARGS, "capacity (tenths of warps per SM) must be in [5, 640]");
       h->sm_capacity_x10 = value;
@@ -746,6 +753,7 @@ int hg_get_tuning(hg_handle* h, int key, int* value) {
   else if (key == HG_TUNE_SPREAD) *value = h->spread;
   else if (key == HG_TUNE_LANES_D42) *value = h->lanes_d42;
   else if (key == HG_TUNE_SM_CAPACITY) *value = h->sm_capacity_x10;
+  else if (key == HG_TUNE_REFINE_POOL_MB) *value = (int)(h->refine_pool_max >> 20);
   else return fail(h, HG_ERR_ARGS, "unknown tuning key %d", key);
   return HG_OK;
 }

@@ -11,7 +11,6 @@ x = 1 - mu plane, section planes); they run on the GPU inside the integrator.
 from dataclasses import dataclass
 
 import numpy as np
-import torch
 
 from . import propagate as P
 

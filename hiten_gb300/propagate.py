@@ -251,21 +251,24 @@ class tuning:
     steps per segment of the scheduled driver, ``spread`` one 4-warp block
     per SM for DOP853, ``lanes_d42`` in {0 (auto), 7, 14} lanes per 42-dim
     trajectory, ``sm_capacity`` the warps an SM serves at full speed in the
-    layout cost models (a float, default 3.0).  Usable as a context manager
+    layout cost models (a float, default 3.0), ``refine_pool_mb`` the largest
+    crossing-record pool of a single-pass call (larger ones refine inline).  Usable as a context manager
     (restores the previous values on exit) or as a plain call."""
 
     _KEYS = (("lanes_d6", _lib.HG_TUNE_DOP853_LANES_D6), ("block", _lib.HG_TUNE_BLOCK_THREADS),
              ("seg_steps", _lib.HG_TUNE_SEG_STEPS), ("spread", _lib.HG_TUNE_SPREAD),
-             ("lanes_d42", _lib.HG_TUNE_LANES_D42), ("sm_capacity", _lib.HG_TUNE_SM_CAPACITY))
+             ("lanes_d42", _lib.HG_TUNE_LANES_D42), ("sm_capacity", _lib.HG_TUNE_SM_CAPACITY),
+             ("refine_pool_mb", _lib.HG_TUNE_REFINE_POOL_MB))
 
     def __init__(self, lanes_d6=None, block=None, device=None, seg_steps=None, spread=None, lanes_d42=None,
-                 sm_capacity=None):
+                 sm_capacity=None, refine_pool_mb=None):
         dev = _device(device)
         self.H = _lib.handle(dev.index or 0)
         self.old = {k: self.H.get_tuning(key) for k, key in self._KEYS}
         new = {"lanes_d6": lanes_d6, "block": block, "seg_steps": seg_steps,
                "spread": None if spread is None else int(bool(spread)), "lanes_d42": lanes_d42,
-               "sm_capacity": None if sm_capacity is None else int(round(10 * sm_capacity))}
+               "sm_capacity": None if sm_capacity is None else int(round(10 * sm_capacity)),
+               "refine_pool_mb": refine_pool_mb}
         for k, key in self._KEYS:
             if new[k] is not None:
                 self.H.set_tuning(key, new[k])

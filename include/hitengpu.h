@@ -267,6 +267,10 @@ int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_ma
  * the per-step latency), 0 = automatic (the default).
  * HG_TUNE_SM_CAPACITY: the layout cost models' FP64 capacity of an SM, in
  * tenths of a warp's demand (default 30: three warps run at full speed).
+ * HG_TUNE_REFINE_POOL_MB: largest record pool (MB, default 8192) a single-pass
+ * DOP853 call allocates to refine its event crossings after the integration;
+ * larger requests (N x max_hits x (15 dim + 3) doubles) refine inline, with
+ * the same results.
  * HG_TUNE_SPREAD: 1 = DOP853 launches use blocks of four warps that each
  * occupy a whole SM (one warp per SM sub-partition); 0 = HG_TUNE_BLOCK_THREADS
  * blocks (default).
@@ -278,6 +282,7 @@ int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_ma
 #define HG_TUNE_SPREAD 4
 #define HG_TUNE_LANES_D42 5
 #define HG_TUNE_SM_CAPACITY 6
+#define HG_TUNE_REFINE_POOL_MB 7
 int hg_set_tuning(hg_handle* h, int key, int value);
 int hg_get_tuning(hg_handle* h, int key, int* value);
 

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from helpers import rowwise_rel, stm_state
+from helpers import rowwise_rel
 from hiten_gb300 import dynamics as D
 from hiten_gb300 import integrators as I
 from hiten_gb300 import workloads as W

@@ -189,3 +189,20 @@ def test_lane_refill_matches_oracle(gpu, shape, dev_oracle, scheduled):
     assert np.array_equal(_np(res.y_end)[idx], ref["y_end"])
     assert np.array_equal(_np(res.n_accept)[idx], ref["n_accept"])
     assert np.array_equal(_np(res.n_hits)[idx], ref["n_hits"])
+
+
+def test_inline_and_pooled_refinement_agree(gpu):
+    """A record pool over the size limit makes the single-pass call refine
+    crossings inline: the same bits as the pooled refinement."""
+    y0 = W.section_states(300, seed=21)
+    ev = gpu.EventSpec(index=1, offset=0.0, direction=-1, max_hits=6)
+    pooled = gpu.propagate_dop853(y0, 0.0, 20.0, MU, rtol=1e-11, atol=1e-11, event=ev, scheduled=False)
+    with gpu.tuning(refine_pool_mb=0):
+        inline = gpu.propagate_dop853(y0, 0.0, 20.0, MU, rtol=1e-11, atol=1e-11, event=ev, scheduled=False)
+    for f in ("y_end", "n_hits", "n_accept", "status"):
+        assert np.array_equal(_np(getattr(pooled, f)), _np(getattr(inline, f)))
+    n = _np(pooled.n_hits)
+    assert n.max() >= 2
+    for i, k in enumerate(n):
+        assert np.array_equal(_np(pooled.hit_t)[i, :k], _np(inline.hit_t)[i, :k])
+        assert np.array_equal(_np(pooled.hit_y)[i, :k], _np(inline.hit_y)[i, :k])
