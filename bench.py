@@ -267,9 +267,17 @@ def bench_correct(args):
         torch.cuda.synchronize()
         ts.append(time.perf_counter() - t0)
     s = statistics.median(ts)
+    tn = []
+    for _ in range(max(1, args.steps // 4)):
+        t0 = time.perf_counter()
+        nat = corrector.correct_halo_native(g, mu)
+        torch.cuda.synchronize()
+        tn.append(time.perf_counter() - t0)
     _line("halo correction, 2048 guesses (L1/L2, Az 0.01-0.4)", "orbits corrected/s", len(g) / s, "orbits/s",
           s * 1e3, {"orbits": len(g)}, converged=int((res.status == 0).sum()),
-          iterations_hist=np.bincount(res.iterations).tolist(), gpu_launches=res.launches)
+          iterations_hist=np.bincount(res.iterations).tolist(), gpu_launches=res.launches,
+          native_driver={"ms": statistics.median(tn) * 1e3, "converged": int((nat.status == 0).sum()),
+                         "same_iterations": bool(np.array_equal(nat.iterations, res.iterations))})
 
 
 def bench_serving(args):

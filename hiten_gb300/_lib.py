@@ -16,18 +16,20 @@ HG_STEP_UNDERFLOW = 2
 HG_NONFINITE = 3
 HG_NEWTON_DIVERGED = 4
 HG_EVENT_NOT_FOUND = 5
+HG_LINE_SEARCH_FAILED = 6
 HG_ERR_ARGS = 10
 HG_ERR_CUDA = 11
 HG_ERR_NO_DEVICE = 12
 
 STATUS_NAMES = {0: "OK", 1: "MAX_STEPS", 2: "STEP_UNDERFLOW", 3: "NONFINITE", 4: "NEWTON_DIVERGED",
-                5: "EVENT_NOT_FOUND", 10: "ERR_ARGS", 11: "ERR_CUDA", 12: "ERR_NO_DEVICE"}
+                5: "EVENT_NOT_FOUND", 6: "LINE_SEARCH_FAILED", 10: "ERR_ARGS", 11: "ERR_CUDA", 12: "ERR_NO_DEVICE"}
 
 EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg_propagate_fixed",
             "hg_propagate_dop853", "hg_probe_fp64_peak", "hg_propagate_dop853_noalloc", "hg_set_tuning",
             "hg_get_tuning", "hg_section_detect", "hg_trajectory_filters", "hg_propagate_fixed_event",
             "hg_dop853_segmented_workspace_bytes", "hg_propagate_dop853_segmented",
-            "hg_propagate_dop853_scheduled", "hg_get_counter", "hg_radius_best", "hg_nearest_neighbor")
+            "hg_propagate_dop853_scheduled", "hg_get_counter", "hg_radius_best", "hg_nearest_neighbor",
+            "hg_newton_opts_default", "hg_correct_halo")
 HG_COUNTER_KERNEL_LAUNCHES = 1
 HG_RUNNING = -1
 HG_TUNE_BLOCK_THREADS = 1
@@ -55,6 +57,13 @@ class hg_event(C.Structure):
 class hg_dop853_opts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("max_step", C.c_double), ("min_step", C.c_double),
                 ("max_steps", C.c_longlong), ("fwd", C.c_int), ("flip_lo", C.c_int), ("flip_hi", C.c_int)]
+
+
+class hg_newton_opts(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_attempts", C.c_int), ("max_delta", C.c_double),
+                ("alpha_reduction", C.c_double), ("min_alpha", C.c_double), ("armijo_c", C.c_double),
+                ("cond_threshold", C.c_double), ("event_rtol", C.c_double), ("event_atol", C.c_double),
+                ("stm_rtol", C.c_double), ("stm_atol", C.c_double), ("steps", C.c_int)]
 
 
 class hg_config(C.Structure):
@@ -122,6 +131,11 @@ def load(build_if_missing=True):
         L.hg_radius_best.restype = C.c_int
         L.hg_nearest_neighbor.argtypes = [C.c_int, _P, _P, C.c_double, _P, _P]
         L.hg_nearest_neighbor.restype = C.c_int
+        L.hg_newton_opts_default.argtypes = [C.POINTER(hg_newton_opts)]
+        L.hg_newton_opts_default.restype = None
+        L.hg_correct_halo.argtypes = [_P, C.c_double, C.c_int, _P, C.c_longlong, _P, _P, _P, _P,
+                                      C.POINTER(hg_newton_opts), _P]
+        L.hg_correct_halo.restype = C.c_int
         L.hg_get_counter.argtypes = [_P, C.c_int, C.POINTER(C.c_longlong)]
         L.hg_get_counter.restype = C.c_int
         L.hg_probe_fp64_peak.argtypes = [_P, C.POINTER(C.c_double)]

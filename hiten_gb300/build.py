@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libhitengpu.so")
 BUILD_DIR = os.path.join(HERE, "_build")
 SOURCES = [os.path.join(CSRC, "hg_api.cu"), os.path.join(CSRC, "hg_noalloc.cu"), os.path.join(CSRC, "hg_section.cu"),
-           os.path.join(CSRC, "hg_connect.cu")]
+           os.path.join(CSRC, "hg_connect.cu"), os.path.join(CSRC, "hg_correct.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("hg_kernels.cuh", "hg_crmath.cuh", "hg_crmath_tables.h",
                                                   "hg_tableaux.h")] + [os.path.join(REPO, "include", "hitengpu.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
@@ -43,7 +43,10 @@ def build(force=False, verbose=False):
     if not force and not stale():
         return LIB
     tmp = LIB + f".tmp{os.getpid()}"
+    # host code: no contraction and no builtin pow (the reference's numpy
+    # arithmetic); device code: --fmad=false
     flags = ["-std=c++20", ARCH, "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
+             "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fno-builtin-pow",
              "-I" + os.path.join(REPO, "include"), "-I" + CSRC]
     if verbose:
         flags.append("-Xptxas=-v")

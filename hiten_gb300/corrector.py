@@ -252,3 +252,39 @@ def correct_halo(guesses, mu, options=None, backend=None, device=None):
     x0[:, ctrl] = params
     return HaloCorrectionResult(x0=x0, half_period=tev_out, period=2.0 * tev_out, iterations=iters,
                                 residual_norm=rnorm_out, status=status, launches=getattr(be, "launches", 0))
+
+
+def correct_halo_native(guesses, mu, options=None, device=None):
+    """correct_halo through the library's native driver (``hg_correct_halo``):
+    the same batched Newton/Armijo loop on the host side of the C ABI, for
+    callers that bind the library without Python.  Returns a
+    HaloCorrectionResult (launches not counted)."""
+    import ctypes as C
+
+    import torch
+
+    from . import _lib
+    o = options or HaloCorrectionOptions()
+    dev = P._device(device)
+    g = np.atleast_2d(np.asarray(guesses, dtype=np.float64))
+    N = g.shape[0]
+    x = torch.as_tensor(g, device=dev).t().contiguous()
+    half = torch.empty(max(N, 1), dtype=torch.float64, device=dev)
+    resid = torch.empty(max(N, 1), dtype=torch.float64, device=dev)
+    iters = torch.empty(max(N, 1), dtype=torch.int32, device=dev)
+    status = torch.empty(max(N, 1), dtype=torch.int32, device=dev)
+    no = _lib.hg_newton_opts(o.tol, o.max_attempts, np.inf if o.max_delta is None else o.max_delta,
+                             o.alpha_reduction, o.min_alpha, o.armijo_c, o.cond_threshold, o.event_rtol,
+                             o.event_atol, o.stm_rtol, o.stm_atol, o.steps)
+    H = _lib.handle(dev.index or 0)
+    with torch.cuda.device(dev):
+        H.check(H.lib.hg_correct_halo(H.ptr, float(mu), N, P._ptr(x), max(N, 1), P._ptr(half), P._ptr(iters),
+                                      P._ptr(resid), P._ptr(status), C.byref(no),
+                                      C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
+    st = status[:N].cpu().numpy().astype(np.int32)
+    # the library's status codes are the corrector's: OK 0, max iterations 4,
+    # no crossing 5, line search 6
+    hp = half[:N].cpu().numpy()
+    return HaloCorrectionResult(x0=x[:, :N].t().cpu().numpy(), half_period=hp, period=2.0 * hp,
+                                iterations=iters[:N].cpu().numpy().astype(np.int64),
+                                residual_norm=resid[:N].cpu().numpy(), status=st, launches=0)

@@ -28,6 +28,7 @@ extern "C" {
 #define HG_NONFINITE 3      /* state became NaN/Inf */
 #define HG_NEWTON_DIVERGED 4
 #define HG_EVENT_NOT_FOUND 5
+#define HG_LINE_SEARCH_FAILED 6 /* per orbit: Armijo found no productive step */
 #define HG_ERR_ARGS 10      /* invalid argument (call status) */
 #define HG_ERR_CUDA 11      /* CUDA runtime error (call status) */
 #define HG_ERR_NO_DEVICE 12
@@ -236,6 +237,38 @@ int hg_section_detect(int N, int m, const double* samples, long long ld,
  * common/energy.py:26-74 (_max_rel_energy_error). */
 int hg_trajectory_filters(int N, int m, const double* samples, long long ld, double mu,
                           double* min_r1, double* min_r2, double* max_rel_energy, void* stream);
+
+/* Options of hg_correct_halo (defaults: hg_newton_opts_default; the values
+ * of types/services/orbits.py:851-915 and corrector/options). */
+typedef struct hg_newton_opts {
+  double tol;            /* stop when the residual inf-norm < tol (1e-12) */
+  int max_attempts;      /* Newton iterations (50) */
+  double max_delta;      /* inf-norm cap of a step (1e-2; inf: none) */
+  double alpha_reduction;/* Armijo backtracking factor (0.5) */
+  double min_alpha;      /* smallest step scale tried (1e-4) */
+  double armijo_c;       /* sufficient-decrease constant (0.1) */
+  double cond_threshold; /* Tikhonov 1e-12 above this condition number (1e8) */
+  double event_rtol, event_atol;  /* half-period crossing search (1e-12) */
+  double stm_rtol, stm_atol;      /* STM propagation (1e-12) */
+  int steps;             /* dense samples of the STM propagation (500; the last is used) */
+} hg_newton_opts;
+void hg_newton_opts_default(hg_newton_opts* o);
+
+/* Batched single-shooting correction of halo orbits: every orbit's controls
+ * (x0, vy0) are corrected so that vx and vz vanish at the first y = 0
+ * crossing; all orbits still iterating share each propagation launch.  x:
+ * device [6][ld] initial states, overwritten by the corrected ones;
+ * half_period, residual (final inf-norm), iterations, status (HG_OK,
+ * HG_NEWTON_DIVERGED, HG_EVENT_NOT_FOUND, HG_LINE_SEARCH_FAILED): device [N].
+ * Synchronous on `stream`; allocates its working buffers.  Host arithmetic
+ * follows the reference's numpy expressions; an exactly singular Jacobian
+ * (which the reference hands to lstsq) ends that orbit's line search.
+ * Replaces: corrector/backends/newton.py:39-143 with
+ * corrector/operators.py:408-452, types/services/orbits.py:851-948,
+ * corrector/backends/base.py:187-245, corrector/stepping/armijo.py:58-164
+ * (orbit.correct() for halo orbits). */
+int hg_correct_halo(hg_handle* h, double mu, int N, double* x, long long ld, double* half_period, int* iterations,
+                    double* residual, int* status, const hg_newton_opts* opts, void* stream);
 
 /* Section-point matching for connections (handle-free, asynchronous on
  * `stream`; point sets as two coordinate arrays each).
