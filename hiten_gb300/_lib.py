@@ -20,16 +20,19 @@ HG_LINE_SEARCH_FAILED = 6
 HG_ERR_ARGS = 10
 HG_ERR_CUDA = 11
 HG_ERR_NO_DEVICE = 12
+HG_ERR_TIMEOUT = 13
 
 STATUS_NAMES = {0: "OK", 1: "MAX_STEPS", 2: "STEP_UNDERFLOW", 3: "NONFINITE", 4: "NEWTON_DIVERGED",
-                5: "EVENT_NOT_FOUND", 6: "LINE_SEARCH_FAILED", 10: "ERR_ARGS", 11: "ERR_CUDA", 12: "ERR_NO_DEVICE"}
+                5: "EVENT_NOT_FOUND", 6: "LINE_SEARCH_FAILED", 10: "ERR_ARGS", 11: "ERR_CUDA", 12: "ERR_NO_DEVICE", 13: "ERR_TIMEOUT"}
 
 EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg_propagate_fixed",
             "hg_propagate_dop853", "hg_probe_fp64_peak", "hg_propagate_dop853_noalloc", "hg_set_tuning",
             "hg_get_tuning", "hg_section_detect", "hg_trajectory_filters", "hg_propagate_fixed_event",
             "hg_dop853_segmented_workspace_bytes", "hg_propagate_dop853_segmented",
             "hg_propagate_dop853_scheduled", "hg_get_counter", "hg_radius_best", "hg_nearest_neighbor",
-            "hg_newton_opts_default", "hg_correct_halo")
+            "hg_newton_opts_default", "hg_correct_halo", "hg_serve_config_default", "hg_serve_create",
+            "hg_serve_destroy", "hg_serve_submit", "hg_serve_poll", "hg_serve_wait", "hg_serve_fetch",
+            "hg_serve_cancel", "hg_serve_stats")
 HG_COUNTER_KERNEL_LAUNCHES = 1
 HG_RUNNING = -1
 HG_TUNE_BLOCK_THREADS = 1
@@ -64,6 +67,10 @@ class hg_newton_opts(C.Structure):
                 ("alpha_reduction", C.c_double), ("min_alpha", C.c_double), ("armijo_c", C.c_double),
                 ("cond_threshold", C.c_double), ("event_rtol", C.c_double), ("event_atol", C.c_double),
                 ("stm_rtol", C.c_double), ("stm_atol", C.c_double), ("steps", C.c_int)]
+
+
+class hg_serve_config(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_longlong), ("max_concurrent", C.c_int)]
 
 
 class hg_config(C.Structure):
@@ -136,6 +143,21 @@ def load(build_if_missing=True):
         L.hg_correct_halo.argtypes = [_P, C.c_double, C.c_int, _P, C.c_longlong, _P, _P, _P, _P,
                                       C.POINTER(hg_newton_opts), _P]
         L.hg_correct_halo.restype = C.c_int
+        L.hg_serve_config_default.argtypes = [C.POINTER(hg_serve_config)]
+        L.hg_serve_config_default.restype = None
+        L.hg_serve_create.argtypes = [C.POINTER(hg_serve_config), C.POINTER(_P)]
+        L.hg_serve_destroy.argtypes = [_P]
+        L.hg_serve_submit.argtypes = [_P, C.c_double, C.c_int, C.c_int, _P, C.c_double, C.c_double,
+                                      C.POINTER(hg_dop853_opts), C.POINTER(hg_event), C.POINTER(C.c_longlong)]
+        L.hg_serve_poll.argtypes = [_P, C.c_longlong, C.POINTER(C.c_int)]
+        L.hg_serve_wait.argtypes = [_P, C.c_longlong, C.c_double]
+        L.hg_serve_fetch.argtypes = [_P, C.c_longlong, _P, _P, _P, _P, _P, _P, _P, _P]
+        L.hg_serve_cancel.argtypes = [_P, C.c_longlong]
+        L.hg_serve_stats.argtypes = [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_longlong),
+                                     C.POINTER(C.c_longlong)]
+        for f in ("hg_serve_create", "hg_serve_destroy", "hg_serve_submit", "hg_serve_poll", "hg_serve_wait",
+                  "hg_serve_fetch", "hg_serve_cancel", "hg_serve_stats"):
+            getattr(L, f).restype = C.c_int
         L.hg_get_counter.argtypes = [_P, C.c_int, C.POINTER(C.c_longlong)]
         L.hg_get_counter.restype = C.c_int
         L.hg_probe_fp64_peak.argtypes = [_P, C.POINTER(C.c_double)]

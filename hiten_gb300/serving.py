@@ -227,3 +227,92 @@ def poisson_requests(rate_hz, duration_s, mu, seed=0, manifold_seeds=None, size_
         out.append(Request(rid=rid, kind=kind, payload=payload, arrival=t))
         rid += 1
     return out
+
+
+class NativeServer:
+    """The library's native request server (``hg_serve_*``): continuous
+    batching of DOP853 propagation requests behind the C ABI, for callers
+    that do not run this Python engine.  Requests with the same problem (mu,
+    dimension, span, options, event) are merged; results equal direct calls."""
+
+    def __init__(self, device=0, hbm_budget_bytes=8 << 30, max_concurrent=4):
+        import ctypes as C
+        from . import _lib
+        self._C, self._lib = C, _lib
+        self.L = _lib.load()
+        cfg = _lib.hg_serve_config(int(device), int(hbm_budget_bytes), int(max_concurrent))
+        self.ptr = C.c_void_p()
+        rc = self.L.hg_serve_create(C.byref(cfg), C.byref(self.ptr))
+        if rc != _lib.HG_OK:
+            raise _lib.HitenGpuError(rc, "hg_serve_create failed")
+        self.meta = {}
+
+    def _check(self, rc, what):
+        if rc != self._lib.HG_OK:
+            raise self._lib.HitenGpuError(rc, what)
+
+    def submit(self, y0, mu, t0, tmax, rtol=1e-12, atol=1e-12, max_step=1e4, min_step=None, max_steps=100_000,
+               fwd=1, flip=None, event=None):
+        C, _lib = self._C, self._lib
+        y = np.ascontiguousarray(np.atleast_2d(np.asarray(y0, dtype=np.float64)))
+        n, dim = y.shape
+        lo, hi = P._flip(dim, fwd, flip)
+        opts = _lib.hg_dop853_opts(float(rtol), float(atol), float(max_step),
+                                   float(10.0 * P.EPS if min_step is None else min_step), int(max_steps), int(fwd),
+                                   lo, hi)
+        ev = None
+        hits = 0
+        if event is not None:
+            hits = int(event.max_hits)
+            ev = _lib.hg_event(int(event.index), float(event.offset), int(event.direction), hits,
+                               float(event.xtol), float(event.gtol))
+        rid = C.c_longlong(0)
+        self._check(self.L.hg_serve_submit(self.ptr, float(mu), dim, n, y.ctypes.data_as(C.c_void_p), float(t0),
+                                           float(tmax), C.byref(opts), C.byref(ev) if ev is not None else None,
+                                           C.byref(rid)), "hg_serve_submit")
+        self.meta[rid.value] = (n, dim, hits)
+        return rid.value
+
+    def poll(self, rid):
+        st = self._C.c_int(0)
+        self._check(self.L.hg_serve_poll(self.ptr, int(rid), self._C.byref(st)), "hg_serve_poll")
+        return st.value
+
+    def wait(self, rid, timeout=120.0):
+        self._check(self.L.hg_serve_wait(self.ptr, int(rid), float(timeout)), "hg_serve_wait")
+
+    def fetch(self, rid):
+        C = self._C
+        n, dim, hits = self.meta.pop(rid)
+        out = {"y_end": np.empty((n, dim)), "t_end": np.empty(n), "n_accept": np.empty(n, np.int32),
+               "n_reject": np.empty(n, np.int32), "status": np.empty(n, np.int32)}
+        if hits:
+            out.update(hit_t=np.empty((n, hits)), hit_y=np.empty((n, hits, dim)), n_hits=np.empty(n, np.int32))
+        p = lambda k: out[k].ctypes.data_as(C.c_void_p) if k in out else None  # noqa: E731
+        self._check(self.L.hg_serve_fetch(self.ptr, int(rid), p("y_end"), p("t_end"), p("hit_t"), p("hit_y"),
+                                          p("n_hits"), p("n_accept"), p("n_reject"), p("status")), "hg_serve_fetch")
+        return out
+
+    def cancel(self, rid):
+        ok = self.L.hg_serve_cancel(self.ptr, int(rid)) == self._lib.HG_OK
+        if ok:
+            self.meta.pop(rid, None)
+        return ok
+
+    def stats(self):
+        C = self._C
+        p50, p99, n, b = C.c_double(0), C.c_double(0), C.c_longlong(0), C.c_longlong(0)
+        self._check(self.L.hg_serve_stats(self.ptr, C.byref(p50), C.byref(p99), C.byref(n), C.byref(b)),
+                    "hg_serve_stats")
+        return {"p50_ms": p50.value, "p99_ms": p99.value, "requests": n.value, "batches": b.value}
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.L.hg_serve_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

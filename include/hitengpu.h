@@ -32,6 +32,7 @@ extern "C" {
 #define HG_ERR_ARGS 10      /* invalid argument (call status) */
 #define HG_ERR_CUDA 11      /* CUDA runtime error (call status) */
 #define HG_ERR_NO_DEVICE 12
+#define HG_ERR_TIMEOUT 13   /* hg_serve_wait: the request did not finish in time */
 
 typedef struct hg_handle hg_handle;
 
@@ -269,6 +270,38 @@ void hg_newton_opts_default(hg_newton_opts* o);
  * (orbit.correct() for halo orbits). */
 int hg_correct_halo(hg_handle* h, double mu, int N, double* x, long long ld, double* half_period, int* iterations,
                     double* residual, int* status, const hg_newton_opts* opts, void* stream);
+
+/* Native request server (continuous batching of DOP853 propagation
+ * requests).  A worker thread merges every pending request that shares a
+ * problem (mu, dim, t0, tmax, options, event) into one batch, admits batches
+ * while their device footprint fits hbm_budget_bytes, runs up to
+ * max_concurrent batches at once on its own streams and handles (wide 6-dim
+ * batches as host-scheduled segments) and keeps each request's results on
+ * the host until fetched.  Results equal a direct hg_propagate_dop853 call
+ * on the request alone.  Requests: y0 host row-major (N, dim); results host
+ * row-major: y_end (N, dim), t_end (N), hit_t (N, max_hits), hit_y (N,
+ * max_hits, dim), n_hits / n_accept / n_reject / status (N); null outputs
+ * are skipped.  Poll states: 0 pending, 1 running, 2 done, 3 failed.
+ * Latency = submit to completion; hg_serve_stats reports its p50 / p99.
+ * Replaces: nothing in the reference (its solves are synchronous calls);
+ * the serving pattern of this library's Python engine behind the C ABI. */
+typedef struct hg_server hg_server;
+typedef struct hg_serve_config {
+  int device;
+  long long hbm_budget_bytes;
+  int max_concurrent;
+} hg_serve_config;
+void hg_serve_config_default(hg_serve_config* c);
+int hg_serve_create(const hg_serve_config* cfg, hg_server** out);
+int hg_serve_destroy(hg_server* s);
+int hg_serve_submit(hg_server* s, double mu, int dim, int N, const double* y0, double t0, double tmax,
+                    const hg_dop853_opts* opts, const hg_event* ev, long long* request_id);
+int hg_serve_poll(hg_server* s, long long request_id, int* state);
+int hg_serve_wait(hg_server* s, long long request_id, double timeout_s);
+int hg_serve_fetch(hg_server* s, long long request_id, double* y_end, double* t_end, double* hit_t,
+                   double* hit_y, int* n_hits, int* n_accept, int* n_reject, int* status);
+int hg_serve_cancel(hg_server* s, long long request_id);
+int hg_serve_stats(hg_server* s, double* p50_ms, double* p99_ms, long long* requests, long long* batches);
 
 /* Section-point matching for connections (handle-free, asynchronous on
  * `stream`; point sets as two coordinate arrays each).
