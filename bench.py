@@ -521,10 +521,13 @@ def main():
 
     if rank == 0:
         prof = os.path.join(HERE, "profiles", "traffic_dop853_manifold.json")
-        traffic = None
+        traffic, pipe = None, None
         if os.path.exists(prof):
             with open(prof) as f:
-                traffic = json.load(f).get("dram_bytes_per_launch")
+                rec = json.load(f)
+            traffic = rec.get("dram_bytes_per_launch")
+            pipe = {k: rec[k] for k in ("fp64_pipe_active", "fp64_issue_frac", "threads_per_instruction") if k in rec}
+            pipe["source"] = "ncu, dominant launch (profiles/dop853_manifold_16384.md)"
         achieved = flops / (kernel_ms * 1e-3) / 1e12
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
@@ -536,7 +539,8 @@ def main():
                                              "segment, 16384 live trajectories x 32 steps), ncu",
                             "peak_source": "measured: DFMA throughput probe (hg_probe_fp64_peak) on this GPU; "
                                            "MEASURED_PEAKS.json has no FP64 entry",
-                            "flops_per_attempted_step": FLOPS_PER_ATTEMPT_D6},
+                            "flops_per_attempted_step": FLOPS_PER_ATTEMPT_D6,
+                            "fp64_pipe": pipe},
                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
                "plan": {"chosen": autotune.plan_name(plan), "autotune_ms": plan_ms},
