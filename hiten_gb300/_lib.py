@@ -17,13 +17,14 @@ HG_NONFINITE = 3
 HG_NEWTON_DIVERGED = 4
 HG_EVENT_NOT_FOUND = 5
 HG_LINE_SEARCH_FAILED = 6
+HG_SYNC_TIMEOUT = 7
 HG_ERR_ARGS = 10
 HG_ERR_CUDA = 11
 HG_ERR_NO_DEVICE = 12
 HG_ERR_TIMEOUT = 13
 
 STATUS_NAMES = {0: "OK", 1: "MAX_STEPS", 2: "STEP_UNDERFLOW", 3: "NONFINITE", 4: "NEWTON_DIVERGED",
-                5: "EVENT_NOT_FOUND", 6: "LINE_SEARCH_FAILED", 10: "ERR_ARGS", 11: "ERR_CUDA", 12: "ERR_NO_DEVICE", 13: "ERR_TIMEOUT"}
+                5: "EVENT_NOT_FOUND", 6: "LINE_SEARCH_FAILED", 7: "SYNC_TIMEOUT", 10: "ERR_ARGS", 11: "ERR_CUDA", 12: "ERR_NO_DEVICE", 13: "ERR_TIMEOUT"}
 
 EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg_propagate_fixed",
             "hg_propagate_dop853", "hg_probe_fp64_peak", "hg_propagate_dop853_noalloc", "hg_set_tuning",

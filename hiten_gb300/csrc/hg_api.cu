@@ -9,6 +9,7 @@
 #include <new>
 
 #include "hg_kernels.cuh"
+#include "hg_pair.cuh"
 #include "hitengpu.h"
 
 struct hg_handle {
@@ -17,7 +18,7 @@ struct hg_handle {
   int* counters = nullptr;  // scratch: lane-refill counters
   int block = 32;           // threads per block (32, 64 or 128)
   int lanes_d6 = 0;         // lanes per 6-dim DOP853 trajectory: 0 auto, 1, 2, 6
-  int lanes_d42 = 0;        // lanes per 42-dim trajectory (fixed RK and DOP853): 0 auto, 7, 14
+  int lanes_d42 = 0;        // lanes per 42-dim trajectory: 0 auto, 7, 14, 12 (paired warps, fixed RK)
   int sm_capacity_x10 = 30;  // warps' FP64 demand an SM serves at full speed, x10 (layout cost models)
   long long refine_pool_max = 8LL << 30;  // largest record pool a single-pass call allocates (bytes)
   int seg_steps = 16;       // attempted steps per segment of the scheduled DOP853 driver
@@ -85,14 +86,41 @@ int launch_fixed(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
 // column per lane: half the stage work per lane, twice the warps).  Unless
 // fixed by tuning, the one with the least time per step, where a warp's step
 // takes lat(G) (G = 14: 0.65 of G = 7) while its SM holds at most three
-// warps' FP64 demand, beyond which warps share the SM's FP64 unit.
-int lanes_d42(const hg_handle* h, int n) {
-  if (h->lanes_d42 != 0) return h->lanes_d42;
+// warps' FP64 demand, beyond which warps share the SM's FP64 unit.  With
+// `pair` the paired-warp layout (12 lanes on two warps, five trajectories
+// per pair, lat 0.5) competes too.
+int lanes_d42(const hg_handle* h, int n, bool pair = false) {
+  if (h->lanes_d42 != 0) return (h->lanes_d42 == 12 && !pair) ? 7 : h->lanes_d42;
   const double cap = 0.1 * h->sm_capacity_x10 * h->sm_count;
   const double w7 = (double)((n + 3) / 4), w14 = (double)((n + 1) / 2);
+  const double wp = 2.0 * (double)((n + hg::kPairTraj - 1) / hg::kPairTraj);
   const double c7 = 1.0 * (w7 > cap ? w7 / cap : 1.0);
   const double c14 = 0.65 * (w14 > cap ? w14 / cap : 1.0);
+  const double cp = 0.5 * (wp > cap ? wp / cap : 1.0);
+  if (pair && cp < c7 && cp < c14) return 12;
   return c14 < c7 ? 14 : 7;
+}
+
+// Paired-warp fixed-step launch: blocks of two pairs (four warps, one per
+// sub-partition); while the blocks fit one per SM, each reserves more than
+// half of the SM's shared memory so that no two share an SM.
+template <int ORDER>
+int launch_fixed_pair(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
+  const int block = 128;
+  const int per_block = 2 * hg::kPairTraj;
+  const int grid = (p.N + per_block - 1) / per_block;
+  if (grid < 1) return HG_OK;
+  size_t smem = 0;
+  if (grid <= h->sm_count && h->smem_per_sm > 0) {
+    smem = (size_t)(h->smem_per_sm / 2 + 1024);
+    if (cudaFuncSetAttribute(hg::fixed_rk_pair_kernel<ORDER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess) {
+      cudaGetLastError();
+      smem = 0;
+    }
+  }
+  hg::fixed_rk_pair_kernel<ORDER><<<grid, block, smem, s>>>(p);
+  return check_launch(h, "fixed_rk_pair_kernel");
 }
 
 int fixed_common(hg_handle* h, double mu, int order, int dim, int N, const double* y0, long long ld_in,
@@ -127,7 +155,13 @@ int fixed_dispatch(hg_handle* h, int order, int dim, const hg::FixedParams& p, c
     if (order == 6) return launch_fixed<6, 1>(h, p, s);
     return launch_fixed<8, 1>(h, p, s);
   }
-  if (p.ev_index < 0 && lanes_d42(h, p.N) == 14) {
+  const int g42 = p.ev_index < 0 ? lanes_d42(h, p.N, true) : 7;
+  if (g42 == 12) {
+    if (order == 4) return launch_fixed_pair<4>(h, p, s);
+    if (order == 6) return launch_fixed_pair<6>(h, p, s);
+    return launch_fixed_pair<8>(h, p, s);
+  }
+  if (g42 == 14) {
     if (order == 4) return launch_fixed<4, 14>(h, p, s);
     if (order == 6) return launch_fixed<6, 14>(h, p, s);
     return launch_fixed<8, 14>(h, p, s);
@@ -722,7 +756,8 @@ int hg_set_tuning(hg_handle* h, int key, int value) {
       h->sm_capacity_x10 = value;
       return HG_OK;
     case HG_TUNE_LANES_D42:
-      if (value != 0 && value != 7 && value != 14) return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 7 or 14");
+      if (value != 0 && value != 7 && value != 14 && value != 12)
+        return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 7, 14 or 12 (paired warps)");
       h->lanes_d42 = value;
       return HG_OK;
     case HG_TUNE_SPREAD:

@@ -13,7 +13,8 @@
 //   * hg_pow15 / hg_pow25: x*sqrt(x) in double-double.  s = RN(sqrt(x)),
 //     the residual x - s^2 is exact (fma), sqrt(x) = s + (x - s^2)/(2s) to
 //     ~2^-104, and x*s is split exactly; total error ~2^-100 before the
-//     final rounding.
+//     final rounding.  (hg_pow15_25 on the device: the same split from a
+//     Goldschmidt square root, see there.)
 //   * hg_pow: exp(y * log(x)).  log by Tang's table method (F_j = 1+j/1024,
 //     log(1+v) series, v = (m-F)/F in double-double), exp by Tang's table
 //     method (2^(j/256) in double-double, Cody-Waite reduction with ln2/256
@@ -140,7 +141,41 @@ HG_HD double hg_pow15(double x) {
 }
 
 // Both x^1.5 and x^2.5 (shared square root).
+//
+// Device: the range test runs on the integer pipe (exponent field of x in
+// [625, 1421], i.e. 2^-398 <= x < 2^399, sign clear), and sqrt(x) as
+// g + e comes from Goldschmidt's coupled iteration (g -> sqrt(x),
+// h -> 1/(2 sqrt(x)); P. Markstein, "Software division and square root
+// using Goldschmidt's algorithms", 6th Conf. on Real Numbers and Computers,
+// 2004) seeded by the hardware reciprocal-square-root estimate (PTX
+// rsqrt.approx.f64, ~2^-22 relative): two iterations bring g and h to
+// rounding level, the residual d = x - g^2 (one fma) gives e = d h, and
+// x (g + e) is split exactly as on the host: ~2^-102 relative error before
+// the final rounding, 10 FP64 operations for the square root instead of a
+// correctly rounded sqrt plus a reciprocal square root.  Host: the
+// sqrt-based double-double of hg_pow15_dd.
 HG_HD void hg_pow15_25(double x, double& p15, double& p25) {
+#if defined(__CUDA_ARCH__)
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  if ((unsigned)(bits >> 52) - 625u > 796u) {
+    p15 = pow(x, 1.5);
+    p25 = pow(x, 2.5);
+    return;
+  }
+  double y0;
+  asm("rsqrt.approx.f64 %0, %1;" : "=d"(y0) : "d"(x));
+  double g = x * y0, h = 0.5 * y0;
+  double r = fma(-g, h, 0.5);
+  g = fma(g, r, g);
+  h = fma(h, r, h);
+  r = fma(-g, h, 0.5);
+  g = fma(g, r, g);
+  h = fma(h, r, h);
+  const double e = fma(-g, g, x) * h;
+  const double hi = x * g;
+  double lo = fma(x, g, -hi);
+  lo = fma(x, e, lo);
+#else
   if (!(x > 0.0) || !(x < 1e120) || x < 1e-120) {
     p15 = pow(x, 1.5);
     p25 = pow(x, 2.5);
@@ -148,11 +183,23 @@ HG_HD void hg_pow15_25(double x, double& p15, double& p25) {
   }
   double hi, lo;
   hg_pow15_dd(x, hi, lo);
+#endif
   p15 = hi + lo;
   const double h2 = x * hi;
   double l2 = fma(x, hi, -h2);
   l2 = fma(x, lo, l2);
   p25 = h2 + l2;
+  // The one family of hard cases the double-double cannot resolve:
+  // x = 2^(2q) (1 - 2^-53) (mantissa all ones, even biased exponent), where
+  // x^1.5 = 2^(3q) (1 - 1.5 u + 0.375 u^2 + ...) lies 0.375 u^2 (u = 2^-53)
+  // above a rounding midpoint.  Exactly: RN(x^1.5) = 2^(3q) (1 - u),
+  // RN(x^2.5) = 2^(5q) (1 - 2u).
+  const uint64_t b = hg_bits(x);
+  if ((b & 0x000FFFFFFFFFFFFFull) == 0x000FFFFFFFFFFFFFull && ((b >> 52) & 1u) == 0) {
+    const int q = ((int)(b >> 52) - 1022) / 2;
+    p15 = hg_from_bits(((uint64_t)(3 * q + 1022) << 52) | 0x000FFFFFFFFFFFFFull);
+    p25 = hg_from_bits(((uint64_t)(5 * q + 1022) << 52) | 0x000FFFFFFFFFFFFEull);
+  }
 }
 
 // log(x) as double-double, x > 0 finite.  Absolute error <~ 2^-85.

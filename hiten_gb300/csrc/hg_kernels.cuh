@@ -681,11 +681,99 @@ __device__ __forceinline__ bool finite_bits(double a) {
 // ---------------------------------------------------------------------------
 // Fixed-step RK kernels, integrators/rk.py:154-215 and :531-588
 // ---------------------------------------------------------------------------
-template <int ORDER, int G>
-__device__ __forceinline__ void rk_fixed_step(const Layout<G>& L, const double (&y)[Layout<G>::NC], double h,
-                                              double mu, const Dir& dir, double (&yn)[Layout<G>::NC]) {
+// The products h * a_ij and h * b_j of one fixed step, formed where they
+// are used (every lane of a trajectory forms all of them).
+template <int ORDER>
+struct InlineCoef {
+  double h;
+  template <int I, int J>
+  __device__ __forceinline__ double a() const {
+    return h * FixedTab<ORDER>::a(I, J);
+  }
+  template <int J>
+  __device__ __forceinline__ double b() const {
+    return h * FixedTab<ORDER>::b(J);
+  }
+};
+
+// Position of a_ij (i >= 1, j < i, nonzero) in the list of the tableau's
+// nonzero A entries by rows, followed by the nonzero B entries (b_j at
+// fixed_flat(S, j)); -1 for a zero entry.
+template <int ORDER>
+__host__ __device__ constexpr int fixed_flat(int i, int j) {
   using T = FixedTab<ORDER>;
-  constexpr int NC = Layout<G>::NC;
+  int q = 0;
+  for (int r = 1; r < T::S; ++r)
+    for (int c = 0; c < r; ++c) {
+      if (T::a(r, c) != 0.0) {
+        if (r == i && c == j) return q;
+        ++q;
+      }
+    }
+  for (int c = 0; c < T::S; ++c) {
+    if (T::b(c) != 0.0) {
+      if (i == T::S && c == j) return q;
+      ++q;
+    }
+  }
+  return -1;
+}
+
+// The same products spread over a warp whose lanes all step with the same h
+// (fixed-step runs): lane l forms the products of list positions l, l + 32
+// and l + 64 (three FP64 multiplies per step instead of one per entry) and
+// each stage fetches its coefficients by shuffle.  Bit-identical: every
+// product is the same h * a.  All 32 lanes must be present.
+template <int ORDER>
+struct WarpCoef {
+  static_assert(fixed_flat<ORDER>(FixedTab<ORDER>::S, FixedTab<ORDER>::S) < 0, "");
+  double base[3];  // this lane's tableau entries
+  double v[3];     // this lane's products for the current step
+  __device__ __forceinline__ explicit WarpCoef(int lane) {
+    using T = FixedTab<ORDER>;
+    base[0] = base[1] = base[2] = 0.0;
+    static_for<T::S>([&](auto ic) {
+      constexpr int i = decltype(ic)::value;
+      static_for<i>([&](auto jc) {
+        constexpr int j = decltype(jc)::value;
+        if constexpr (T::a(i, j) != 0.0) {
+          constexpr int q = fixed_flat<ORDER>(i, j);
+          static_assert(q >= 0 && q < 96, "");
+          if (lane == q % 32) base[q / 32] = T::a(i, j);
+        }
+      });
+    });
+    static_for<T::S>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      if constexpr (T::b(j) != 0.0) {
+        constexpr int q = fixed_flat<ORDER>(T::S, j);
+        static_assert(q >= 0 && q < 96, "");
+        if (lane == q % 32) base[q / 32] = T::b(j);
+      }
+    });
+  }
+  __device__ __forceinline__ void set_step(double h) {
+    v[0] = h * base[0];
+    v[1] = h * base[1];
+    v[2] = h * base[2];
+  }
+  template <int I, int J>
+  __device__ __forceinline__ double a() const {
+    constexpr int q = fixed_flat<ORDER>(I, J);
+    return __shfl_sync(0xFFFFFFFFu, v[q / 32], q % 32);
+  }
+  template <int J>
+  __device__ __forceinline__ double b() const {
+    constexpr int q = fixed_flat<ORDER>(FixedTab<ORDER>::S, J);
+    return __shfl_sync(0xFFFFFFFFu, v[q / 32], q % 32);
+  }
+};
+
+template <int ORDER, class LT, class CF>
+__device__ __forceinline__ void rk_fixed_step(const LT& L, const double (&y)[LT::NC], const CF& cf, double mu,
+                                              const Dir& dir, double (&yn)[LT::NC]) {
+  using T = FixedTab<ORDER>;
+  constexpr int NC = LT::NC;
   double k[T::S][NC];
   L.rhs(y, mu, dir, k[0]);
   static_for<T::S - 1>([&](auto ic) {
@@ -695,9 +783,8 @@ __device__ __forceinline__ void rk_fixed_step(const Layout<G>& L, const double (
     for (int d = 0; d < NC; ++d) ys[d] = y[d];
     static_for<i>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
-      constexpr double a = T::a(i, j);
-      if constexpr (a != 0.0) {
-        const double c = h * a;
+      if constexpr (T::a(i, j) != 0.0) {
+        const double c = cf.template a<i, j>();
 #pragma unroll
         for (int d = 0; d < NC; ++d) ys[d] = ys[d] + c * k[j][d];
       }
@@ -708,13 +795,18 @@ __device__ __forceinline__ void rk_fixed_step(const Layout<G>& L, const double (
   for (int d = 0; d < NC; ++d) yn[d] = y[d];
   static_for<T::S>([&](auto jc) {
     constexpr int j = decltype(jc)::value;
-    constexpr double b = T::b(j);
-    if constexpr (b != 0.0) {
-      const double c = h * b;
+    if constexpr (T::b(j) != 0.0) {
+      const double c = cf.template b<j>();
 #pragma unroll
       for (int d = 0; d < NC; ++d) yn[d] = yn[d] + c * k[j][d];
     }
   });
+}
+
+template <int ORDER, class LT>
+__device__ __forceinline__ void rk_fixed_step(const LT& L, const double (&y)[LT::NC], double h, double mu,
+                                              const Dir& dir, double (&yn)[LT::NC]) {
+  rk_fixed_step<ORDER>(L, y, InlineCoef<ORDER>{h}, mu, dir, yn);
 }
 
 struct FixedParams {
@@ -802,7 +894,7 @@ __global__ void __launch_bounds__(128) fixed_rk_event_kernel(FixedParams p) {
     const double t_n = p.t_vals[idx];
     const double h = p.t_vals[idx + 1] - t_n;
     double yn[6], f_new[6];
-    rk_fixed_step<ORDER, G>(L, y, h, p.mu, p.dir, yn);
+    rk_fixed_step<ORDER>(L, y, h, p.mu, p.dir, yn);
     L.rhs(yn, p.mu, p.dir, f_new);
     const double g_new = bcast(ev_mine ? (pick<6>(yn, ev_r) - p.ev_offset) : 0.0);
     if (event_crossed(g_prev, g_new, p.ev_dir)) {
@@ -888,7 +980,7 @@ __global__ void __launch_bounds__(128) fixed_rk_kernel(FixedParams p) {
   for (int idx = 0; idx < p.n - 1; ++idx) {
     const double h = p.t_vals[idx + 1] - p.t_vals[idx];
     double yn[NC];
-    rk_fixed_step<ORDER, G>(L, y, h, p.mu, p.dir, yn);
+    rk_fixed_step<ORDER>(L, y, h, p.mu, p.dir, yn);
 #pragma unroll
     for (int r = 0; r < NC; ++r) {
       y[r] = yn[r];

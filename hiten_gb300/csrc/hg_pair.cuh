@@ -1,0 +1,287 @@
+// Paired-warp layout for the 42-dim variational system (fixed-step RK).
+//
+// Why.  On GB300 an FP64 warp instruction holds its SM sub-partition's FP64
+// pipe for ~64 cycles whatever the number of active lanes, so one warp's
+// step costs (its FP64 instructions) x ~64 cycles.  A batch of about a
+// thousand 42-dim trajectories fills fewer warps than the GPU has
+// sub-partitions, and its time is the per-warp instruction count of a step.
+// The state of a trajectory (6 components, the Hessian of the potential and
+// the accelerations) and its STM (36 components, F(x) Phi) are two
+// instruction streams of about the same length; run on two warps of one
+// block, on two sub-partitions, they halve that count.
+//
+// Layout.  A trajectory group is five trajectories served by two warps:
+//   * the state warp: lane 6t + j (t < 5, j < 6) holds state component 36 + j
+//     of trajectory t and does job j of the shared Hessian (hessian_split);
+//     lanes 30 and 31 shadow group 4 (they repeat job 0 and write nothing);
+//   * the STM warp: lane 6t + c holds column c of Phi (components 6r + c,
+//     r = 0..5); lanes 30 and 31 shadow column 5 of trajectory 4.
+// At every right-hand-side evaluation the state warp forms the Hessian from
+// its stage state and hands the six entries of each trajectory to the STM
+// warp through shared memory (a ring of kPairSlots slots; an mbarrier pair
+// per slot, "full" after the state warp wrote it, "empty" after the STM warp
+// read it), while the STM warp forms its stage columns.  The step's
+// coefficients h * a_ij are spread over the lanes (WarpCoef).  Every operation and operand is the
+// one the 7-lane layout uses (Layout<7>), so the results are bit-identical.
+//
+// Waits are bounded: a hand-off that has not completed within
+// kPairWaitNs of wall time marks the warp broken; it stops waiting and
+// arriving, the partner's waits run out in turn, both leave the step loop
+// and the group's trajectories report HG_SYNC_TIMEOUT.
+#pragma once
+
+#include "hg_kernels.cuh"
+
+namespace hg {
+
+constexpr unsigned long long kPairWaitNs = 2000000000ull;  // 2 s per hand-off
+constexpr int kPairTraj = 5;                                // trajectories per warp pair
+constexpr unsigned kPairSlots = 4;                          // hand-off ring depth
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  [[maybe_unused]] unsigned long long state;
+  asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred P;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, P;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for the completion of the phase with the given parity; false when it
+// has not completed within kPairWaitNs (or 2^30 polls).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  if (mbar_test(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (unsigned it = 1; it < (1u << 30); ++it) {
+    if (mbar_test(bar, parity)) return true;
+    if ((it & 63u) == 0 && global_ns() - t0 > kPairWaitNs) return false;
+  }
+  return false;
+}
+
+// Shared-memory hand-off of one warp pair.
+struct PairLink {
+  double H[kPairSlots][kPairTraj][6];  // slot, trajectory, (xx, yy, zz, xy, xz, yz)
+  unsigned long long full[kPairSlots];
+  unsigned long long empty[kPairSlots];
+  int fin[kPairTraj];     // STM columns finite, per trajectory
+  int broken;             // STM warp gave up a wait
+};
+
+// Lane placement shared by both warps of a pair.
+struct PairLane {
+  int t;           // trajectory in the group (0..4)
+  int role;        // 0..5; 6 and 7 on the shadow lanes 30, 31
+  int base;        // first lane of the trajectory
+  unsigned gmask;  // lanes of the trajectory (group 4 includes the shadows)
+  __device__ __forceinline__ explicit PairLane(int lane) {
+    t = lane < 30 ? lane / 6 : 4;
+    role = lane < 30 ? lane % 6 : lane - 24;
+    base = 6 * t;
+    gmask = t < 4 ? (0x3Fu << base) : 0xFF000000u;
+  }
+};
+
+// State warp: one state component per lane (NC = 1).
+struct PairState {
+  static constexpr int D = 42;
+  static constexpr int NC = 1;
+  int role, base, t;
+  unsigned gmask;
+  PairLink* link;
+  mutable unsigned seq;  // right-hand-side evaluations so far
+  mutable bool broken;
+  __device__ __forceinline__ int comp(int) const { return 36 + (role < 6 ? role : 0); }
+  __device__ __forceinline__ double from(double v, int r) const { return __shfl_sync(gmask, v, base + r); }
+  __device__ __forceinline__ void rhs(const double (&v)[1], double mu, const Dir& dir, double (&dv)[1]) const {
+    const double x = from(v[0], 0), y = from(v[0], 1), z = from(v[0], 2);
+    const double vx = from(v[0], 3), vy = from(v[0], 4);
+    // position lanes: their derivative is the velocity of lane role + 3
+    const double u = from(v[0], role < 3 ? role + 3 : 0);
+    const Hess H = hessian_split(*this, role < 6 ? role : 0, x, y, z, vx, vy, mu);
+    const unsigned b = seq % kPairSlots, use = seq / kPairSlots;
+    if (!broken && use >= 1) {
+      // the slot's previous contents must have been read (warp-uniform verdict)
+      const bool ok = mbar_wait(&link->empty[b], (use - 1u) & 1u);
+      broken = !__all_sync(0xFFFFFFFFu, ok);
+    }
+    if (!broken) {
+      if (role < 6) {
+        const double e = role == 0   ? H.xx
+                         : role == 1 ? H.yy
+                         : role == 2 ? H.zz
+                         : role == 3 ? H.xy
+                         : role == 4 ? H.xz
+                                     : H.yz;
+        link->H[b][t][role] = e;
+      }
+      mbar_arrive(&link->full[b]);
+    }
+    ++seq;
+    const double d = role < 3 ? u : (role == 3 ? H.ax : (role == 4 ? H.ay : H.az));
+    const int c = comp(0);
+    dv[0] = neg_if(d, c >= dir.neg_lo && c < dir.neg_hi);
+  }
+};
+
+// STM warp: one column of Phi per lane (NC = 6, rows 0..5).
+struct PairStm {
+  static constexpr int D = 42;
+  static constexpr int NC = 6;
+  int col, t;
+  PairLink* link;
+  mutable unsigned seq;
+  mutable bool broken;
+  __device__ __forceinline__ int comp(int r) const { return 6 * r + col; }
+  __device__ __forceinline__ void rhs(const double (&v)[6], double mu, const Dir& dir, double (&dv)[6]) const {
+    (void)mu;
+    const unsigned b = seq % kPairSlots;
+    double xx = 0.0, yy = 0.0, zz = 0.0, xy = 0.0, xz = 0.0, yz = 0.0;
+    if (!broken) {
+      const bool ok = mbar_wait(&link->full[b], (seq / kPairSlots) & 1u);
+      broken = !__all_sync(0xFFFFFFFFu, ok);
+    }
+    if (!broken) {
+      const double* e = link->H[b][t];
+      xx = e[0];
+      yy = e[1];
+      zz = e[2];
+      xy = e[3];
+      xz = e[4];
+      yz = e[5];
+      mbar_arrive(&link->empty[b]);
+    }
+    ++seq;
+    // rows of F(x) @ Phi[:, col] (dynamics/rtbp.py:204-209), as Layout<7>
+    dv[0] = v[3];
+    dv[1] = v[4];
+    dv[2] = v[5];
+    dv[3] = ((xx * v[0] + xy * v[1]) + xz * v[2]) + 2.0 * v[4];
+    dv[4] = ((xy * v[0] + yy * v[1]) + yz * v[2]) + (-2.0) * v[3];
+    dv[5] = (xz * v[0] + yz * v[1]) + zz * v[2];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      const int c = comp(r);
+      dv[r] = neg_if(dv[r], c >= dir.neg_lo && c < dir.neg_hi);
+    }
+  }
+};
+
+// One warp's part of a fixed-step propagation (rk.py:531-588): loads its
+// components, steps through the nodes, writes rows 0, out_every, ...
+// Returns whether its components stayed finite.
+template <int ORDER, class LT>
+__device__ __forceinline__ bool pair_fixed_run(const LT& L, const FixedParams& p, int traj, bool writes) {
+  constexpr int NC = LT::NC;
+  double y[NC];
+#pragma unroll
+  for (int r = 0; r < NC; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld_in + traj];
+  if (writes) {
+#pragma unroll
+    for (int r = 0; r < NC; ++r) p.out[(long long)L.comp(r) * p.ld_out + traj] = y[r];
+  }
+  const long long row = 42LL * p.ld_out;
+  bool finite = true;
+  WarpCoef<ORDER> cf(threadIdx.x & 31);
+  for (int idx = 0; idx < p.n - 1; ++idx) {
+    const double h = p.t_vals[idx + 1] - p.t_vals[idx];
+    cf.set_step(h);
+    double yn[NC];
+    rk_fixed_step<ORDER>(L, y, cf, p.mu, p.dir, yn);
+#pragma unroll
+    for (int r = 0; r < NC; ++r) {
+      y[r] = yn[r];
+      finite = finite && finite_bits(yn[r]);
+    }
+    if (writes && (idx + 1) % p.out_every == 0) {
+      double* o = p.out + (long long)((idx + 1) / p.out_every) * row;
+#pragma unroll
+      for (int r = 0; r < NC; ++r) o[(long long)L.comp(r) * p.ld_out + traj] = y[r];
+    }
+    if (L.broken) break;
+  }
+  return finite;
+}
+
+// Blocks of 2P warps (P = blockDim.x / 64 pairs): warps 0..P-1 are the state
+// warps of pairs 0..P-1, warps P..2P-1 their STM warps, so each warp of a
+// four-warp block lands on its own sub-partition.
+template <int ORDER>
+__global__ void __launch_bounds__(128) fixed_rk_pair_kernel(FixedParams p) {
+  __shared__ PairLink links[2];
+  const int w = threadIdx.x >> 5;
+  const int npairs = blockDim.x >> 6;
+  const int pair = w % npairs;
+  const bool stm = w >= npairs;
+  const int lane = threadIdx.x & 31;
+  PairLink* lk = &links[pair];
+  if (threadIdx.x < npairs * (int)kPairSlots) {
+    PairLink* l = &links[threadIdx.x / kPairSlots];
+    const int s = threadIdx.x % kPairSlots;
+    mbar_init(&l->full[s], 32);
+    mbar_init(&l->empty[s], 32);
+    if (s == 0) l->broken = 0;
+  }
+  __syncthreads();
+  const PairLane pl(lane);
+  const int group = blockIdx.x * npairs + pair;
+  const bool active = group * kPairTraj < p.N;  // uniform over the pair's two warps
+  const int traj = group * kPairTraj + pl.t;
+  const bool valid = active && traj < p.N;
+  const int tc = valid ? traj : (active ? p.N - 1 : 0);
+  bool finite = true, broken = false;
+  if (active) {
+    if (!stm) {
+      PairState L;
+      L.role = pl.role;
+      L.base = pl.base;
+      L.t = pl.t;
+      L.gmask = pl.gmask;
+      L.link = lk;
+      L.seq = 0;
+      L.broken = false;
+      finite = pair_fixed_run<ORDER>(L, p, tc, valid && pl.role < 6);
+      broken = L.broken;
+      finite = __all_sync(pl.gmask, finite);
+    } else {
+      PairStm L;
+      L.col = pl.role < 6 ? pl.role : 5;
+      L.t = pl.t;
+      L.link = lk;
+      L.seq = 0;
+      L.broken = false;
+      finite = pair_fixed_run<ORDER>(L, p, tc, valid && pl.role < 6);
+      broken = L.broken;
+      finite = __all_sync(pl.gmask, finite);
+      if (pl.role == 0) lk->fin[pl.t] = finite ? 1 : 0;
+      if (broken && lane == 0) lk->broken = 1;
+    }
+  }
+  __syncthreads();
+  if (!stm && valid && pl.role == 0 && p.status) {
+    const bool all_fin = finite && lk->fin[pl.t] != 0;
+    p.status[traj] = (broken || lk->broken) ? HG_SYNC_TIMEOUT : (all_fin ? HG_OK : HG_NONFINITE);
+  }
+}
+
+}  // namespace hg

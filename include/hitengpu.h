@@ -29,6 +29,7 @@ extern "C" {
 #define HG_NEWTON_DIVERGED 4
 #define HG_EVENT_NOT_FOUND 5
 #define HG_LINE_SEARCH_FAILED 6 /* per orbit: Armijo found no productive step */
+#define HG_SYNC_TIMEOUT 7   /* per trajectory: a hand-off between the warps of a paired layout timed out */
 #define HG_ERR_ARGS 10      /* invalid argument (call status) */
 #define HG_ERR_CUDA 11      /* CUDA runtime error (call status) */
 #define HG_ERR_NO_DEVICE 12
@@ -330,7 +331,10 @@ int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_ma
  * hg_propagate_dop853_scheduled (default 16).
  * HG_TUNE_LANES_D42: lanes per 42-dim trajectory (fixed RK without an event
  * and DOP853): 7 (an STM column per lane), 14 (half a column per lane: 0.65x
- * the per-step latency), 0 = automatic (the default).
+ * the per-step latency), 12 (paired warps, fixed RK without an event only:
+ * a state warp with the Hessian and an STM warp per five trajectories,
+ * ~0.5x the per-step latency of 7; DOP853 then uses 7), 0 = automatic (the
+ * default).
  * HG_TUNE_SM_CAPACITY: the layout cost models' FP64 capacity of an SM, in
  * tenths of a warp's demand (default 30: three warps run at full speed).
  * HG_TUNE_REFINE_POOL_MB: largest record pool (MB, default 8192) a single-pass

@@ -3,6 +3,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <stdint.h>
+#include <string.h>
 #include "hg_crmath.cuh"
 #if defined(__aarch64__)
 typedef long double q_t;
@@ -32,6 +33,22 @@ int main(int argc, char** argv) {
     const double xe = pow(10.0, -30.0 + 33.0 * urand());
     const double y = ys[i & 3];
     if (hg_pow(xe, y) != (double)QPOW((q_t)xe, (q_t)y)) ++badp;
+  }
+  // binade edges over a wide exponent range: mantissas just below the next
+  // power of two (the hard cases of x^1.5 near a rounding midpoint) and
+  // just above a power of two
+  for (long i = 0; i < n; ++i) {
+    const uint64_t r = (uint64_t)(urand() * 9007199254740992.0);
+    const int mode = (int)(i % 2);
+    const uint64_t mant = mode == 0 ? 0x000FFFFFFFFFFFFFull - (r & 0xFF) : (r & 0xFF);
+    const uint64_t e = 1023 + (r >> 8) % 601 - 300;
+    const uint64_t bits = (e << 52) | mant;
+    double x;
+    memcpy(&x, &bits, 8);
+    double a, b;
+    hg_pow15_25(x, a, b);
+    if (a != (double)QPOW((q_t)x, (q_t)1.5)) ++bad15;
+    if (b != (double)QPOW((q_t)x, (q_t)2.5)) ++bad25;
   }
   printf("%ld %ld %ld %ld\n", n, bad15, bad25, badp);
   return 0;

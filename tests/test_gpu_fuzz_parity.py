@@ -81,7 +81,7 @@ def test_fuzz_fixed_rk_bitexact(gpu, dev_oracle, case):
     out_every = int(rng.integers(1, 50))
     fwd = int(rng.choice([1, -1]))
     flip = (36, 42) if dim == 42 else (0, 6)
-    with gpu.tuning(lanes_d42=int(rng.choice([7, 14])), block=int(rng.choice([32, 64, 128]))):
+    with gpu.tuning(lanes_d42=int(rng.choice([7, 14, 12])), block=int(rng.choice([32, 64, 128]))):
         out = _np(gpu.propagate_fixed(y0, t, MU, order=order, out_every=out_every, fwd=fwd, flip=flip))
     ref, st = dev_oracle.fixed_rk_batch(order, y0, t, MU, out_every=out_every, fwd=fwd, flip=flip)
     assert st == 0

@@ -1,0 +1,75 @@
+"""Paired-warp 42-dim layout (a state warp with the shared Hessian and an STM
+warp per five trajectories, shared-memory hand-off per stage): bit-identical
+to the CPU oracle and to the single-warp layouts, for every order, ragged
+batch sizes, both launch shapes (one block per SM while the blocks fit, plain
+blocks beyond) and every flip range, including the STM components."""
+import numpy as np
+import pytest
+
+from hiten_gb300 import _lib
+from hiten_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+MU = W.MU_EM
+
+
+@pytest.fixture(scope="module")
+def dev_oracle(oracle):
+    oracle.set_mode(oracle.MODE_DEVICE)
+    yield oracle
+    oracle.set_mode(oracle.MODE_PYTHON)
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("order", [4, 6, 8])
+@pytest.mark.parametrize("n", [1, 7, 10, 23])
+@pytest.mark.parametrize("fwd,flip", [(1, None), (-1, (36, 42)), (-1, (0, 42)), (-1, (30, 40))])
+def test_pair_fixed_matches_oracle(gpu, dev_oracle, order, n, fwd, flip):
+    y0 = W.stm_fixed_batch(64, seed=3)[:n]
+    t = np.linspace(0.0, 0.8, 121)
+    with gpu.tuning(lanes_d42=12):
+        out, st = gpu.propagate_fixed(y0, t, MU, order=order, out_every=7, fwd=fwd, flip=flip, return_status=True)
+    ref, rst = dev_oracle.fixed_rk_batch(order, y0, t, MU, out_every=7, fwd=fwd, flip=flip)
+    assert rst == 0
+    assert np.all(_np(st) == _lib.HG_OK)
+    assert np.array_equal(_np(out), ref.transpose(1, 0, 2))
+
+
+def test_pair_many_blocks_equals_single_warp_layouts(gpu, dev_oracle):
+    # 2003 trajectories: 201 blocks of two pairs, more than one per SM, so
+    # the launch runs without the one-block-per-SM reservation; the last
+    # block is ragged (three trajectories in its first pair, none in its second)
+    y0 = W.stm_fixed_batch(2003, seed=5)
+    t = np.linspace(0.0, 0.5, 51)
+    outs = {}
+    for lanes in (12, 7, 14):
+        with gpu.tuning(lanes_d42=lanes):
+            outs[lanes] = _np(gpu.propagate_fixed(y0, t, MU, order=8, out_every=5))
+    assert np.array_equal(outs[12], outs[7])
+    assert np.array_equal(outs[12], outs[14])
+    idx = np.array([0, 4, 5, 999, 2000, 2002])
+    ref, rst = dev_oracle.fixed_rk_batch(8, y0[idx], t, MU, out_every=5)
+    assert rst == 0
+    assert np.array_equal(outs[12][:, idx], ref.transpose(1, 0, 2))
+
+
+def test_pair_nonfinite_status_per_trajectory(gpu):
+    # trajectory 6 starts on the first primary (r1 = 0): its state and STM turn
+    # non-finite; its neighbours in the same pair are unaffected
+    y0 = W.stm_fixed_batch(64, seed=7)[:12].copy()
+    y0[6, 36:] = [-MU, 0.0, 0.0, 0.0, 0.0, 0.0]
+    t = np.linspace(0.0, 0.2, 21)
+    res = {}
+    for lanes in (12, 7):
+        with gpu.tuning(lanes_d42=lanes):
+            out, st = gpu.propagate_fixed(y0, t, MU, order=8, out_every=4, return_status=True)
+        res[lanes] = (_np(out), _np(st))
+    st = res[12][1]
+    assert st[6] == _lib.HG_NONFINITE
+    assert np.all(np.delete(st, 6) == _lib.HG_OK)
+    assert np.array_equal(res[12][1], res[7][1])
+    ok = np.delete(np.arange(12), 6)
+    assert np.array_equal(res[12][0][:, ok], res[7][0][:, ok])

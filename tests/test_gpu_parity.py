@@ -16,9 +16,10 @@ MU = W.MU_EM
 
 
 @pytest.fixture(params=[(1, 32, 0, 7), (2, 32, 0, 14), (1, 128, 0, 14), (2, 64, 0, 7), (6, 32, 0, 14),
-                        (6, 128, 0, 7), (1, 32, 1, 14), (6, 32, 1, 7)],
+                        (6, 128, 0, 7), (1, 32, 1, 14), (6, 32, 1, 7), (2, 32, 0, 12)],
                 ids=["lanes1-b32-d42x7", "lanes2-b32-d42x14", "lanes1-b128-d42x14", "lanes2-b64-d42x7",
-                     "lanes6-b32-d42x14", "lanes6-b128-d42x7", "lanes1-spread-d42x14", "lanes6-spread-d42x7"])
+                     "lanes6-b32-d42x14", "lanes6-b128-d42x7", "lanes1-spread-d42x14", "lanes6-spread-d42x7",
+                     "lanes2-b32-d42pair"])
 def shape(request, gpu):
     """Every launch shape must give the same bits (6-dim lanes, block, spread,
     42-dim lanes)."""
@@ -54,7 +55,7 @@ def test_fixed_matches_oracle_bitexact(gpu, shape, dev_oracle, order, dim):
     assert np.array_equal(out, ref.transpose(1, 0, 2))
 
 
-@pytest.mark.parametrize("lanes42", [7, 14])
+@pytest.mark.parametrize("lanes42", [7, 14, 12])
 def test_fixed_rk8_stm_config_rows_bitexact(gpu, dev_oracle, lanes42):
     """The 42-dim RK8 workload (t in [0,3], 3000 steps, every 100th state) on 16 states."""
     y0 = W.stm_fixed_batch(1024, seed=0)[:16]
