@@ -1,5 +1,6 @@
 // Standalone FP64 pipe probe (not part of the library): DFMA throughput with 32/8/1 active lanes
-// per warp at 4..32 warps/SM, and DMUL, sqrt, IEEE division and __drcp_rn rates.  Bounded loops,
+// per warp at 4..32 warps/SM, DMUL, sqrt, IEEE division and __drcp_rn rates, and the cycles per warp
+// instruction of 1..8 dependent chains per thread at one warp per SM sub-partition.  Bounded loops,
 // writes only out[0].  Build: nvcc -gencode arch=compute_103a,code=sm_103a -O3 -o probe fp64_pipe_probe.cu
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -50,6 +51,35 @@ __global__ void k_rcp(double* out, int iters) {
   double s = 0; for (int i = 0; i < 8; ++i) s += x[i];
   if (s == 1.2345) out[0] = s;
 }
+// K independent dependent chains per thread, one warp per SM sub-partition
+// (blocks of four warps, one block per SM through shared memory); cycles
+// per warp instruction from clock64 of block 0.  MUL: dmul then dadd.
+template <int K, bool MUL>
+__global__ void k_chains(double* out, int iters, double a, double b, long long* cyc) {
+  extern __shared__ double pad[];
+  double x[K];
+  for (int i = 0; i < K; ++i) x[i] = threadIdx.x * 1e-9 + i + 1.0;
+  const long long t0 = clock64();
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int i = 0; i < K; ++i) x[i] = MUL ? x[i] * a + b : fma(x[i], a, b);
+  const long long t1 = clock64();
+  double s = 0;
+  for (int i = 0; i < K; ++i) s += x[i];
+  if (s == 1.2345) out[0] = s + pad[0];
+  if (threadIdx.x == 0 && blockIdx.x == 0) cyc[0] = t1 - t0;
+}
+template <int K, bool MUL>
+void chains(double* out, long long* cyc, int sms, int smem_sm) {
+  const int iters = 4096;
+  const size_t smem = smem_sm / 2 + 1024;
+  cudaFuncSetAttribute(k_chains<K, MUL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  for (int r = 0; r < 2; ++r) k_chains<K, MUL><<<sms, 128, smem>>>(out, iters, 0.999999, 1e-7, cyc);
+  long long c = 0;
+  cudaMemcpy(&c, cyc, 8, cudaMemcpyDeviceToHost);
+  printf("%s chains %d: %.1f cycles per warp instruction\n", MUL ? "dmul+dadd" : "dfma", K,
+         (double)c / iters / K / (MUL ? 2 : 1));
+}
 int main() {
   int sms; cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
   int clk; cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, 0);
@@ -81,6 +111,17 @@ int main() {
   cudaEventElapsedTime(&ms, a, b); printf("div+add: %.3e lane-op/s\n", 8.0 * iters / 8 * threads * blocks / (ms * 1e-3));
   cudaEventRecord(a); k_rcp<<<blocks, threads>>>(out, iters / 8); cudaEventRecord(b); cudaEventSynchronize(b);
   cudaEventElapsedTime(&ms, a, b); printf("rcp+add: %.3e lane-op/s\n", 8.0 * iters / 8 * threads * blocks / (ms * 1e-3));
+  int smem_sm = 0;
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, 0);
+  long long* cyc;
+  cudaMalloc(&cyc, 64);
+  chains<1, false>(out, cyc, sms, smem_sm);
+  chains<2, false>(out, cyc, sms, smem_sm);
+  chains<4, false>(out, cyc, sms, smem_sm);
+  chains<8, false>(out, cyc, sms, smem_sm);
+  chains<1, true>(out, cyc, sms, smem_sm);
+  chains<2, true>(out, cyc, sms, smem_sm);
+  chains<4, true>(out, cyc, sms, smem_sm);
   printf("err: %s\n", cudaGetErrorString(cudaGetLastError()));
   return 0;
 }

@@ -88,7 +88,8 @@ int launch_fixed(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
 // takes lat(G) (G = 14: 0.65 of G = 7) while its SM holds at most three
 // warps' FP64 demand, beyond which warps share the SM's FP64 unit.  With
 // `pair` the paired-warp layout (12 lanes on two warps, five trajectories
-// per pair, lat 0.5) competes too.
+// per pair, lat 0.6: RK8 on GB300, 125 ms against 214 ms for G = 7 over 3000
+// steps of 512 states) competes too.
 int lanes_d42(const hg_handle* h, int n, bool pair = false) {
   if (h->lanes_d42 != 0) return (h->lanes_d42 == 12 && !pair) ? 7 : h->lanes_d42;
   const double cap = 0.1 * h->sm_capacity_x10 * h->sm_count;
@@ -96,22 +97,23 @@ int lanes_d42(const hg_handle* h, int n, bool pair = false) {
   const double wp = 2.0 * (double)((n + hg::kPairTraj - 1) / hg::kPairTraj);
   const double c7 = 1.0 * (w7 > cap ? w7 / cap : 1.0);
   const double c14 = 0.65 * (w14 > cap ? w14 / cap : 1.0);
-  const double cp = 0.5 * (wp > cap ? wp / cap : 1.0);
+  const double cp = 0.6 * (wp > cap ? wp / cap : 1.0);
   if (pair && cp < c7 && cp < c14) return 12;
   return c14 < c7 ? 14 : 7;
 }
 
 // Paired-warp fixed-step launch: blocks of two pairs (four warps, one per
-// sub-partition); while the blocks fit one per SM, each reserves more than
-// half of the SM's shared memory so that no two share an SM.
+// sub-partition; HG_TUNE_BLOCK_THREADS 128) or of one pair (64: the pairs
+// spread over more SMs); while four-warp blocks fit one per SM, each reserves
+// more than half of the SM's shared memory so that no two share an SM.
 template <int ORDER>
 int launch_fixed_pair(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
-  const int block = 128;
-  const int per_block = 2 * hg::kPairTraj;
+  const int block = h->block >= 128 ? 128 : 64;
+  const int per_block = (block / 64) * hg::kPairTraj;
   const int grid = (p.N + per_block - 1) / per_block;
   if (grid < 1) return HG_OK;
   size_t smem = 0;
-  if (grid <= h->sm_count && h->smem_per_sm > 0) {
+  if (block == 128 && grid <= h->sm_count && h->smem_per_sm > 0) {
     smem = (size_t)(h->smem_per_sm / 2 + 1024);
     if (cudaFuncSetAttribute(hg::fixed_rk_pair_kernel<ORDER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess) {

@@ -195,7 +195,10 @@ struct Layout<1> {
 // ((p + a u) + b w) + c whose operands reproduce hessian42's exactly
 // (x - m == x + (-m), (-a) u == -(a u), -0 + v == v), and those six are
 // exchanged again.  Same operations on the same operands: same bits.
-template <class LT>
+// With OFFDIAG = false the off-diagonal entries are left to the caller:
+// H.xy then carries sxy and H.yz carries qa + qb (H.xz is unset), from which
+// xy = (3y) sxy, xz = (3z) sxy, yz = ((3y) z)(qa + qb) as below.
+template <class LT, bool OFFDIAG = true>
 __device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, double y, double z, double vx, double vy,
                                             double mu) {
   const double mu2 = 1.0 - mu;
@@ -257,9 +260,15 @@ __device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, do
   H.ay = L.from(form, 4);
   H.az = L.from(form, 5);
   const double sxy = sxa + sxb;
-  H.xy = (3.0 * y) * sxy;
-  H.xz = (3.0 * z) * sxy;
-  H.yz = ((3.0 * y) * z) * (qa + qb);
+  if constexpr (OFFDIAG) {
+    H.xy = (3.0 * y) * sxy;
+    H.xz = (3.0 * z) * sxy;
+    H.yz = ((3.0 * y) * z) * (qa + qb);
+  } else {
+    H.xy = sxy;
+    H.xz = 0.0;
+    H.yz = qa + qb;
+  }
   return H;
 }
 

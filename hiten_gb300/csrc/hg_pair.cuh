@@ -16,9 +16,10 @@
 //     lanes 30 and 31 shadow group 4 (they repeat job 0 and write nothing);
 //   * the STM warp: lane 6t + c holds column c of Phi (components 6r + c,
 //     r = 0..5); lanes 30 and 31 shadow column 5 of trajectory 4.
-// At every right-hand-side evaluation the state warp forms the Hessian from
-// its stage state and hands the six entries of each trajectory to the STM
-// warp through shared memory (a ring of kPairSlots slots; an mbarrier pair
+// At every right-hand-side evaluation the state warp forms the Hessian's
+// diagonal from its stage state and hands it, with the two sums and the
+// stage's y and z the off-diagonal entries are products of, to the STM warp
+// (which forms those products) through shared memory (a ring of kPairSlots slots; an mbarrier pair
 // per slot, "full" after the state warp wrote it, "empty" after the STM warp
 // read it), while the STM warp forms its stage columns.  The step's
 // coefficients h * a_ij are spread over the lanes (WarpCoef).  Every operation and operand is the
@@ -81,7 +82,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 
 // Shared-memory hand-off of one warp pair.
 struct PairLink {
-  double H[kPairSlots][kPairTraj][6];  // slot, trajectory, (xx, yy, zz, xy, xz, yz)
+  double H[kPairSlots][kPairTraj][8];  // slot, trajectory, (xx, yy, zz, sxy, qa + qb, y, z, -)
   unsigned long long full[kPairSlots];
   unsigned long long empty[kPairSlots];
   int fin[kPairTraj];     // STM columns finite, per trajectory
@@ -118,7 +119,7 @@ struct PairState {
     const double vx = from(v[0], 3), vy = from(v[0], 4);
     // position lanes: their derivative is the velocity of lane role + 3
     const double u = from(v[0], role < 3 ? role + 3 : 0);
-    const Hess H = hessian_split(*this, role < 6 ? role : 0, x, y, z, vx, vy, mu);
+    const Hess H = hessian_split<PairState, false>(*this, role < 6 ? role : 0, x, y, z, vx, vy, mu);
     const unsigned b = seq % kPairSlots, use = seq / kPairSlots;
     if (!broken && use >= 1) {
       // the slot's previous contents must have been read (warp-uniform verdict)
@@ -127,13 +128,15 @@ struct PairState {
     }
     if (!broken) {
       if (role < 6) {
+        // xx, yy, zz, sxy, qa + qb; the sixth lane adds the stage's y and z
         const double e = role == 0   ? H.xx
                          : role == 1 ? H.yy
                          : role == 2 ? H.zz
                          : role == 3 ? H.xy
-                         : role == 4 ? H.xz
-                                     : H.yz;
+                         : role == 4 ? H.yz
+                                     : y;
         link->H[b][t][role] = e;
+        if (role == 5) link->H[b][t][6] = z;
       }
       mbar_arrive(&link->full[b]);
     }
@@ -166,10 +169,12 @@ struct PairStm {
       xx = e[0];
       yy = e[1];
       zz = e[2];
-      xy = e[3];
-      xz = e[4];
-      yz = e[5];
+      const double sxy = e[3], qab = e[4], y = e[5], z = e[6];
       mbar_arrive(&link->empty[b]);
+      // the off-diagonal entries, as hessian42 forms them
+      xy = (3.0 * y) * sxy;
+      xz = (3.0 * z) * sxy;
+      yz = ((3.0 * y) * z) * qab;
     }
     ++seq;
     // rows of F(x) @ Phi[:, col] (dynamics/rtbp.py:204-209), as Layout<7>

@@ -333,7 +333,8 @@ int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_ma
  * and DOP853): 7 (an STM column per lane), 14 (half a column per lane: 0.65x
  * the per-step latency), 12 (paired warps, fixed RK without an event only:
  * a state warp with the Hessian and an STM warp per five trajectories,
- * ~0.5x the per-step latency of 7; DOP853 then uses 7), 0 = automatic (the
+ * ~0.6x the per-step latency of 7; blocks of one pair, or of two pairs with
+ * HG_TUNE_BLOCK_THREADS 128; DOP853 then uses 7), 0 = automatic (the
  * default).
  * HG_TUNE_SM_CAPACITY: the layout cost models' FP64 capacity of an SM, in
  * tenths of a warp's demand (default 30: three warps run at full speed).
