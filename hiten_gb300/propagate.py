@@ -179,11 +179,13 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
     lo, hi = _flip(dim, fwd, flip)
     opts = _lib.hg_dop853_opts(float(rtol), float(atol), float(max_step), float(min_step), int(max_steps),
                                int(fwd), lo, hi)
+    # every entry of these is written by the kernels (per trajectory, at its
+    # end or pause); the hit arrays keep NaN where no crossing was found
     y_end = torch.empty((dim, ld), dtype=torch.float64, device=dev)
     t_end = torch.empty(ld, dtype=torch.float64, device=dev)
-    n_acc = torch.zeros(ld, dtype=torch.int32, device=dev)
-    n_rej = torch.zeros(ld, dtype=torch.int32, device=dev)
-    status = torch.zeros(ld, dtype=torch.int32, device=dev)
+    n_acc = torch.empty(ld, dtype=torch.int32, device=dev)
+    n_rej = torch.empty(ld, dtype=torch.int32, device=dev)
+    status = torch.empty(ld, dtype=torch.int32, device=dev)
     evp = None
     hit_t = hit_y = n_hits = None
     if event is not None:
@@ -192,7 +194,7 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
                             float(event.gtol))
         hit_t = torch.full((mh, ld), float("nan"), dtype=torch.float64, device=dev)
         hit_y = torch.full((mh, dim, ld), float("nan"), dtype=torch.float64, device=dev)
-        n_hits = torch.zeros(ld, dtype=torch.int32, device=dev)
+        n_hits = torch.empty(ld, dtype=torch.int32, device=dev)
     samples = None
     if n_samples:
         rows = 1 if sample_last_only else int(n_samples)
