@@ -90,16 +90,36 @@ int launch_fixed(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
 // `pair` the paired-warp layout (12 lanes on two warps, five trajectories
 // per pair, lat 0.6: RK8 on GB300, 125 ms against 214 ms for G = 7 over 3000
 // steps of 512 states) competes too.
-int lanes_d42(const hg_handle* h, int n, bool pair = false) {
+int lanes_d42(const hg_handle* h, int n, bool pair = false, double pair_lat = 0.0) {
   if (h->lanes_d42 != 0) return (h->lanes_d42 == 12 && !pair) ? 7 : h->lanes_d42;
   const double cap = 0.1 * h->sm_capacity_x10 * h->sm_count;
   const double w7 = (double)((n + 3) / 4), w14 = (double)((n + 1) / 2);
   const double wp = 2.0 * (double)((n + hg::kPairTraj - 1) / hg::kPairTraj);
   const double c7 = 1.0 * (w7 > cap ? w7 / cap : 1.0);
   const double c14 = 0.65 * (w14 > cap ? w14 / cap : 1.0);
-  const double cp = 0.6 * (wp > cap ? wp / cap : 1.0);
-  if (pair && cp < c7 && cp < c14) return 12;
+  const double cp = pair_lat * (wp > cap ? wp / cap : 1.0);
+  if (pair && pair_lat > 0.0 && cp < c7 && cp < c14) return 12;
   return c14 < c7 ? 14 : 7;
+}
+
+// Per-step latency of the paired-warp layout relative to G = 7 (0: not
+// chosen automatically).
+constexpr double kPairLatFixed = 0.6;
+// DOP853, no event, no per-step dense samples (STM legs of the corrector:
+// 2.72 ms against 2.93 (G = 7) and 3.50 (G = 14) for 2048 orbits; 1.92
+// against 1.98 / 2.53 for 512).  Runs sampling every step (one trajectory,
+// 2000 samples) are faster on G = 14 and never pick the pair.
+constexpr double kPairLatDop = 0.5;
+
+// Paired-warp DOP853 launch (42-dim, no event, single pass): blocks of one
+// pair (two with HG_TUNE_BLOCK_THREADS 128).
+int launch_dop853_pair(hg_handle* h, const hg::DopParams& p, cudaStream_t s) {
+  const int block = h->block >= 128 ? 128 : 64;
+  const int per_block = (block / 64) * hg::kPairTraj;
+  const int grid = (p.N + per_block - 1) / per_block;
+  if (grid < 1) return HG_OK;
+  hg::dop853_pair_kernel<<<grid, block, 0, s>>>(p);
+  return check_launch(h, "dop853_pair_kernel");
 }
 
 // Paired-warp fixed-step launch: blocks of two pairs (four warps, one per
@@ -157,7 +177,7 @@ int fixed_dispatch(hg_handle* h, int order, int dim, const hg::FixedParams& p, c
     if (order == 6) return launch_fixed<6, 1>(h, p, s);
     return launch_fixed<8, 1>(h, p, s);
   }
-  const int g42 = p.ev_index < 0 ? lanes_d42(h, p.N, true) : 7;
+  const int g42 = p.ev_index < 0 ? lanes_d42(h, p.N, true, kPairLatFixed) : 7;
   if (g42 == 12) {
     if (order == 4) return launch_fixed_pair<4>(h, p, s);
     if (order == 6) return launch_fixed_pair<6>(h, p, s);
@@ -269,7 +289,9 @@ Shape dop_shape(const hg_handle* h, K kernel) {
 template <int G>
 int launch_dop853(hg_handle* h, hg::DopParams p, cudaStream_t s) {
   if (p.N <= 0) return HG_OK;
-  const Shape sh = dop_shape(h, hg::dop853_kernel<G>);
+  // launches without dense samples run the kernel built without that path
+  auto kern = p.m >= 2 ? hg::dop853_kernel<G, true> : hg::dop853_kernel<G, false>;
+  const Shape sh = dop_shape(h, kern);
   const int kBlock = sh.block;
   const int per_sm = sh.per_sm;
   cudaError_t e;
@@ -284,7 +306,7 @@ int launch_dop853(hg_handle* h, hg::DopParams p, cudaStream_t s) {
     e = cudaMemsetAsync(h->counters, 0, sizeof(int), s);
     if (e != cudaSuccess) return fail(h, HG_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
   }
-  hg::dop853_kernel<G><<<grid, kBlock, sh.smem, s>>>(p);
+  kern<<<grid, kBlock, sh.smem, s>>>(p);
   return check_launch(h, "dop853_kernel");
 }
 
@@ -347,7 +369,8 @@ long long seg_ws_layout(int N, int D, int max_hits, char* base, SegWs* w) {
 // running are appended to list[a ^ 1].
 template <int G>
 int launch_segment(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_steps, int a, int n_live, cudaStream_t s) {
-  const Shape sh = dop_shape(h, hg::dop853_kernel<G>);
+  auto kern = p.m >= 2 ? hg::dop853_kernel<G, true> : hg::dop853_kernel<G, false>;
+  const Shape sh = dop_shape(h, kern);
   const int kBlock = sh.block;
   const int per_sm = sh.per_sm;
   const int tpb = (kBlock / 32) * hg::Layout<G>::TPW;
@@ -369,7 +392,7 @@ int launch_segment(hg_handle* h, hg::DopParams p, const SegWs& w, int seg_steps,
   p.n_in = w.count + a;
   p.active_out = w.list[b];
   p.n_out = w.count + b;
-  hg::dop853_kernel<G><<<grid, kBlock, sh.smem, s>>>(p);
+  kern<<<grid, kBlock, sh.smem, s>>>(p);
   return check_launch(h, "dop853_kernel (segment)");
 }
 
@@ -613,7 +636,12 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
     else
       rc2 = launch_dop853<1>(h, p, s);
   } else {
-    rc2 = lanes_d42(h, N) == 14 ? launch_dop853<14>(h, p, s) : launch_dop853<7>(h, p, s);
+    const bool per_step_samples = p.m >= 2 && !p.dense_last;
+    const int g = lanes_d42(h, N, p.ev_index < 0, per_step_samples ? 0.0 : kPairLatDop);
+    if (g == 12 && p.ev_index < 0)
+      rc2 = launch_dop853_pair(h, p, s);
+    else
+      rc2 = g == 14 ? launch_dop853<14>(h, p, s) : launch_dop853<7>(h, p, s);
   }
   if (rc2 != HG_OK) return rc2;
   return refine_pending(h, p, dim, s);

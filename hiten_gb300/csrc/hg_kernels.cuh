@@ -502,6 +502,42 @@ __device__ __forceinline__ double np_dot_self(const double* v) {
   }
 }
 
+// Both np_dot_self<42> of the 42-vectors va and vb (shared memory) over a
+// lane group of at least six lanes (L.role, L.base, L.gmask; role r acts as
+// r % 6).  The sixteen blocked terms a[k][m] = v[8k+m]^2 + v[8k+4+m]^2 of
+// each vector are spread over three lanes (va on roles 0..2, vb on 3..5),
+// gathered by shuffle, and the two reductions (blocked sums, then the fused
+// tail over components 32..41) run side by side on the two halves: the same
+// operations in the same order as np_dot_self<42>, ~43 FP64 instructions per
+// lane for both norms instead of ~146.
+template <class LT>
+__device__ __forceinline__ void dots42_group(const LT& L, const double* va, const double* vb, double& da, double& db) {
+  const int r = L.role % 6;
+  const bool second = r >= 3;
+  const double* v = second ? vb : va;
+  const int r3 = second ? r - 3 : r;
+  const int off = second ? 3 : 0;
+  double aj[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const int j = r3 + 3 * i;
+    const int jj = j < 16 ? j : 15;
+    const int b0 = 8 * (jj >> 2) + (jj & 3);
+    aj[i] = v[b0] * v[b0] + v[b0 + 4] * v[b0 + 4];
+  }
+  double a[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) a[j] = __shfl_sync(L.gmask, aj[j / 3], L.base + off + j % 3);
+  double sm[4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) sm[m] = ((a[m] + a[4 + m]) + a[8 + m]) + a[12 + m];
+  double dot = (sm[0] + sm[2]) + (sm[1] + sm[3]);
+#pragma unroll
+  for (int i = 32; i < 42; ++i) dot = fma(v[i], v[i], dot);
+  da = __shfl_sync(L.gmask, dot, L.base);
+  db = __shfl_sync(L.gmask, dot, L.base + 3);
+}
+
 // Squared 2-norm of the full D-vector whose 6 components per lane are v, in
 // the numpy dot order above.  G = 1: the vector is the lane's own registers;
 // G = 7: the group assembles it in a 42-double shared-memory slot.
@@ -515,28 +551,41 @@ struct Gather<1> {
     for (int i = 0; i < 6; ++i) s = fma(v[i], v[i], s);
     return s;
   }
+  __device__ __forceinline__ void dot2(const Layout<1>& L, const double (&a)[6], const double (&b)[6], double& da,
+                                       double& db) const {
+    da = dot(L, a);
+    db = dot(L, b);
+  }
 };
 template <>
 struct Gather<7> {
-  double* slot;  // 42 doubles in shared memory
-  __device__ __forceinline__ double dot(const Layout<7>& L, const double (&v)[6]) const {
+  double* slot;  // 84 doubles in shared memory (two 42-vectors)
+  __device__ __forceinline__ void dot2(const Layout<7>& L, const double (&a)[6], const double (&b)[6], double& da,
+                                       double& db) const {
     __syncwarp(L.gmask);
 #pragma unroll
-    for (int r = 0; r < 6; ++r) slot[L.comp(r)] = v[r];
+    for (int r = 0; r < 6; ++r) {
+      slot[L.comp(r)] = a[r];
+      slot[42 + L.comp(r)] = b[r];
+    }
     __syncwarp(L.gmask);
-    return np_dot_self<42>(slot);
+    dots42_group(L, slot, slot + 42, da, db);
   }
 };
 
 template <>
 struct Gather<14> {
-  double* slot;  // 42 doubles in shared memory
-  __device__ __forceinline__ double dot(const Layout<14>& L, const double (&v)[3]) const {
+  double* slot;  // 84 doubles in shared memory (two 42-vectors)
+  __device__ __forceinline__ void dot2(const Layout<14>& L, const double (&a)[3], const double (&b)[3], double& da,
+                                       double& db) const {
     __syncwarp(L.gmask);
 #pragma unroll
-    for (int r = 0; r < 3; ++r) slot[L.comp(r)] = v[r];
+    for (int r = 0; r < 3; ++r) {
+      slot[L.comp(r)] = a[r];
+      slot[42 + L.comp(r)] = b[r];
+    }
     __syncwarp(L.gmask);
-    return np_dot_self<42>(slot);
+    dots42_group(L, slot, slot + 42, da, db);
   }
 };
 
@@ -553,6 +602,11 @@ struct Gather<2> {
     for (int i = 0; i < 3; ++i) s = fma(v[i], v[i], s);
     return __shfl_sync(L.gmask, s, L.base + 1);
   }
+  __device__ __forceinline__ void dot2(const Layout<2>& L, const double (&a)[3], const double (&b)[3], double& da,
+                                       double& db) const {
+    da = dot(L, a);
+    db = dot(L, b);
+  }
 };
 
 template <>
@@ -567,6 +621,11 @@ struct Gather<6> {
       s = fma(c, c, s);
     }
     return s;
+  }
+  __device__ __forceinline__ void dot2(const Layout<6>& L, const double (&a)[1], const double (&b)[1], double& da,
+                                       double& db) const {
+    da = dot(L, a);
+    db = dot(L, b);
   }
 };
 
@@ -621,8 +680,8 @@ __device__ __forceinline__ double exp_scaled(double e, double Lh, double Ll) {
 // power is the correctly rounded one hg_pow gives.  Zero, NaN and
 // err >= 1e300 take no logarithm: their factors are the clamp bounds (a
 // rejected err >= 1e300 gives 0.9 * err^(-1/8) < 0.2).
-template <int G>
-__device__ __forceinline__ double pi_factor(const Layout<G>& L, bool accepted, double err, double err_prev,
+template <class LT>
+__device__ __forceinline__ double pi_factor(const LT& L, bool accepted, double err, double err_prev,
                                             double& prev_pow) {
   const double beta = 1.0 / (8.0 + 1.0);
   const double alpha = 0.4 * beta;
@@ -633,7 +692,7 @@ __device__ __forceinline__ double pi_factor(const Layout<G>& L, bool accepted, d
     double Lh, Ll;
     hg_log_dd(err, Lh, Ll);
     const double e1 = accepted ? -beta : -rexp;
-    if constexpr (G == 1) {
+    if constexpr (std::is_same_v<LT, Layout<1>>) {
       p1 = exp_scaled(e1, Lh, Ll);
       pa = exp_scaled(alpha, Lh, Ll);
     } else {
@@ -1079,12 +1138,12 @@ struct DopParams {
 
 #define HG_RUNNING (-1)
 
-template <int G>
-struct DopLane {
-  static constexpr int NC = Layout<G>::NC;
+template <class LT>
+struct DopLaneT {
+  static constexpr int NC = LT::NC;
   // one attempted DOP853 step; k[0] = f(t, y) on entry; k[12] = f(t+h, y_high)
   // on exit.
-  __device__ __forceinline__ static void step(const Layout<G>& L, const double (&y)[NC], double h, double mu,
+  __device__ __forceinline__ static void step(const LT& L, const double (&y)[NC], double h, double mu,
                                               const Dir& dir, double (&k)[13][NC], double (&yh)[NC],
                                               double (&e5)[NC], double (&e3)[NC]) {
     using T = DopTab;
@@ -1142,7 +1201,7 @@ struct DopLane {
   }
 
   // _dop853_build_dense_cache: F[0..6][6] for this lane's components.
-  __device__ __forceinline__ static void dense_cache(const Layout<G>& L, const double (&y_old)[NC],
+  __device__ __forceinline__ static void dense_cache(const LT& L, const double (&y_old)[NC],
                                                      const double (&y_new)[NC], double hseg, double mu,
                                                      const Dir& dir, const double (&k)[13][NC],
                                                      double (&F)[7][NC]) {
@@ -1222,6 +1281,9 @@ struct DopLane {
   }
 };
 
+template <int G>
+using DopLane = DopLaneT<Layout<G>>;
+
 // Lane -> (group, role) for one launch; false for the idle lanes of a warp.
 template <int G>
 __device__ __forceinline__ bool setup_layout(Layout<G>& L, Gather<G>& gat, double* sm_gather, int& traj) {
@@ -1250,7 +1312,7 @@ __device__ __forceinline__ bool setup_layout(Layout<G>& L, Gather<G>& gat, doubl
     L.base = g * 14;
     L.gmask = 0x3FFFu << L.base;
     traj = warp * 2 + g;
-    gat.slot = sm_gather + ((threadIdx.x >> 5) * 2 + g) * 42;
+    gat.slot = sm_gather + ((threadIdx.x >> 5) * 2 + g) * 84;
   } else {
     if (lane >= 28) return false;
     const int g = lane / 7;
@@ -1258,7 +1320,7 @@ __device__ __forceinline__ bool setup_layout(Layout<G>& L, Gather<G>& gat, doubl
     L.base = g * 7;
     L.gmask = 0x7Fu << L.base;
     traj = warp * 4 + g;
-    gat.slot = sm_gather + ((threadIdx.x >> 5) * 4 + g) * 42;
+    gat.slot = sm_gather + ((threadIdx.x >> 5) * 4 + g) * 84;
   }
   return true;
 }
@@ -1267,7 +1329,7 @@ __device__ __forceinline__ bool setup_layout(Layout<G>& L, Gather<G>& gat, doubl
 // norm (one 42-double slot per lane group).
 template <int G>
 __host__ __device__ constexpr int gather_smem_doubles() {
-  return G == 7 ? 4 * 4 * 42 : (G == 14 ? 4 * 2 * 42 : 1);
+  return G == 7 ? 4 * 4 * 84 : (G == 14 ? 4 * 2 * 84 : 1);
 }
 
 template <int G>
@@ -1416,7 +1478,9 @@ __global__ void __launch_bounds__(128) refine_kernel(DopParams p) {
   }
 }
 
-template <int G>
+// DENSE = false compiles the dense-output path out (launches without
+// samples): fewer live registers in the step loop.
+template <int G, bool DENSE = true>
 __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
   constexpr int D = Layout<G>::D;
   constexpr int NC = Layout<G>::NC;
@@ -1455,7 +1519,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
     if (has_event) g_prev = ev.bcast(ev.mine ? (pick<NC>(y, ev.r) - p.ev_offset) : 0.0);
     double h, t, err_prev, prev_pow;
     int acc, rej, hits, q_next;
-    const bool dense = p.m >= 2;
+    const bool dense = DENSE && p.m >= 2;
     if (resume) {
       h = p.ws_h[traj];
       t = p.t_end[traj];
@@ -1474,8 +1538,10 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
         b[d] = k[0][d] / scale0;
       }
       const double sn = sqrt((double)D);
-      const double d0 = sqrt(gat.dot(L, a)) / sn;
-      const double d1 = sqrt(gat.dot(L, b)) / sn;
+      double na, nb;
+      gat.dot2(L, a, b, na, nb);
+      const double d0 = sqrt(na) / sn;
+      const double d1 = sqrt(nb) / sn;
       h = select_initial_step(d0, d1, p.min_step, p.max_step);
       t = t0;
       err_prev = -1.0;
@@ -1517,8 +1583,8 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
           s5[d] = hg_div_rn(e5[d], scale, is);
           s3[d] = hg_div_rn(e3[d], scale, is);
         }
-        const double n5 = gat.dot(L, s5);
-        const double n3 = gat.dot(L, s3);
+        double n5, n3;
+        gat.dot2(L, s5, s3, n5, n3);
         if (n5 == 0.0 && n3 == 0.0)
           err_norm = 0.0;
         else
@@ -1580,7 +1646,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
       } else {
         ++rej;
       }
-      h = h * pi_factor<G>(L, accepted, err_norm, err_prev, prev_pow);
+      h = h * pi_factor(L, accepted, err_norm, err_prev, prev_pow);
       if (accepted) {
         err_prev = err_norm;
         if constexpr (G > 1) fin = __all_sync(L.gmask, fin);

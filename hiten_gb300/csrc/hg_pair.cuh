@@ -107,6 +107,7 @@ struct PairLane {
 struct PairState {
   static constexpr int D = 42;
   static constexpr int NC = 1;
+  static constexpr bool kState = true;
   int role, base, t;
   unsigned gmask;
   PairLink* link;
@@ -151,7 +152,10 @@ struct PairState {
 struct PairStm {
   static constexpr int D = 42;
   static constexpr int NC = 6;
+  static constexpr bool kState = false;
   int col, t;
+  int role, base;  // lane placement (role 0..7, as in the state warp), for group-wide steps
+  unsigned gmask;
   PairLink* link;
   mutable unsigned seq;
   mutable bool broken;
@@ -272,6 +276,9 @@ __global__ void __launch_bounds__(128) fixed_rk_pair_kernel(FixedParams p) {
       PairStm L;
       L.col = pl.role < 6 ? pl.role : 5;
       L.t = pl.t;
+      L.role = pl.role;
+      L.base = pl.base;
+      L.gmask = pl.gmask;
       L.link = lk;
       L.seq = 0;
       L.broken = false;
@@ -287,6 +294,252 @@ __global__ void __launch_bounds__(128) fixed_rk_pair_kernel(FixedParams p) {
     const bool all_fin = finite && lk->fin[pl.t] != 0;
     p.status[traj] = (broken || lk->broken) ? HG_SYNC_TIMEOUT : (all_fin ? HG_OK : HG_NONFINITE);
   }
+}
+
+// ---------------------------------------------------------------------------
+// DOP853 on the paired warps (42-dim, single pass, no event; rk.py:2375-2549)
+// ---------------------------------------------------------------------------
+// Besides the Hessian hand-off, the step-size control needs norms over all
+// 42 components: both warps store their components of two vectors (and one
+// flag each) in a per-trajectory gather slot, meet at a two-warp barrier (an
+// mbarrier with 64 arrivals, two slots alternating by exchange), and every
+// lane then forms the same numpy-order dots -- so both warps take the same
+// accept / reject decisions, step sizes and dense-output samples.  Each warp
+// loops while any of its five trajectories is running; finished ones keep
+// computing on their frozen state without committing anything, so every
+// hand-off has all 32 lanes of both warps.
+struct PairGather {
+  double v[2][kPairTraj][2][44];  // slot, trajectory, vector, 42 components + the two warps' flags
+  unsigned long long bar[2];
+};
+
+template <class LT>
+__device__ __forceinline__ void pair_exchange(const LT& L, PairGather* gx, unsigned& gseq,
+                                              const double (&a)[LT::NC], const double (&b)[LT::NC],
+                                              double flag, double& dot_a, double& dot_b, double& flag_other) {
+  const unsigned sl = gseq & 1u;
+  double* va = gx->v[sl][L.t][0];
+  double* vb = gx->v[sl][L.t][1];
+  if (!L.broken) {
+    if (L.role < 6) {
+#pragma unroll
+      for (int r = 0; r < LT::NC; ++r) {
+        va[L.comp(r)] = a[r];
+        vb[L.comp(r)] = b[r];
+      }
+      if (L.role == 0) va[LT::kState ? 42 : 43] = flag;
+    }
+    mbar_arrive(&gx->bar[sl]);
+    const bool ok = mbar_wait(&gx->bar[sl], (gseq >> 1) & 1u);
+    L.broken = !__all_sync(0xFFFFFFFFu, ok);
+  }
+  ++gseq;
+  dots42_group(L, va, vb, dot_a, dot_b);
+  flag_other = va[LT::kState ? 43 : 42];
+}
+
+// One warp's part of the DOP853 propagation of its five trajectories.
+// Returns its broken flag.
+template <class LT>
+__device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, PairGather* gx, int traj, bool valid,
+                                             bool writes) {
+  constexpr int NC = LT::NC;
+  constexpr int D = 42;
+  const double t0 = p.t0_arr ? p.t0_arr[traj] : p.t0;
+  const double tmax = p.tmax_arr ? p.tmax_arr[traj] : p.tmax;
+  double y[NC];
+#pragma unroll
+  for (int r = 0; r < NC; ++r) y[r] = p.y0[(long long)L.comp(r) * p.ld + traj];
+  double k[13][NC];
+  L.rhs(y, p.mu, p.dir, k[0]);
+  unsigned gseq = 0;
+  double h;
+  {
+    double a[NC], b[NC];
+#pragma unroll
+    for (int d = 0; d < NC; ++d) {
+      const double scale0 = p.atol + p.rtol * fabs(y[d]);
+      a[d] = y[d] / scale0;
+      b[d] = k[0][d] / scale0;
+    }
+    double da, db, unused;
+    pair_exchange(L, gx, gseq, a, b, 0.0, da, db, unused);
+    const double sn = sqrt((double)D);
+    h = select_initial_step(sqrt(da) / sn, sqrt(db) / sn, p.min_step, p.max_step);
+  }
+  double t = t0, err_prev = -1.0, prev_pow = 0.0;
+  int acc = 0, rej = 0;
+  const bool dense = p.m >= 2;
+  int q_next = (dense && p.dense_last) ? p.m - 1 : 0;
+  int status = HG_OK;
+  bool running = valid;
+  double step_ls = 0.0;
+  if (dense) step_ls = (tmax - t0) / (double)(p.m - 1);
+  auto sample_t = [&](int q) -> double { return q == p.m - 1 ? tmax : (double)q * step_ls + t0; };
+  // integrators/rk.py loop test (t - t_end) * direction < 0, direction +1
+  bool live = running && (t - tmax < 0.0);
+  while (__any_sync(0xFFFFFFFFu, live)) {
+    bool go = live;
+    if (go && (long long)(acc + rej) >= p.max_steps) {
+      status = HG_MAX_STEPS;
+      running = false;
+      go = false;
+    }
+    double hh = h;
+    if (go) {
+      hh = clamp_step(hh, p.max_step, p.min_step);
+      hh = adjust_step_to_endpoint(t, hh, tmax);
+    }
+    double yh[NC], e5[NC], e3[NC];
+    DopLaneT<LT>::step(L, y, hh, p.mu, p.dir, k, yh, e5, e3);
+    double s5[NC], s3[NC];
+    bool fin = true;
+#pragma unroll
+    for (int d = 0; d < NC; ++d) {
+      const double scale = p.atol + p.rtol * np_maximum_abs(y[d], yh[d]);
+      const double is = hg_rcp_rn(scale);
+      s5[d] = hg_div_rn(e5[d], scale, is);
+      s3[d] = hg_div_rn(e3[d], scale, is);
+      fin = fin && finite_bits(yh[d]);
+    }
+    fin = __all_sync(L.gmask, fin);
+    double n5, n3, fin_other;
+    pair_exchange(L, gx, gseq, s5, s3, fin ? 1.0 : 0.0, n5, n3, fin_other);
+    fin = fin && fin_other != 0.0;
+    double err_norm;
+    if (n5 == 0.0 && n3 == 0.0)
+      err_norm = 0.0;
+    else
+      err_norm = (fabs(hh) * n5) / sqrt((n5 + 0.01 * n3) * (double)D);
+    const bool accepted = err_norm <= 1.0;
+    const double t_new = t + hh;
+    // dense samples inside (t, t_new] (reference: searchsorted on nodes);
+    // the cache's three extra evaluations run on the whole warp
+    bool need = false, last = false;
+    if (go && accepted && dense) {
+      last = !(t_new - tmax < 0.0);
+      need = q_next < p.m && (last || sample_t(q_next) < t_new);
+    }
+    if (__any_sync(0xFFFFFFFFu, need)) {
+      const double hseg = t_new - t;
+      double F[7][NC];
+      DopLaneT<LT>::dense_cache(L, y, yh, hseg, p.mu, p.dir, k, F);
+      if (need) {
+        while (q_next < p.m && (last || sample_t(q_next) < t_new)) {
+          const double x = (sample_t(q_next) - t) / hseg;
+          if (writes) {
+            double* o = p.y_out + (long long)(p.dense_last ? 0 : q_next) * D * p.ld;
+#pragma unroll
+            for (int d = 0; d < NC; ++d) o[(long long)L.comp(d) * p.ld + traj] = DopLaneT<LT>::eval1(y[d], F, d, x);
+          }
+          ++q_next;
+        }
+      }
+    }
+    if (go) {
+      if (accepted) {
+        ++acc;
+        t = t_new;
+#pragma unroll
+        for (int d = 0; d < NC; ++d) {
+          y[d] = yh[d];
+          k[0][d] = k[12][d];
+        }
+      } else {
+        ++rej;
+      }
+      h = hh * pi_factor(L, accepted, err_norm, err_prev, prev_pow);
+      if (accepted) {
+        err_prev = err_norm;
+        if (!fin) {
+          status = HG_NONFINITE;
+          running = false;
+        }
+      } else {
+        h = clamp_step(h, p.max_step, p.min_step);
+      }
+    }
+    live = running && (t - tmax < 0.0) && !L.broken;
+  }
+  if (valid && writes) {
+    // the reference's dense output falls back to the single stored node when
+    // no step was taken
+    if (dense) {
+      while (q_next < p.m) {
+        double* o = p.y_out + (long long)(p.dense_last ? 0 : q_next) * D * p.ld;
+#pragma unroll
+        for (int d = 0; d < NC; ++d) o[(long long)L.comp(d) * p.ld + traj] = y[d];
+        ++q_next;
+      }
+    }
+    if (p.y_end) {
+#pragma unroll
+      for (int d = 0; d < NC; ++d) p.y_end[(long long)L.comp(d) * p.ld + traj] = y[d];
+    }
+    if (LT::kState && L.role == 0) {
+      if (p.t_end) p.t_end[traj] = t;
+      if (p.n_accept) p.n_accept[traj] = acc;
+      if (p.n_reject) p.n_reject[traj] = rej;
+      if (p.status) p.status[traj] = status;
+    }
+  }
+  return L.broken;
+}
+
+// Blocks of one or two pairs, laid out as fixed_rk_pair_kernel's.
+__global__ void __launch_bounds__(128) dop853_pair_kernel(DopParams p) {
+  __shared__ PairLink links[2];
+  __shared__ PairGather gathers[2];
+  const int w = threadIdx.x >> 5;
+  const int npairs = blockDim.x >> 6;
+  const int pair = w % npairs;
+  const bool stm = w >= npairs;
+  const int lane = threadIdx.x & 31;
+  PairLink* lk = &links[pair];
+  PairGather* gx = &gathers[pair];
+  if (threadIdx.x < npairs * (int)kPairSlots) {
+    PairLink* l = &links[threadIdx.x / kPairSlots];
+    const int s = threadIdx.x % kPairSlots;
+    mbar_init(&l->full[s], 32);
+    mbar_init(&l->empty[s], 32);
+    if (s == 0) l->broken = 0;
+    if (s < 2) mbar_init(&gathers[threadIdx.x / kPairSlots].bar[s], 64);
+  }
+  __syncthreads();
+  const PairLane pl(lane);
+  const int group = blockIdx.x * npairs + pair;
+  const bool active = group * kPairTraj < p.N;  // uniform over the pair's two warps
+  const int traj = group * kPairTraj + pl.t;
+  const bool valid = active && traj < p.N;
+  const int tc = valid ? traj : (active ? p.N - 1 : 0);
+  bool broken = false;
+  if (active) {
+    if (!stm) {
+      PairState L;
+      L.role = pl.role;
+      L.base = pl.base;
+      L.t = pl.t;
+      L.gmask = pl.gmask;
+      L.link = lk;
+      L.seq = 0;
+      L.broken = false;
+      broken = pair_dop_run(L, p, gx, tc, valid, valid && pl.role < 6);
+    } else {
+      PairStm L;
+      L.col = pl.role < 6 ? pl.role : 5;
+      L.t = pl.t;
+      L.role = pl.role;
+      L.base = pl.base;
+      L.gmask = pl.gmask;
+      L.link = lk;
+      L.seq = 0;
+      L.broken = false;
+      broken = pair_dop_run(L, p, gx, tc, valid, valid && pl.role < 6);
+      if (broken && lane == 0) lk->broken = 1;
+    }
+  }
+  __syncthreads();
+  if (!stm && valid && pl.role == 0 && p.status && (broken || lk->broken)) p.status[traj] = HG_SYNC_TIMEOUT;
 }
 
 }  // namespace hg

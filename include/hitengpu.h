@@ -331,11 +331,11 @@ int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_ma
  * hg_propagate_dop853_scheduled (default 16).
  * HG_TUNE_LANES_D42: lanes per 42-dim trajectory (fixed RK without an event
  * and DOP853): 7 (an STM column per lane), 14 (half a column per lane: 0.65x
- * the per-step latency), 12 (paired warps, fixed RK without an event only:
- * a state warp with the Hessian and an STM warp per five trajectories,
- * ~0.6x the per-step latency of 7; blocks of one pair, or of two pairs with
- * HG_TUNE_BLOCK_THREADS 128; DOP853 then uses 7), 0 = automatic (the
- * default).
+ * the per-step latency), 12 (paired warps, fixed RK and single-pass DOP853
+ * without an event: a state warp with the Hessian and an STM warp per five
+ * trajectories, ~0.6x the per-step latency of 7 for RK8; blocks of one pair,
+ * or of two pairs with HG_TUNE_BLOCK_THREADS 128; other calls then use 7),
+ * 0 = automatic (the default).
  * HG_TUNE_SM_CAPACITY: the layout cost models' FP64 capacity of an SM, in
  * tenths of a warp's demand (default 30: three warps run at full speed).
  * HG_TUNE_REFINE_POOL_MB: largest record pool (MB, default 8192) a single-pass

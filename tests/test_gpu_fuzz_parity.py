@@ -97,7 +97,7 @@ def test_fuzz_dop853_dense_42_bitexact(gpu, dev_oracle, case):
     T = float(rng.uniform(0.3, 3.0))
     m = int(rng.integers(2, 60))
     fwd = int(rng.choice([1, -1]))
-    with gpu.tuning(lanes_d42=int(rng.choice([7, 14]))):
+    with gpu.tuning(lanes_d42=int(rng.choice([7, 14, 12]))):
         res = gpu.propagate_dop853(y0, 0.0, T, MU, rtol=tol, atol=tol, fwd=fwd, flip=(36, 42), n_samples=m)
     out = _np(res.samples)
     for i in range(n):

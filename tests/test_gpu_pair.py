@@ -73,3 +73,61 @@ def test_pair_nonfinite_status_per_trajectory(gpu):
     assert np.array_equal(res[12][1], res[7][1])
     ok = np.delete(np.arange(12), 6)
     assert np.array_equal(res[12][0][:, ok], res[7][0][:, ok])
+
+
+# ------------------------------------------------------------------ DOP853 (42-dim, paired warps)
+def _dop(gpu, lanes, y0, t0, tf, **kw):
+    with gpu.tuning(lanes_d42=lanes):
+        return gpu.propagate_dop853(y0, t0, tf, MU, flip=(36, 42) if kw.get("fwd", 1) == -1 else None, **kw)
+
+
+@pytest.mark.parametrize("n", [1, 6, 11])
+@pytest.mark.parametrize("fwd", [1, -1])
+@pytest.mark.parametrize("m,last", [(2, False), (37, False), (500, True)])
+def test_pair_dop853_dense_matches_oracle(gpu, dev_oracle, n, fwd, m, last):
+    y0 = W.stm_fixed_batch(64, seed=11)[:n]
+    tf = np.linspace(0.4, 1.6, n)  # per-trajectory spans
+    res = _dop(gpu, 12, y0, 0.0, tf, rtol=1e-11, atol=1e-11, fwd=fwd, n_samples=m, sample_last_only=last)
+    out = _np(res.samples)
+    assert np.all(_np(res.status) == _lib.HG_OK)
+    for i in range(n):
+        ref, na, nr, st = dev_oracle.dop853_dense(y0[i], np.linspace(0.0, tf[i], m), MU, rtol=1e-11, atol=1e-11,
+                                                  fwd=fwd, flip=(36, 42) if fwd == -1 else None)
+        assert st == 0
+        assert np.array_equal(out[:, i], ref[-1:] if last else ref)
+        assert int(_np(res.n_accept)[i]) == na and int(_np(res.n_reject)[i]) == nr
+    # the end state and time (not part of the dense output) as the single-warp kernel
+    r7 = _dop(gpu, 7, y0, 0.0, tf, rtol=1e-11, atol=1e-11, fwd=fwd, n_samples=m, sample_last_only=last)
+    assert np.array_equal(_np(res.y_end), _np(r7.y_end))
+    assert np.array_equal(_np(res.t_end), _np(r7.t_end))
+
+
+def test_pair_dop853_many_equals_single_warp_layouts(gpu):
+    # 1003 trajectories (201 pairs, ragged last group), uneven spans and step counts
+    y0 = W.stm_fixed_batch(1003, seed=12)
+    tf = np.random.default_rng(3).uniform(0.2, 2.0, len(y0))
+    fields = ("y_end", "t_end", "n_accept", "n_reject", "status", "samples")
+    res = {lanes: _dop(gpu, lanes, y0, 0.0, tf, n_samples=25) for lanes in (12, 7, 14)}
+    for f in fields:
+        assert np.array_equal(_np(getattr(res[12], f)), _np(getattr(res[7], f))), f
+        assert np.array_equal(_np(getattr(res[12], f)), _np(getattr(res[14], f))), f
+
+
+def test_pair_dop853_step_budget_status(gpu):
+    # trajectory 4 starts on the first primary: its field is not finite, every
+    # attempt is rejected and it runs out of steps like the single-warp kernel
+    y0 = W.stm_fixed_batch(64, seed=13)[:9].copy()
+    y0[4, 36:] = [-MU, 0.0, 0.0, 0.0, 0.0, 0.0]
+    for max_steps in (7, 2000):
+        r12 = _dop(gpu, 12, y0, 0.0, 1.0, max_steps=max_steps)
+        r7 = _dop(gpu, 7, y0, 0.0, 1.0, max_steps=max_steps)
+        for f in ("status", "n_accept", "n_reject", "t_end"):
+            assert np.array_equal(_np(getattr(r12, f)), _np(getattr(r7, f))), f
+        ok = _np(r12.status) == _lib.HG_OK
+        assert np.array_equal(_np(r12.y_end)[ok], _np(r7.y_end)[ok])
+        st = _np(r12.status)
+        assert st[4] == _lib.HG_MAX_STEPS
+        if max_steps == 7:
+            assert np.all(st == _lib.HG_MAX_STEPS)
+        else:
+            assert np.all(np.delete(st, 4) == _lib.HG_OK)
