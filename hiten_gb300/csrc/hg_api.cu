@@ -823,6 +823,13 @@ int hg_get_tuning(hg_handle* h, int key, int* value) {
   return HG_OK;
 }
 
+int hg_selftest_bounded_wait(hg_handle* h, int limit_ms, int* out3, void* stream) {
+  if (!h || !out3 || limit_ms < 1 || limit_ms > 2000) return fail(h, HG_ERR_ARGS, "bad self-test arguments");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, HG_ERR_CUDA, "cudaSetDevice");
+  hg::bounded_wait_selftest_kernel<<<1, 64, 0, (cudaStream_t)stream>>>(out3, 1000000ull * (unsigned long long)limit_ms);
+  return check_launch(h, "bounded_wait_selftest_kernel");
+}
+
 int hg_probe_fp64_peak(hg_handle* h, double* tflops) {
   if (!h || !tflops) return HG_ERR_ARGS;
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, HG_ERR_CUDA, "cudaSetDevice");

@@ -69,15 +69,45 @@ __device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned pari
 }
 
 // Wait for the completion of the phase with the given parity; false when it
-// has not completed within kPairWaitNs (or 2^30 polls).
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+// has not completed within limit_ns (or 2^30 polls).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity,
+                                          unsigned long long limit_ns = kPairWaitNs) {
   if (mbar_test(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   for (unsigned it = 1; it < (1u << 30); ++it) {
     if (mbar_test(bar, parity)) return true;
-    if ((it & 63u) == 0 && global_ns() - t0 > kPairWaitNs) return false;
+    if ((it & 63u) == 0 && global_ns() - t0 > limit_ns) return false;
   }
   return false;
+}
+
+// Self-test of the bounded wait (one block of two warps): warp 0 waits on a
+// barrier that nothing arrives at and must give up after limit_ns; then warp
+// 1 arrives at a second barrier and warp 0's wait on it must succeed.
+// out[0] = 1 if the first wait ran out, out[1] = 1 if the second completed,
+// out[2] = elapsed nanoseconds of the first wait.
+__global__ void bounded_wait_selftest_kernel(int* out, unsigned long long limit_ns) {
+  __shared__ unsigned long long bars[2];
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 32);
+    mbar_init(&bars[1], 32);
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5;
+  if (w == 0) {
+    const unsigned long long t0 = global_ns();
+    const bool ok0 = mbar_wait(&bars[0], 0, limit_ns);  // nothing arrives
+    const unsigned long long dt = global_ns() - t0;
+    const bool ran_out = !__any_sync(0xFFFFFFFFu, ok0);
+    const bool ok1 = __all_sync(0xFFFFFFFFu, mbar_wait(&bars[1], 0, limit_ns));
+    if (threadIdx.x == 0) {
+      out[0] = ran_out ? 1 : 0;
+      out[1] = ok1 ? 1 : 0;
+      out[2] = (int)(dt > 2000000000ull ? 2000000000ull : dt);
+    }
+  } else {
+    mbar_arrive(&bars[1]);
+  }
 }
 
 // Shared-memory hand-off of one warp pair.

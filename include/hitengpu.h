@@ -364,6 +364,15 @@ int hg_get_tuning(hg_handle* h, int key, int* value);
 #define HG_COUNTER_KERNEL_LAUNCHES 1
 int hg_get_counter(hg_handle* h, int key, long long* value);
 
+/* Self-test of the bounded inter-warp wait the paired 42-dim layouts use
+ * (every hand-off wait gives up after a time limit and the kernel reports
+ * HG_SYNC_TIMEOUT instead of hanging): one warp waits limit_ms on a barrier
+ * nothing arrives at, then on one the other warp arrives at.  out3 (device,
+ * 3 ints): [0] 1 if the first wait ran out, [1] 1 if the second completed,
+ * [2] nanoseconds the first wait took.  Asynchronous on `stream`.
+ * Replaces: nothing (failure-path test of the library's own waits). */
+int hg_selftest_bounded_wait(hg_handle* h, int limit_ms, int* out3, void* stream);
+
 /* Measured FP64 fused-multiply-add throughput of this device (TFLOP/s,
  * counting an FMA as 2 flops): runs a short dependent-chain-free DFMA loop
  * on all SMs and times it with CUDA events.  Synchronous. */

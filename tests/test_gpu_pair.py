@@ -131,3 +131,23 @@ def test_pair_dop853_step_budget_status(gpu):
             assert np.all(st == _lib.HG_MAX_STEPS)
         else:
             assert np.all(np.delete(st, 4) == _lib.HG_OK)
+
+
+def test_bounded_inter_warp_wait_runs_out_and_reports(gpu):
+    """The hand-off waits of the paired layouts are bounded: a wait that
+    nothing satisfies gives up after its limit (no hang, the context stays
+    usable) and a satisfied one completes."""
+    import ctypes as C
+    import torch
+    dev = torch.device("cuda", 0)
+    out = torch.full((3,), -1, dtype=torch.int32, device=dev)
+    H = _lib.handle(0)
+    H.check(H.lib.hg_selftest_bounded_wait(H.ptr, 50, C.c_void_p(out.data_ptr()),
+                                           C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
+    ran_out, completed, ns = (int(v) for v in out.cpu())
+    assert ran_out == 1 and completed == 1
+    assert 50_000_000 <= ns < 1_000_000_000
+    # the context is still usable
+    y0 = W.stm_fixed_batch(8, seed=1)
+    out2 = _np(gpu.propagate_fixed(y0, np.linspace(0.0, 0.1, 11), MU, order=8))
+    assert np.all(np.isfinite(out2))
