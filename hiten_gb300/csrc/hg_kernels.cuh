@@ -1138,12 +1138,126 @@ struct DopParams {
 
 #define HG_RUNNING (-1)
 
+// Position of the nonzero a_ij (1 <= i < 12, j < i) in DOP853's list of
+// nonzero stage coefficients by rows, followed by the nonzero b_j
+// (dop_flat(12, j)); -1 for a zero entry.  dop_nnz(): the list's length.
+__host__ __device__ constexpr int dop_flat(int i, int j) {
+  int q = 0;
+  for (int r = 1; r < DopTab::S; ++r)
+    for (int c = 0; c < r; ++c) {
+      if (DopTab::a(r, c) != 0.0) {
+        if (r == i && c == j) return q;
+        ++q;
+      }
+    }
+  for (int c = 0; c < DopTab::S; ++c) {
+    if (DopTab::b(c) != 0.0) {
+      if (i == DopTab::S && c == j) return q;
+      ++q;
+    }
+  }
+  return -1;
+}
+__host__ __device__ constexpr int dop_first_nonzero_e(bool e5) {
+  for (int j = 0; j < 13; ++j)
+    if ((e5 ? DopTab::e5(j) : DopTab::e3(j)) != 0.0) return j;
+  return -1;
+}
+__host__ __device__ constexpr int dop_nnz() {
+  int q = 0;
+  for (int r = 1; r < DopTab::S; ++r)
+    for (int c = 0; c < r; ++c) q += DopTab::a(r, c) != 0.0;
+  for (int c = 0; c < DopTab::S; ++c) q += DopTab::b(c) != 0.0;
+  return q;
+}
+
+// The products h * a_ij, h * b_j of one DOP853 step, formed where they are
+// used (one lane per trajectory).
+struct DopInlineCoef {
+  double h;
+  __device__ __forceinline__ void set_step(double hh) { h = hh; }
+  template <int I, int J>
+  __device__ __forceinline__ double a() const {
+    return h * DopTab::a(I, J);
+  }
+  template <int J>
+  __device__ __forceinline__ double b() const {
+    return h * DopTab::b(J);
+  }
+};
+
+// The list of nonzero coefficients itself (a_ij by rows, then b_j), written
+// into shared memory by the block's threads (entry q by thread q mod the
+// block size) before any lane leaves: `tab` must hold dop_nnz() doubles and
+// be followed by __syncthreads().
+__device__ __forceinline__ void dop_coef_table_init(double* tab) {
+  static_for<DopTab::S>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
+    static_for<i>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      if constexpr (DopTab::a(i, j) != 0.0) {
+        if ((unsigned)dop_flat(i, j) % blockDim.x == threadIdx.x) tab[dop_flat(i, j)] = DopTab::a(i, j);
+      }
+    });
+  });
+  static_for<DopTab::S>([&](auto jc) {
+    constexpr int j = decltype(jc)::value;
+    if constexpr (DopTab::b(j) != 0.0) {
+      if ((unsigned)dop_flat(DopTab::S, j) % blockDim.x == threadIdx.x) tab[dop_flat(DopTab::S, j)] = DopTab::b(j);
+    }
+  });
+}
+
+// The same products spread over the NL lanes of a trajectory's group (its h
+// is group-uniform): lane r forms list positions r, r + NL, ... from the
+// shared-memory table (ceil(58 / NL) FP64 multiplies per step instead of 58)
+// and the stages fetch them by shuffle within the group.  Bit-identical:
+// every product is the same h * a.
+template <int NL>
+struct DopGroupCoef {
+  static constexpr int K = dop_nnz();
+  static constexpr int P = (K + NL - 1) / NL;
+  const double* tab;  // dop_coef_table_init
+  int r;              // this lane's share
+  int src;            // first lane of the group
+  unsigned gmask;     // the group's lanes
+  double v[P];
+  __device__ __forceinline__ DopGroupCoef(const double* table, int share, int group_base, unsigned mask)
+      : tab(table), r(share), src(group_base), gmask(mask) {}
+  __device__ __forceinline__ void set_step(double h) {
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      const int q = r + NL * i;
+      v[i] = h * (q < K ? tab[q] : 0.0);
+    }
+  }
+  template <int I, int J>
+  __device__ __forceinline__ double a() const {
+    constexpr int q = dop_flat(I, J);
+    static_assert(q >= 0, "");
+    return __shfl_sync(gmask, v[q / NL], src + q % NL);
+  }
+  template <int J>
+  __device__ __forceinline__ double b() const {
+    constexpr int q = dop_flat(DopTab::S, J);
+    static_assert(q >= 0, "");
+    return __shfl_sync(gmask, v[q / NL], src + q % NL);
+  }
+};
+
 template <class LT>
 struct DopLaneT {
   static constexpr int NC = LT::NC;
   // one attempted DOP853 step; k[0] = f(t, y) on entry; k[12] = f(t+h, y_high)
   // on exit.
   __device__ __forceinline__ static void step(const LT& L, const double (&y)[NC], double h, double mu,
+                                              const Dir& dir, double (&k)[13][NC], double (&yh)[NC],
+                                              double (&e5)[NC], double (&e3)[NC]) {
+    step(L, y, DopInlineCoef{h}, h, mu, dir, k, yh, e5, e3);
+  }
+  // the same with the products h * a_ij, h * b_j from `cf` (set for h)
+  template <class CF>
+  __device__ __forceinline__ static void step(const LT& L, const double (&y)[NC], const CF& cf, double h, double mu,
                                               const Dir& dir, double (&k)[13][NC], double (&yh)[NC],
                                               double (&e5)[NC], double (&e3)[NC]) {
     using T = DopTab;
@@ -1154,9 +1268,8 @@ struct DopLaneT {
       for (int d = 0; d < NC; ++d) ys[d] = y[d];
       static_for<i>([&](auto jc) {
         constexpr int j = decltype(jc)::value;
-        constexpr double a = T::a(i, j);
-        if constexpr (a != 0.0) {
-          const double c = h * a;
+        if constexpr (T::a(i, j) != 0.0) {
+          const double c = cf.template a<i, j>();
 #pragma unroll
           for (int d = 0; d < NC; ++d) ys[d] = ys[d] + c * k[j][d];
         }
@@ -1167,30 +1280,29 @@ struct DopLaneT {
     for (int d = 0; d < NC; ++d) yh[d] = y[d];
     static_for<T::S>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
-      constexpr double b = T::b(j);
-      if constexpr (b != 0.0) {
-        const double c = h * b;
+      if constexpr (T::b(j) != 0.0) {
+        const double c = cf.template b<j>();
 #pragma unroll
         for (int d = 0; d < NC; ++d) yh[d] = yh[d] + c * k[j][d];
       }
     });
     L.rhs(yh, mu, dir, k[12]);
-#pragma unroll
-    for (int d = 0; d < NC; ++d) {
-      e5[d] = 0.0;
-      e3[d] = 0.0;
-    }
+    // err5 = sum_j E5_j k_j (the reference starts from zeros; the first term
+    // is taken as the start here: only the sign of an all-zero sum can
+    // differ, and err5 / err3 enter the step control squared)
     static_for<13>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
       constexpr double c5 = T::e5(j);
       constexpr double c3 = T::e3(j);
       if constexpr (c5 != 0.0) {
+        constexpr bool first = dop_first_nonzero_e(true) == j;
 #pragma unroll
-        for (int d = 0; d < NC; ++d) e5[d] = e5[d] + c5 * k[j][d];
+        for (int d = 0; d < NC; ++d) e5[d] = first ? c5 * k[j][d] : e5[d] + c5 * k[j][d];
       }
       if constexpr (c3 != 0.0) {
+        constexpr bool first = dop_first_nonzero_e(false) == j;
 #pragma unroll
-        for (int d = 0; d < NC; ++d) e3[d] = e3[d] + c3 * k[j][d];
+        for (int d = 0; d < NC; ++d) e3[d] = first ? c3 * k[j][d] : e3[d] + c3 * k[j][d];
       }
     });
 #pragma unroll
@@ -1283,6 +1395,21 @@ struct DopLaneT {
 
 template <int G>
 using DopLane = DopLaneT<Layout<G>>;
+
+// Step-coefficient provider of a layout: spread over the group for the
+// groups of 6 and 14 lanes (few components per lane), formed inline for 1,
+// 2 and 7 (whose lanes have no registers to spare).
+template <int G>
+__host__ __device__ constexpr bool dop_spread_coef() {
+  return G == 6 || G == 14;
+}
+template <int G>
+__device__ __forceinline__ auto dop_coef(const Layout<G>& L, const double* tab) {
+  if constexpr (dop_spread_coef<G>())
+    return DopGroupCoef<G>(tab, L.role, L.base, L.gmask);
+  else
+    return DopInlineCoef{0.0};
+}
 
 // Lane -> (group, role) for one launch; false for the idle lanes of a warp.
 template <int G>
@@ -1488,10 +1615,16 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
   Gather<G> gat;
   int traj;
   __shared__ double sm_gather[gather_smem_doubles<G>()];  // 4 warps x 4 groups
+  __shared__ double sm_coef[dop_spread_coef<G>() ? dop_nnz() : 1];
+  if constexpr (dop_spread_coef<G>()) {
+    dop_coef_table_init(sm_coef);
+    __syncthreads();
+  }
   if (!setup_layout<G>(L, gat, sm_gather, traj)) return;
   const bool leader = is_leader<G>(L);
   const bool has_event = p.ev_index >= 0 && p.max_hits > 0;
   const EvCtx<G> ev(L, has_event ? p.ev_index : -1);
+  auto cf = dop_coef<G>(L, sm_coef);
 
   int slot = traj;
   while (true) {
@@ -1572,7 +1705,8 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
       h = clamp_step(h, p.max_step, p.min_step);
       h = adjust_step_to_endpoint(t, h, tmax);
       double yh[NC], e5[NC], e3[NC];
-      DopLane<G>::step(L, y, h, p.mu, p.dir, k, yh, e5, e3);
+      cf.set_step(h);
+      DopLane<G>::step(L, y, cf, h, p.mu, p.dir, k, yh, e5, e3);
       double err_norm;
       {
         double s5[NC], s3[NC];

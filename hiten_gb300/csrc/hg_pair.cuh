@@ -371,8 +371,8 @@ __device__ __forceinline__ void pair_exchange(const LT& L, PairGather* gx, unsig
 // One warp's part of the DOP853 propagation of its five trajectories.
 // Returns its broken flag.
 template <class LT>
-__device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, PairGather* gx, int traj, bool valid,
-                                             bool writes) {
+__device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, PairGather* gx, const double* coef_tab,
+                                             int traj, bool valid, bool writes) {
   constexpr int NC = LT::NC;
   constexpr int D = 42;
   const double t0 = p.t0_arr ? p.t0_arr[traj] : p.t0;
@@ -408,6 +408,7 @@ __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, Pa
   auto sample_t = [&](int q) -> double { return q == p.m - 1 ? tmax : (double)q * step_ls + t0; };
   // integrators/rk.py loop test (t - t_end) * direction < 0, direction +1
   bool live = running && (t - tmax < 0.0);
+  DopGroupCoef<6> cf(coef_tab, L.role % 6, L.base, L.gmask);
   while (__any_sync(0xFFFFFFFFu, live)) {
     bool go = live;
     if (go && (long long)(acc + rej) >= p.max_steps) {
@@ -421,7 +422,8 @@ __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, Pa
       hh = adjust_step_to_endpoint(t, hh, tmax);
     }
     double yh[NC], e5[NC], e3[NC];
-    DopLaneT<LT>::step(L, y, hh, p.mu, p.dir, k, yh, e5, e3);
+    cf.set_step(hh);
+    DopLaneT<LT>::step(L, y, cf, hh, p.mu, p.dir, k, yh, e5, e3);
     double s5[NC], s3[NC];
     bool fin = true;
 #pragma unroll
@@ -520,6 +522,8 @@ __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, Pa
 __global__ void __launch_bounds__(128) dop853_pair_kernel(DopParams p) {
   __shared__ PairLink links[2];
   __shared__ PairGather gathers[2];
+  __shared__ double coef_tab[dop_nnz()];
+  dop_coef_table_init(coef_tab);
   const int w = threadIdx.x >> 5;
   const int npairs = blockDim.x >> 6;
   const int pair = w % npairs;
@@ -553,7 +557,7 @@ __global__ void __launch_bounds__(128) dop853_pair_kernel(DopParams p) {
       L.link = lk;
       L.seq = 0;
       L.broken = false;
-      broken = pair_dop_run(L, p, gx, tc, valid, valid && pl.role < 6);
+      broken = pair_dop_run(L, p, gx, coef_tab, tc, valid, valid && pl.role < 6);
     } else {
       PairStm L;
       L.col = pl.role < 6 ? pl.role : 5;
@@ -564,7 +568,7 @@ __global__ void __launch_bounds__(128) dop853_pair_kernel(DopParams p) {
       L.link = lk;
       L.seq = 0;
       L.broken = false;
-      broken = pair_dop_run(L, p, gx, tc, valid, valid && pl.role < 6);
+      broken = pair_dop_run(L, p, gx, coef_tab, tc, valid, valid && pl.role < 6);
       if (broken && lane == 0) lk->broken = 1;
     }
   }
