@@ -1,14 +1,16 @@
-// Paired-warp layout for the 42-dim variational system (fixed-step RK).
+// Paired-warp layout for the 42-dim variational system: fixed-step RK
+// (fixed_rk_pair_kernel) and single-pass DOP853 without an event
+// (dop853_pair_kernel).
 //
 // Why.  On GB300 an FP64 warp instruction holds its SM sub-partition's FP64
-// pipe for ~64 cycles whatever the number of active lanes, so one warp's
-// step costs (its FP64 instructions) x ~64 cycles.  A batch of about a
-// thousand 42-dim trajectories fills fewer warps than the GPU has
-// sub-partitions, and its time is the per-warp instruction count of a step.
-// The state of a trajectory (6 components, the Hessian of the potential and
-// the accelerations) and its STM (36 components, F(x) Phi) are two
-// instruction streams of about the same length; run on two warps of one
-// block, on two sub-partitions, they halve that count.
+// pipe for 64 (DFMA) to 76 (DMUL, DADD) cycles whatever the number of active
+// lanes, so one warp's step costs (its FP64 instructions) x ~70 cycles.  A
+// batch of about a thousand 42-dim trajectories fills fewer warps than the
+// GPU has sub-partitions, and its time is the per-warp instruction count of
+// a step.  The state of a trajectory (6 components, the Hessian of the
+// potential and the accelerations) and its STM (36 components, F(x) Phi)
+// are two instruction streams of about the same length; run on two warps of
+// one block, on two sub-partitions, they halve that count.
 //
 // Layout.  A trajectory group is five trajectories served by two warps:
 //   * the state warp: lane 6t + j (t < 5, j < 6) holds state component 36 + j
@@ -19,11 +21,11 @@
 // At every right-hand-side evaluation the state warp forms the Hessian's
 // diagonal from its stage state and hands it, with the two sums and the
 // stage's y and z the off-diagonal entries are products of, to the STM warp
-// (which forms those products) through shared memory (a ring of kPairSlots slots; an mbarrier pair
-// per slot, "full" after the state warp wrote it, "empty" after the STM warp
-// read it), while the STM warp forms its stage columns.  The step's
-// coefficients h * a_ij are spread over the lanes (WarpCoef).  Every operation and operand is the
-// one the 7-lane layout uses (Layout<7>), so the results are bit-identical.
+// (which forms those products) through shared memory: a ring of kPairSlots
+// slots with an mbarrier pair per slot, "full" after the state warp wrote
+// it, "empty" after the STM warp read it; meanwhile the STM warp forms its
+// stage columns.  Every operation and operand is the one the 7-lane layout
+// uses (Layout<7>), so the results are bit-identical.
 //
 // Waits are bounded: a hand-off that has not completed within
 // kPairWaitNs of wall time marks the warp broken; it stops waiting and
