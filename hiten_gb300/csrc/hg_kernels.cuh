@@ -479,6 +479,8 @@ struct Layout<6> {
 // numpy float64 dot order of the host the reference fixtures come from:
 // sequential fused accumulation for n < 16, a 32-element blocked sum plus a
 // fused tail for n = 42.  v is the full vector (identical in every lane).
+// This single-lane statement defines the order; the kernels evaluate it
+// spread over a lane group (dots42_group, and the Gather<G> helpers below).
 template <int D>
 __device__ __forceinline__ double np_dot_self(const double* v) {
   if constexpr (D == 6) {
