@@ -273,11 +273,13 @@ def bench_correct(args):
         nat = corrector.correct_halo_native(g, mu)
         torch.cuda.synchronize()
         tn.append(time.perf_counter() - t0)
-    _line("halo correction, 2048 guesses (L1/L2, Az 0.01-0.4)", "orbits corrected/s", len(g) / s, "orbits/s",
-          s * 1e3, {"orbits": len(g)}, converged=int((res.status == 0).sum()),
-          iterations_hist=np.bincount(res.iterations).tolist(), gpu_launches=res.launches,
-          native_driver={"ms": statistics.median(tn) * 1e3, "converged": int((nat.status == 0).sum()),
-                         "same_iterations": bool(np.array_equal(nat.iterations, res.iterations))})
+    sn = statistics.median(tn)
+    _line("halo correction, 2048 guesses (L1/L2, Az 0.01-0.4)", "orbits corrected/s", len(g) / sn, "orbits/s",
+          sn * 1e3, {"orbits": len(g), "driver": "native C-ABI hg_correct_halo"},
+          converged=int((nat.status == 0).sum()), iterations_hist=np.bincount(nat.iterations).tolist(),
+          python_host_loop={"ms": s * 1e3, "orbits_per_s": len(g) / s, "converged": int((res.status == 0).sum()),
+                            "gpu_launches": res.launches,
+                            "iterations_hist": np.bincount(res.iterations).tolist()})
 
 
 def bench_serving(args):
