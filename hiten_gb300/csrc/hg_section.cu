@@ -10,7 +10,9 @@
 // end values are both strictly positive or both strictly negative (and not
 // within the on-surface tolerance) cannot produce a crossing under linear
 // interpolation (every sub-interval value is a convex combination of two
-// same-signed numbers), so it is skipped without changing any result.
+// same-signed numbers), nor under cubic interpolation while the end values
+// clear the Hermite bounds below, so it is skipped without changing any
+// result; the scans of the remaining segments are shared by the warp.
 // Candidates are generated in segment order, which is the reference's
 // stable ordering, and deduplicated against the last accepted hit as they
 // stream out.  HBM-bound: each sample is read once (coalesced: samples are
@@ -106,133 +108,214 @@ struct Emitter {
   }
 };
 
+// Per-lane segment context shared during a cooperative scan.
+struct SegCtx {
+  double gk, gk1, d0, d1, dt;
+  bool cub;
+  bool skip0;  // the on-surface left end was accepted: sub-interval 0 is not scanned
+};
+
+// Value of g at sub-interval point q (s = q * step) of a segment: the cubic
+// Hermite or the linear interpolant, as the reference evaluates it.
+__device__ __forceinline__ double seg_point(const SegCtx& c, double s) {
+  return c.cub ? hermite_scalar(s, c.gk, c.gk1, c.d0, c.d1, c.dt) : (1.0 - s) * c.gk + s * c.gk1;
+}
+
+__device__ __forceinline__ bool sub_crosses(double g_lo, double g_hi, int direction) {
+  if (direction == 0) return (g_lo * g_hi <= 0.0) && (g_lo != g_hi);
+  if (direction == 1) return (g_lo < 0.0) && (g_hi >= 0.0);
+  return (g_lo > 0.0) && (g_hi <= 0.0);
+}
+
+// Warp-cooperative detection: the 32 lanes (one trajectory each) walk their
+// segments in lock step.  Each lane decides whether its segment can hold a
+// crossing (the exact skip tests above); the sub-interval scan of every
+// candidate segment is then shared by the whole warp (lane L evaluates the
+// sub-intervals 32 c + L, the same expressions on the same operands as the
+// sequential scan, so the same values), and every lane refines its own
+// crossings in sub-interval order -- Newton and interpolation run across
+// lanes instead of one lane at a time.  Results, their order and the
+// de-duplication are those of the per-trajectory loop.
 __global__ void __launch_bounds__(128) section_kernel(SecParams p) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.N) return;
-  Emitter em(p, i);
+  const int lane = threadIdx.x & 31;
+  const bool valid = i < p.N;
+  const int ii = valid ? i : 0;
+  Emitter em(p, ii);
   const int N = p.m;
   const int r = p.segment_refine;
   const double step = 1.0 / (double)(r + 1);
   const bool dir_any = p.direction == 0;
+  // sub-intervals the reference scans: mm = 0 .. n_sub - 1 (it stops at the
+  // first whose upper end exceeds 1 + 1e-15)
+  int n_sub = 0;
+  while (n_sub <= r && !((double)(n_sub + 1) * step > 1.0 + 1e-15)) ++n_sub;
+  const int n_chunks = (n_sub + 31) / 32;
   double g_prev = 0.0;
-  double gk = smp(p, 0, p.axis, i) - p.offset;
-  double tk = tim(p, 0, i);
-  for (int k = 0; k + 1 < N && !em.full; ++k) {
-    const double gk1 = smp(p, k + 1, p.axis, i) - p.offset;
-    const double tk1 = tim(p, k + 1, i);
-    const double dt = tk1 - tk;
-    const bool near = fabs(gk) < p.tol_on_surface;
-    const bool same_sign = (gk > 0.0 && gk1 > 0.0) || (gk < 0.0 && gk1 < 0.0);
-    const bool tiny = fabs(gk) < 1e-280 || fabs(gk1) < 1e-280;
-    if (!near && same_sign && !tiny && !p.cubic) {
-      g_prev = gk;
-      gk = gk1;
-      tk = tk1;
-      continue;
+  double gk = valid && N > 0 ? smp(p, 0, p.axis, ii) - p.offset : 0.0;
+  double tk = valid && N > 0 ? tim(p, 0, ii) : 0.0;
+  for (int k = 0; k + 1 < N; ++k) {
+    const bool live = valid && !em.full;
+    if (!__any_sync(0xFFFFFFFFu, live)) break;
+    SegCtx c{gk, 0.0, 0.0, 0.0, 0.0, false, false};
+    double tk1 = tk;
+    bool cand = false;
+    if (live) {
+      const double gk1 = smp(p, k + 1, p.axis, ii) - p.offset;
+      tk1 = tim(p, k + 1, ii);
+      const double dt = tk1 - tk;
+      c.gk1 = gk1;
+      c.dt = dt;
+      const bool near = fabs(gk) < p.tol_on_surface;
+      const bool same_sign = (gk > 0.0 && gk1 > 0.0) || (gk < 0.0 && gk1 < 0.0);
+      const bool tiny = fabs(gk) < 1e-280 || fabs(gk1) < 1e-280;
+      cand = true;
+      if (!near && same_sign && !tiny && !p.cubic) cand = false;
+      if (cand) {
+        c.cub = p.cubic && dt > 0.0;
+        if (c.cub) {
+          if (k - 1 >= 0)
+            c.d0 = (gk1 - g_prev) / (tk1 - tim(p, k - 1, ii));
+          else
+            c.d0 = (gk1 - gk) / (tk1 - tk);
+          if (k + 2 < N)
+            c.d1 = ((smp(p, k + 2, p.axis, ii) - p.offset) - gk) / (tim(p, k + 2, ii) - tk);
+          else
+            c.d1 = (gk1 - gk) / (tk1 - tk);
+        }
+        // Cubic segments that cannot cross.  On [0, 1] the Hermite cubic with
+        // end values g0, g1 and end slopes m0 = d0 dt, m1 = d1 dt is the
+        // Bezier curve with control values g0, g0 + m0/3, g1 - m1/3, g1 and
+        // lies in their convex hull; it also satisfies g(s) = g0 H00 + g1 H01
+        // + m0 H10 + m1 H11 with H00, H01 >= 0, H00 + H01 = 1, |H10|, |H11|
+        // <= 4/27.  When either bound keeps it on the side of the
+        // (same-signed) end values by more than 2^-46 (|g0| + |g1| + |m0| +
+        // |m1|) -- far above the rounding of any evaluated point (a few
+        // ulps) -- no sub-interval value changes sign, and skipping the scan
+        // changes no result.
+        if (c.cub && !near && same_sign && !tiny) {
+          const double m0 = c.d0 * dt, m1 = c.d1 * dt;
+          const double am0 = fabs(m0), am1 = fabs(m1);
+          const double margin = 0x1p-46 * ((fabs(gk) + fabs(gk1)) + (am0 + am1));
+          const double sg = gk > 0.0 ? 1.0 : -1.0;
+          const double b1 = sg * (gk + m0 / 3.0), b2 = sg * (gk1 - m1 / 3.0);
+          const bool hull = b1 > margin && b2 > margin && fabs(gk) > margin && fabs(gk1) > margin;
+          const double lo = fmin(fabs(gk), fabs(gk1));
+          const bool basis = lo > (4.0 / 27.0) * (am0 + am1) * (1.0 + 1e-12) + margin;
+          if (hull || basis) cand = false;
+        }
+      }
+      if (cand && near) {
+        bool accept_left;
+        if (dir_any)
+          accept_left = true;
+        else if (p.direction == 1)
+          accept_left = (gk1 >= 0.0) || (k - 1 >= 0 && g_prev <= 0.0);
+        else
+          accept_left = (gk1 <= 0.0) || (k - 1 >= 0 && g_prev >= 0.0);
+        if (accept_left) {
+          double x[6];
+#pragma unroll
+          for (int cc = 0; cc < 6; ++cc) x[cc] = smp(p, k, cc, ii);
+          em.offer(tk, x);
+          c.skip0 = true;
+        }
+      }
+      if (em.full) cand = false;
     }
-    double d0 = 0.0, d1 = 0.0;
-    const bool cub = p.cubic && dt > 0.0;
-    if (cub) {
-      if (k - 1 >= 0)
-        d0 = (gk1 - g_prev) / (tk1 - tim(p, k - 1, i));
-      else
-        d0 = (gk1 - gk) / (tk1 - tk);
-      if (k + 2 < N)
-        d1 = ((smp(p, k + 2, p.axis, i) - p.offset) - gk) / (tim(p, k + 2, i) - tk);
-      else
-        d1 = (gk1 - gk) / (tk1 - tk);
-    }
-    bool accept_left = false;
-    if (near) {
-      if (dir_any)
-        accept_left = true;
-      else if (p.direction == 1)
-        accept_left = (gk1 >= 0.0) || (k - 1 >= 0 && g_prev <= 0.0);
-      else
-        accept_left = (gk1 <= 0.0) || (k - 1 >= 0 && g_prev >= 0.0);
-      if (accept_left) {
+    const unsigned cmask = __ballot_sync(0xFFFFFFFFu, cand);
+    for (int ch = 0; ch < n_chunks && cmask; ++ch) {
+      // scan chunk ch of every candidate segment with the whole warp
+      unsigned my_bits = 0;
+      for (unsigned rest = cmask; rest; rest &= rest - 1) {
+        const int j = __ffs(rest) - 1;
+        SegCtx cj;
+        cj.gk = __shfl_sync(0xFFFFFFFFu, c.gk, j);
+        cj.gk1 = __shfl_sync(0xFFFFFFFFu, c.gk1, j);
+        cj.d0 = __shfl_sync(0xFFFFFFFFu, c.d0, j);
+        cj.d1 = __shfl_sync(0xFFFFFFFFu, c.d1, j);
+        cj.dt = __shfl_sync(0xFFFFFFFFu, c.dt, j);
+        cj.cub = __shfl_sync(0xFFFFFFFFu, (int)c.cub, j) != 0;
+        cj.skip0 = __shfl_sync(0xFFFFFFFFu, (int)c.skip0, j) != 0;
+        const int mm = 32 * ch + lane;
+        bool x = false;
+        if (mm < n_sub && !(cj.skip0 && mm == 0)) {
+          const double g_lo = seg_point(cj, (double)mm * step);
+          const double g_hi = seg_point(cj, (double)(mm + 1) * step);
+          x = sub_crosses(g_lo, g_hi, p.direction);
+        }
+        const unsigned bits = __ballot_sync(0xFFFFFFFFu, x);
+        if (lane == j) my_bits = bits;
+      }
+      // every lane refines its own crossings of this chunk, in order
+      while (my_bits && !em.full) {
+        const int mm = 32 * ch + __ffs(my_bits) - 1;
+        my_bits &= my_bits - 1;
+        const double s_lo = (double)mm * step;
+        const double s_hi = (double)(mm + 1) * step;
+        const double g_lo = seg_point(c, s_lo);
+        const double g_hi = seg_point(c, s_hi);
+        double s_star;
+        if (g_lo == g_hi) {
+          s_star = 0.5 * (s_lo + s_hi);
+        } else {
+          double a = g_lo / (g_lo - g_hi);
+          a = fmin(1.0, fmax(0.0, a));
+          s_star = s_lo + a * (s_hi - s_lo);
+        }
+        if (c.cub) {
+          for (int it = 0; it < p.newton_max_iter; ++it) {
+            const double f = hermite_scalar(s_star, c.gk, c.gk1, c.d0, c.d1, c.dt);
+            const double df = hermite_der(s_star, c.gk, c.gk1, c.d0, c.d1, c.dt);
+            if (df == 0.0) break;
+            s_star -= f / df;
+            if (s_star < s_lo) {
+              s_star = s_lo;
+              break;
+            }
+            if (s_star > s_hi) {
+              s_star = s_hi;
+              break;
+            }
+          }
+        }
+        const double th = (1.0 - s_star) * tk + s_star * tk1;
+        const double dt = c.dt;
         double x[6];
+        if (c.cub && k - 1 >= 0 && k + 2 < N) {
+          const double tm1 = tim(p, k - 1, ii), tp2 = tim(p, k + 2, ii);
+          const double s = s_star;
+          const double om = 1.0 - s;
+          const double h00 = (1.0 + 2.0 * s) * (om * om);
+          const double h10 = s * (om * om);
+          const double h01 = (s * s) * (3.0 - 2.0 * s);
+          const double h11 = (s * s) * (s - 1.0);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) x[c] = smp(p, k, c, i);
-        em.offer(tk, x);
-      }
-    }
-    for (int mm = 0; mm <= r && !em.full; ++mm) {
-      const double s_lo = (double)mm * step;
-      const double s_hi = (double)(mm + 1) * step;
-      if (s_hi > 1.0 + 1e-15) break;
-      if (accept_left && mm == 0) continue;
-      double g_lo, g_hi;
-      if (cub) {
-        g_lo = hermite_scalar(s_lo, gk, gk1, d0, d1, dt);
-        g_hi = hermite_scalar(s_hi, gk, gk1, d0, d1, dt);
-      } else {
-        g_lo = (1.0 - s_lo) * gk + s_lo * gk1;
-        g_hi = (1.0 - s_hi) * gk + s_hi * gk1;
-      }
-      bool crosses;
-      if (dir_any)
-        crosses = (g_lo * g_hi <= 0.0) && (g_lo != g_hi);
-      else if (p.direction == 1)
-        crosses = (g_lo < 0.0) && (g_hi >= 0.0);
-      else
-        crosses = (g_lo > 0.0) && (g_hi <= 0.0);
-      if (!crosses) continue;
-      double s_star;
-      if (g_lo == g_hi) {
-        s_star = 0.5 * (s_lo + s_hi);
-      } else {
-        double a = g_lo / (g_lo - g_hi);
-        a = fmin(1.0, fmax(0.0, a));
-        s_star = s_lo + a * (s_hi - s_lo);
-      }
-      if (cub) {
-        for (int it = 0; it < p.newton_max_iter; ++it) {
-          const double f = hermite_scalar(s_star, gk, gk1, d0, d1, dt);
-          const double df = hermite_der(s_star, gk, gk1, d0, d1, dt);
-          if (df == 0.0) break;
-          s_star -= f / df;
-          if (s_star < s_lo) {
-            s_star = s_lo;
-            break;
+          for (int cc = 0; cc < 6; ++cc) {
+            const double dxdt0 = (smp(p, k + 1, cc, ii) - smp(p, k - 1, cc, ii)) / (tk1 - tm1);
+            const double dxdt1 = (smp(p, k + 2, cc, ii) - smp(p, k, cc, ii)) / (tp2 - tk);
+            x[cc] = ((h00 * smp(p, k, cc, ii) + (h10 * dxdt0) * dt) + h01 * smp(p, k + 1, cc, ii)) + (h11 * dxdt1) * dt;
           }
-          if (s_star > s_hi) {
-            s_star = s_hi;
-            break;
+        } else {
+#pragma unroll
+          for (int cc = 0; cc < 6; ++cc) {
+            const double a0 = smp(p, k, cc, ii);
+            x[cc] = a0 + s_star * (smp(p, k + 1, cc, ii) - a0);
           }
         }
+        em.offer(th, x);
       }
-      const double th = (1.0 - s_star) * tk + s_star * tk1;
-      double x[6];
-      if (cub && k - 1 >= 0 && k + 2 < N) {
-        const double tm1 = tim(p, k - 1, i), tp2 = tim(p, k + 2, i);
-        const double s = s_star;
-        const double om = 1.0 - s;
-        const double h00 = (1.0 + 2.0 * s) * (om * om);
-        const double h10 = s * (om * om);
-        const double h01 = (s * s) * (3.0 - 2.0 * s);
-        const double h11 = (s * s) * (s - 1.0);
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-          const double dxdt0 = (smp(p, k + 1, c, i) - smp(p, k - 1, c, i)) / (tk1 - tm1);
-          const double dxdt1 = (smp(p, k + 2, c, i) - smp(p, k, c, i)) / (tp2 - tk);
-          x[c] = ((h00 * smp(p, k, c, i) + (h10 * dxdt0) * dt) + h01 * smp(p, k + 1, c, i)) + (h11 * dxdt1) * dt;
-        }
-      } else {
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-          const double a0 = smp(p, k, c, i);
-          x[c] = a0 + s_star * (smp(p, k + 1, c, i) - a0);
-        }
-      }
-      em.offer(th, x);
     }
-    g_prev = gk;
-    gk = gk1;
-    tk = tk1;
+    if (live) {
+      g_prev = gk;
+      gk = c.gk1;
+      tk = tk1;
+    }
   }
-  p.n_hits[i] = em.stored;
-  if (p.n_found) p.n_found[i] = em.found;
+  if (valid) {
+    p.n_hits[i] = em.stored;
+    if (p.n_found) p.n_found[i] = em.found;
+  }
 }
 
 // Manifold acceptance filters on sampled trajectories
