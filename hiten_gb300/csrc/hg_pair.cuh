@@ -155,7 +155,7 @@ struct PairState {
     const Hess H = hessian_split<PairState, false>(*this, role < 6 ? role : 0, x, y, z, vx, vy, mu);
     const unsigned b = seq % kPairSlots, use = seq / kPairSlots;
     if (!broken && use >= 1) {
-      // the slot's previous contents must have been read (warp-uniform verdict)
+      // the slot's previous contents must have been read (a warp-uniform outcome)
       const bool ok = mbar_wait(&link->empty[b], (use - 1u) & 1u);
       broken = !__all_sync(0xFFFFFFFFu, ok);
     }
