@@ -91,7 +91,7 @@ int launch_fixed(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
 // per pair, lat 0.6: RK8 on GB300, 125 ms against 214 ms for G = 7 over 3000
 // steps of 512 states) competes too.
 int lanes_d42(const hg_handle* h, int n, bool pair = false, double pair_lat = 0.0) {
-  if (h->lanes_d42 != 0) return (h->lanes_d42 == 12 && !pair) ? 7 : h->lanes_d42;
+  if (h->lanes_d42 != 0) return ((h->lanes_d42 == 12 || h->lanes_d42 == 18) && !pair) ? 7 : h->lanes_d42;
   const double cap = 0.1 * h->sm_capacity_x10 * h->sm_count;
   const double w7 = (double)((n + 3) / 4), w14 = (double)((n + 1) / 2);
   const double wp = 2.0 * (double)((n + hg::kPairTraj - 1) / hg::kPairTraj);
@@ -105,14 +105,27 @@ int lanes_d42(const hg_handle* h, int n, bool pair = false, double pair_lat = 0.
 // Per-step latency of the paired-warp layout relative to G = 7 (0: not
 // chosen automatically).
 constexpr double kPairLatFixed = 0.6;
-// DOP853, no event, no per-step dense samples (STM legs of the corrector:
-// 2.72 ms against 2.93 (G = 7) and 3.50 (G = 14) for 2048 orbits; 1.92
-// against 1.98 / 2.53 for 512).  Runs sampling every step (one trajectory,
-// 2000 samples) are faster on G = 14 and never pick the pair.
-constexpr double kPairLatDop = 0.5;
+// Event-free single-pass DOP853 on 42 components: the three-warp layout
+// (state warp + two half-column STM warps) while its warps fit about three
+// per SM (3 N / 5 <= 3 x SMs), the pair above -- measured for the corrector's
+// STM legs (ms: 64 orbits trio 1.60, pair 1.81, G = 14 1.91, G = 7 2.43; 512
+// orbits 1.68 / 1.88 / 1.95 / 2.53; 2048 orbits 2.91 / 2.66 / 3.42 / 2.97)
+// and one trajectory with 2000 dense samples (7.4 / 10.6 / 9.3 / 15.0).
+int lanes_d42_dop_free(const hg_handle* h, int n) {
+  if (h->lanes_d42 != 0) return h->lanes_d42;
+  const double cap = 0.1 * h->sm_capacity_x10 * h->sm_count;
+  return 3.0 * ((n + hg::kPairTraj - 1) / hg::kPairTraj) <= cap ? 18 : 12;
+}
 
 // Paired-warp DOP853 launch (42-dim, no event, single pass): blocks of one
 // pair (two with HG_TUNE_BLOCK_THREADS 128).
+int launch_dop853_trio(hg_handle* h, const hg::DopParams& p, cudaStream_t s) {
+  const int grid = (p.N + hg::kPairTraj - 1) / hg::kPairTraj;
+  if (grid < 1) return HG_OK;
+  hg::dop853_trio_kernel<<<grid, 96, 0, s>>>(p);
+  return check_launch(h, "dop853_trio_kernel");
+}
+
 int launch_dop853_pair(hg_handle* h, const hg::DopParams& p, cudaStream_t s) {
   const int block = h->block >= 128 ? 128 : 64;
   const int per_block = (block / 64) * hg::kPairTraj;
@@ -636,10 +649,11 @@ int hg_propagate_dop853(hg_handle* h, double mu, int dim, int N, const double* y
     else
       rc2 = launch_dop853<1>(h, p, s);
   } else {
-    const bool per_step_samples = p.m >= 2 && !p.dense_last;
-    const int g = lanes_d42(h, N, p.ev_index < 0, per_step_samples ? 0.0 : kPairLatDop);
+    const int g = p.ev_index < 0 ? lanes_d42_dop_free(h, N) : lanes_d42(h, N);
     if (g == 12 && p.ev_index < 0)
       rc2 = launch_dop853_pair(h, p, s);
+    else if (g == 18 && p.ev_index < 0)
+      rc2 = launch_dop853_trio(h, p, s);
     else
       rc2 = g == 14 ? launch_dop853<14>(h, p, s) : launch_dop853<7>(h, p, s);
   }
@@ -786,8 +800,8 @@ int hg_set_tuning(hg_handle* h, int key, int value) {
       h->sm_capacity_x10 = value;
       return HG_OK;
     case HG_TUNE_LANES_D42:
-      if (value != 0 && value != 7 && value != 14 && value != 12)
-        return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 7, 14 or 12 (paired warps)");
+      if (value != 0 && value != 7 && value != 14 && value != 12 && value != 18)
+        return fail(h, HG_ERR_ARGS, "lanes must be 0 (auto), 7, 14, 12 (paired warps) or 18 (three warps)");
       h->lanes_d42 = value;
       return HG_OK;
     case HG_TUNE_SPREAD:

@@ -140,6 +140,7 @@ struct PairState {
   static constexpr int D = 42;
   static constexpr int NC = 1;
   static constexpr bool kState = true;
+  __device__ __forceinline__ int flag_slot() const { return 42; }  // gather-slot flag entry
   int role, base, t;
   unsigned gmask;
   PairLink* link;
@@ -185,6 +186,7 @@ struct PairStm {
   static constexpr int D = 42;
   static constexpr int NC = 6;
   static constexpr bool kState = false;
+  __device__ __forceinline__ int flag_slot() const { return 43; }  // and 44: the whole STM
   int col, t;
   int role, base;  // lane placement (role 0..7, as in the state warp), for group-wide steps
   unsigned gmask;
@@ -225,6 +227,64 @@ struct PairStm {
       const int c = comp(r);
       dv[r] = neg_if(dv[r], c >= dir.neg_lo && c < dir.neg_hi);
     }
+  }
+};
+
+// Half-column STM warps of the three-warp layout (dop853_trio_kernel): two
+// warps share the 36 STM components of five trajectories.  A half-group of
+// six lanes holds three columns of one trajectory (columns 3 half .. 3 half +
+// 2), each column on a lane pair as in Layout<14>: the even lane rows 0..2,
+// the odd lane rows 3..5; warp w holds half-groups 5w .. 5w + 4 (trajectory
+// = half-group / 2, half = half-group % 2).  A half-group is a complete
+// six-lane group for the step control (coefficients, norms, step-size
+// factor), so each trajectory's two halves take the same decisions.
+struct PairStmHalf {
+  static constexpr int D = 42;
+  static constexpr int NC = 3;
+  static constexpr bool kState = false;
+  int t, half;
+  int role, base;  // lane placement within the half-group (6, 7 on the shadow lanes)
+  unsigned gmask;
+  PairLink* link;
+  mutable unsigned seq;
+  mutable bool broken;
+  __device__ __forceinline__ int flag_slot() const { return 43 + half; }
+  __device__ __forceinline__ int comp(int r) const {
+    const int r6 = role % 6;
+    return 6 * (3 * (r6 & 1) + r) + 3 * half + (r6 >> 1);
+  }
+  __device__ __forceinline__ void rhs(const double (&v)[3], double mu, const Dir& dir, double (&dv)[3]) const {
+    (void)mu;
+    const unsigned b = seq % kPairSlots;
+    double xx = 0.0, yy = 0.0, zz = 0.0, xy = 0.0, xz = 0.0, yz = 0.0;
+    if (!broken) {
+      const bool ok = mbar_wait(&link->full[b], (seq / kPairSlots) & 1u);
+      broken = !__all_sync(0xFFFFFFFFu, ok);
+    }
+    if (!broken) {
+      const double* e = link->H[b][t];
+      xx = e[0];
+      yy = e[1];
+      zz = e[2];
+      const double sxy = e[3], qab = e[4], y = e[5], z = e[6];
+      mbar_arrive(&link->empty[b]);
+      xy = (3.0 * y) * sxy;
+      xz = (3.0 * z) * sxy;
+      yz = ((3.0 * y) * z) * qab;
+    }
+    ++seq;
+    // the partner lane (lane ^ 1) holds the other rows of the column
+    const double q0 = __shfl_xor_sync(gmask, v[0], 1), q1 = __shfl_xor_sync(gmask, v[1], 1),
+                 q2 = __shfl_xor_sync(gmask, v[2], 1);
+    // rows 3..5 of F(x) Phi[:, c] (dynamics/rtbp.py:204-209), as Layout<14>
+    const double r3 = ((xx * q0 + xy * q1) + xz * q2) + 2.0 * v[1];
+    const double r4 = ((xy * q0 + yy * q1) + yz * q2) + (-2.0) * v[0];
+    const double r5 = (xz * q0 + yz * q1) + zz * q2;
+    const bool pos = ((role % 6) & 1) == 0;
+    const double d0 = pos ? q0 : r3, d1 = pos ? q1 : r4, d2 = pos ? q2 : r5;
+    dv[0] = neg_if(d0, comp(0) >= dir.neg_lo && comp(0) < dir.neg_hi);
+    dv[1] = neg_if(d1, comp(1) >= dir.neg_lo && comp(1) < dir.neg_hi);
+    dv[2] = neg_if(d2, comp(2) >= dir.neg_lo && comp(2) < dir.neg_hi);
   }
 };
 
@@ -341,14 +401,16 @@ __global__ void __launch_bounds__(128) fixed_rk_pair_kernel(FixedParams p) {
 // computing on their frozen state without committing anything, so every
 // hand-off has all 32 lanes of both warps.
 struct PairGather {
-  double v[2][kPairTraj][2][44];  // slot, trajectory, vector, 42 components + the two warps' flags
+  // slot, trajectory, vector, 42 components + flags: [42] the state warp's,
+  // [43], [44] the STM's (one warp: both; two half-column warps: one each)
+  double v[2][kPairTraj][2][45];
   unsigned long long bar[2];
 };
 
 template <class LT>
 __device__ __forceinline__ void pair_exchange(const LT& L, PairGather* gx, unsigned& gseq,
                                               const double (&a)[LT::NC], const double (&b)[LT::NC],
-                                              double flag, double& dot_a, double& dot_b, double& flag_other) {
+                                              double flag, double& dot_a, double& dot_b, double& flag_all) {
   const unsigned sl = gseq & 1u;
   double* va = gx->v[sl][L.t][0];
   double* vb = gx->v[sl][L.t][1];
@@ -359,7 +421,10 @@ __device__ __forceinline__ void pair_exchange(const LT& L, PairGather* gx, unsig
         va[L.comp(r)] = a[r];
         vb[L.comp(r)] = b[r];
       }
-      if (L.role == 0) va[LT::kState ? 42 : 43] = flag;
+      if (L.role == 0) {
+        va[L.flag_slot()] = flag;
+        if constexpr (LT::kState == false && LT::NC == 6) va[44] = flag;
+      }
     }
     mbar_arrive(&gx->bar[sl]);
     const bool ok = mbar_wait(&gx->bar[sl], (gseq >> 1) & 1u);
@@ -367,14 +432,23 @@ __device__ __forceinline__ void pair_exchange(const LT& L, PairGather* gx, unsig
   }
   ++gseq;
   dots42_group(L, va, vb, dot_a, dot_b);
-  flag_other = va[LT::kState ? 43 : 42];
+  flag_all = (va[42] != 0.0 && va[43] != 0.0 && va[44] != 0.0) ? 1.0 : 0.0;
 }
 
 // One warp's part of the DOP853 propagation of its five trajectories.
-// Returns its broken flag.
-template <class LT>
+// Decisions that set how many hand-offs a step makes (keep stepping, build a
+// dense cache) are votes over the warp (BLOCK = false: both warps of a pair
+// hold the same trajectories) or over the block (BLOCK = true: the three
+// warps of a trio hold different subsets).  Returns its broken flag.
+template <bool BLOCK, class LT>
 __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, PairGather* gx, const double* coef_tab,
                                              int traj, bool valid, bool writes) {
+  auto vote_any = [](bool v) -> bool {
+    if constexpr (BLOCK)
+      return __syncthreads_or(v ? 1 : 0) != 0;
+    else
+      return __any_sync(0xFFFFFFFFu, v);
+  };
   constexpr int NC = LT::NC;
   constexpr int D = 42;
   const double t0 = p.t0_arr ? p.t0_arr[traj] : p.t0;
@@ -411,7 +485,7 @@ __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, Pa
   // integrators/rk.py loop test (t - t_end) * direction < 0, direction +1
   bool live = running && (t - tmax < 0.0);
   DopGroupCoef<6> cf(coef_tab, L.role % 6, L.base, L.gmask);
-  while (__any_sync(0xFFFFFFFFu, live)) {
+  while (vote_any(live)) {
     bool go = live;
     if (go && (long long)(acc + rej) >= p.max_steps) {
       status = HG_MAX_STEPS;
@@ -437,9 +511,9 @@ __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, Pa
       fin = fin && finite_bits(yh[d]);
     }
     fin = __all_sync(L.gmask, fin);
-    double n5, n3, fin_other;
-    pair_exchange(L, gx, gseq, s5, s3, fin ? 1.0 : 0.0, n5, n3, fin_other);
-    fin = fin && fin_other != 0.0;
+    double n5, n3, fin_all;
+    pair_exchange(L, gx, gseq, s5, s3, fin ? 1.0 : 0.0, n5, n3, fin_all);
+    fin = fin_all != 0.0;
     double err_norm;
     if (n5 == 0.0 && n3 == 0.0)
       err_norm = 0.0;
@@ -454,7 +528,7 @@ __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, Pa
       last = !(t_new - tmax < 0.0);
       need = q_next < p.m && (last || sample_t(q_next) < t_new);
     }
-    if (__any_sync(0xFFFFFFFFu, need)) {
+    if (vote_any(need)) {
       const double hseg = t_new - t;
       double F[7][NC];
       DopLaneT<LT>::dense_cache(L, y, yh, hseg, p.mu, p.dir, k, F);
@@ -559,7 +633,7 @@ __global__ void __launch_bounds__(128) dop853_pair_kernel(DopParams p) {
       L.link = lk;
       L.seq = 0;
       L.broken = false;
-      broken = pair_dop_run(L, p, gx, coef_tab, tc, valid, valid && pl.role < 6);
+      broken = pair_dop_run<false>(L, p, gx, coef_tab, tc, valid, valid && pl.role < 6);
     } else {
       PairStm L;
       L.col = pl.role < 6 ? pl.role : 5;
@@ -570,12 +644,71 @@ __global__ void __launch_bounds__(128) dop853_pair_kernel(DopParams p) {
       L.link = lk;
       L.seq = 0;
       L.broken = false;
-      broken = pair_dop_run(L, p, gx, coef_tab, tc, valid, valid && pl.role < 6);
+      broken = pair_dop_run<false>(L, p, gx, coef_tab, tc, valid, valid && pl.role < 6);
       if (broken && lane == 0) lk->broken = 1;
     }
   }
   __syncthreads();
   if (!stm && valid && pl.role == 0 && p.status && (broken || lk->broken)) p.status[traj] = HG_SYNC_TIMEOUT;
+}
+
+// Three-warp DOP853 (42-dim, single pass, no event): blocks of 96 threads,
+// warp 0 the state warp of five trajectories, warps 1 and 2 their STM as
+// half-columns (PairStmHalf) -- the STM warp's stage work halved, for
+// batches too small to fill the GPU, where one warp's step sets the time.
+// The Hessian ring's "empty" barriers take both STM warps' arrivals, the
+// norm gather all three warps'.
+__global__ void __launch_bounds__(96) dop853_trio_kernel(DopParams p) {
+  __shared__ PairLink link;
+  __shared__ PairGather gather;
+  __shared__ double coef_tab[dop_nnz()];
+  dop_coef_table_init(coef_tab);
+  const int w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x < (int)kPairSlots) {
+    mbar_init(&link.full[threadIdx.x], 32);
+    mbar_init(&link.empty[threadIdx.x], 64);
+    if (threadIdx.x < 2) mbar_init(&gather.bar[threadIdx.x], 96);
+    if (threadIdx.x == 0) link.broken = 0;
+  }
+  __syncthreads();
+  const PairLane pl(lane);
+  const int group = blockIdx.x;
+  const bool active = group * kPairTraj < p.N;  // uniform over the block
+  // trajectory of this lane within the group
+  const int hg = 5 * (w - 1) + pl.t;                 // STM warps: half-group 0..9
+  const int tg = w == 0 ? pl.t : hg / 2;
+  const int traj = group * kPairTraj + tg;
+  const bool valid = active && traj < p.N;
+  const int tc = valid ? traj : (active ? p.N - 1 : 0);
+  bool broken = false;
+  if (active) {
+    if (w == 0) {
+      PairState L;
+      L.role = pl.role;
+      L.base = pl.base;
+      L.t = pl.t;
+      L.gmask = pl.gmask;
+      L.link = &link;
+      L.seq = 0;
+      L.broken = false;
+      broken = pair_dop_run<true>(L, p, &gather, coef_tab, tc, valid, valid && pl.role < 6);
+    } else {
+      PairStmHalf L;
+      L.t = tg;
+      L.half = hg & 1;
+      L.role = pl.role;
+      L.base = pl.base;
+      L.gmask = pl.gmask;
+      L.link = &link;
+      L.seq = 0;
+      L.broken = false;
+      broken = pair_dop_run<true>(L, p, &gather, coef_tab, tc, valid, valid && pl.role < 6);
+      if (broken && lane == 0) link.broken = 1;
+    }
+  }
+  __syncthreads();
+  if (w == 0 && valid && pl.role == 0 && p.status && (broken || link.broken)) p.status[traj] = HG_SYNC_TIMEOUT;
 }
 
 }  // namespace hg

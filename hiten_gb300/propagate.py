@@ -251,7 +251,7 @@ class tuning:
     ``lanes_d6`` in {0 (auto), 1, 2, 6} lanes per 6-dim DOP853 trajectory,
     ``block`` in {32, 64, 128} threads per block, ``seg_steps`` attempted
     steps per segment of the scheduled driver, ``spread`` one 4-warp block
-    per SM for DOP853, ``lanes_d42`` in {0 (auto), 7, 14, 12 (paired warps)} lanes per 42-dim
+    per SM for DOP853, ``lanes_d42`` in {0 (auto), 7, 14, 12 (paired warps), 18 (three warps)} lanes per 42-dim
     trajectory, ``sm_capacity`` the warps an SM serves at full speed in the
     layout cost models (a float, default 3.0), ``refine_pool_mb`` the largest
     crossing-record pool of a single-pass call (larger ones refine inline).  Usable as a context manager

@@ -335,7 +335,9 @@ int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_ma
  * without an event: a state warp with the Hessian and an STM warp per five
  * trajectories, ~0.6x the per-step latency of 7 for RK8; blocks of one pair,
  * or of two pairs with HG_TUNE_BLOCK_THREADS 128; other calls then use 7),
- * 0 = automatic (the default).
+ * 18 (three warps, single-pass DOP853 without an event: the STM of five
+ * trajectories on two warps of half columns; fixed RK and other calls then
+ * use 7), 0 = automatic (the default).
  * HG_TUNE_SM_CAPACITY: the layout cost models' FP64 capacity of an SM, in
  * tenths of a warp's demand (default 30: three warps run at full speed).
  * HG_TUNE_REFINE_POOL_MB: largest record pool (MB, default 8192) a single-pass

@@ -81,13 +81,15 @@ def _dop(gpu, lanes, y0, t0, tf, **kw):
         return gpu.propagate_dop853(y0, t0, tf, MU, flip=(36, 42) if kw.get("fwd", 1) == -1 else None, **kw)
 
 
+@pytest.mark.parametrize("lanes", [12, 18])
 @pytest.mark.parametrize("n", [1, 6, 11])
 @pytest.mark.parametrize("fwd", [1, -1])
 @pytest.mark.parametrize("m,last", [(2, False), (37, False), (500, True)])
-def test_pair_dop853_dense_matches_oracle(gpu, dev_oracle, n, fwd, m, last):
+def test_pair_dop853_dense_matches_oracle(gpu, dev_oracle, lanes, n, fwd, m, last):
+    # 12: paired warps; 18: three warps (state + two half-column STM warps)
     y0 = W.stm_fixed_batch(64, seed=11)[:n]
     tf = np.linspace(0.4, 1.6, n)  # per-trajectory spans
-    res = _dop(gpu, 12, y0, 0.0, tf, rtol=1e-11, atol=1e-11, fwd=fwd, n_samples=m, sample_last_only=last)
+    res = _dop(gpu, lanes, y0, 0.0, tf, rtol=1e-11, atol=1e-11, fwd=fwd, n_samples=m, sample_last_only=last)
     out = _np(res.samples)
     assert np.all(_np(res.status) == _lib.HG_OK)
     for i in range(n):
@@ -107,10 +109,11 @@ def test_pair_dop853_many_equals_single_warp_layouts(gpu):
     y0 = W.stm_fixed_batch(1003, seed=12)
     tf = np.random.default_rng(3).uniform(0.2, 2.0, len(y0))
     fields = ("y_end", "t_end", "n_accept", "n_reject", "status", "samples")
-    res = {lanes: _dop(gpu, lanes, y0, 0.0, tf, n_samples=25) for lanes in (12, 7, 14)}
+    res = {lanes: _dop(gpu, lanes, y0, 0.0, tf, n_samples=25) for lanes in (12, 18, 7, 14)}
     for f in fields:
         assert np.array_equal(_np(getattr(res[12], f)), _np(getattr(res[7], f))), f
         assert np.array_equal(_np(getattr(res[12], f)), _np(getattr(res[14], f))), f
+        assert np.array_equal(_np(getattr(res[18], f)), _np(getattr(res[7], f))), f
 
 
 def test_pair_dop853_step_budget_status(gpu):
@@ -120,9 +123,11 @@ def test_pair_dop853_step_budget_status(gpu):
     y0[4, 36:] = [-MU, 0.0, 0.0, 0.0, 0.0, 0.0]
     for max_steps in (7, 2000):
         r12 = _dop(gpu, 12, y0, 0.0, 1.0, max_steps=max_steps)
+        r18 = _dop(gpu, 18, y0, 0.0, 1.0, max_steps=max_steps)
         r7 = _dop(gpu, 7, y0, 0.0, 1.0, max_steps=max_steps)
         for f in ("status", "n_accept", "n_reject", "t_end"):
             assert np.array_equal(_np(getattr(r12, f)), _np(getattr(r7, f))), f
+            assert np.array_equal(_np(getattr(r18, f)), _np(getattr(r7, f))), f
         ok = _np(r12.status) == _lib.HG_OK
         assert np.array_equal(_np(r12.y_end)[ok], _np(r7.y_end)[ok])
         st = _np(r12.status)
