@@ -33,7 +33,7 @@ EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg
             "hg_propagate_dop853_scheduled", "hg_get_counter", "hg_radius_best", "hg_nearest_neighbor",
             "hg_newton_opts_default", "hg_correct_halo", "hg_serve_config_default", "hg_serve_create",
             "hg_serve_destroy", "hg_serve_submit", "hg_serve_poll", "hg_serve_wait", "hg_serve_fetch",
-            "hg_serve_cancel", "hg_serve_stats", "hg_selftest_bounded_wait")
+            "hg_serve_cancel", "hg_serve_stats", "hg_selftest_bounded_wait", "hg_host_pow")
 HG_COUNTER_KERNEL_LAUNCHES = 1
 HG_RUNNING = -1
 HG_TUNE_BLOCK_THREADS = 1
@@ -162,6 +162,8 @@ def load(build_if_missing=True):
         L.hg_get_counter.argtypes = [_P, C.c_int, C.POINTER(C.c_longlong)]
         L.hg_selftest_bounded_wait.argtypes = [_P, C.c_int, _P, _P]
         L.hg_selftest_bounded_wait.restype = C.c_int
+        L.hg_host_pow.argtypes = [C.c_longlong, _P, C.c_double, _P]
+        L.hg_host_pow.restype = None
         L.hg_get_counter.restype = C.c_int
         L.hg_probe_fp64_peak.argtypes = [_P, C.POINTER(C.c_double)]
         L.hg_probe_fp64_peak.restype = C.c_int

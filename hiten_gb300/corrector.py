@@ -24,11 +24,12 @@ STM integration and one batched event integration per Armijo level, over the
 orbits still active.  The small 2x2 linear algebra runs in numpy exactly as
 the reference does (stacked LAPACK calls give the same bits as single calls).
 """
-import math
+import ctypes as C
 from dataclasses import dataclass
 
 import numpy as np
 
+from . import _lib
 from . import propagate as P
 from .workloads import identity_stm_state
 
@@ -91,9 +92,13 @@ class GpuShootingBackend:
 def _libm_pow(a, e):
     """Elementwise C `pow`: what the reference's numpy-scalar `**` computes
     (numpy's array `**` takes other paths: `x*x` for 2, SIMD kernels for
-    fractional exponents, which differ in the last bit)."""
+    fractional exponents, which differ in the last bit); one call into the
+    library's host loop (`hg_host_pow`) instead of a Python call per element."""
     flat = np.ascontiguousarray(a, dtype=np.float64).ravel()
-    return np.fromiter((math.pow(v, e) for v in flat.tolist()), dtype=np.float64, count=flat.size).reshape(a.shape)
+    out = np.empty_like(flat)
+    if flat.size:
+        _lib.load().hg_host_pow(flat.size, flat.ctypes.data_as(C.c_void_p), float(e), out.ctypes.data_as(C.c_void_p))
+    return out.reshape(np.shape(a))
 
 
 def halo_quadratic_term(x_ev, Phi, mu):

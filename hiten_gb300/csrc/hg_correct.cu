@@ -170,6 +170,11 @@ bool solve2(const double J[4], const double b[2], double x[2]) {
 
 extern "C" {
 
+void hg_host_pow(long long n, const double* x, double e, double* out) {
+  if (n <= 0 || !x || !out) return;
+  for (long long i = 0; i < n; ++i) out[i] = pow(x[i], e);
+}
+
 void hg_newton_opts_default(hg_newton_opts* o) {
   if (!o) return;
   o->tol = 1e-12;

@@ -366,6 +366,15 @@ int hg_get_tuning(hg_handle* h, int key, int* value);
 #define HG_COUNTER_KERNEL_LAUNCHES 1
 int hg_get_counter(hg_handle* h, int key, long long* value);
 
+/* Host helper: out[i] = pow(x[i], e) through the C library's pow, i < n
+ * (host arrays).  The reference's numpy-scalar `**` calls C pow (numpy's
+ * array `**` takes other code paths that differ in the last bit); the
+ * Python corrector uses this to evaluate its batched quadratic term with
+ * the reference's bits.  Synchronous, no device work.
+ * Replaces: the scalar `**` of types/services/orbits.py:917-948
+ * (_halo_quadratic_term), evaluated per orbit in the reference. */
+void hg_host_pow(long long n, const double* x, double e, double* out);
+
 /* Self-test of the bounded inter-warp wait the paired 42-dim layouts use
  * (every hand-off wait gives up after a time limit and the kernel reports
  * HG_SYNC_TIMEOUT instead of hanging): one warp waits limit_ms on a barrier
