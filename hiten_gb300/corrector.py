@@ -50,6 +50,10 @@ class HaloCorrectionOptions:
     alpha_reduction: float = 0.5
     min_alpha: float = 1e-4
     armijo_c: float = 0.1
+    # Armijo trials evaluated per round and orbit (the next step fractions in
+    # one propagation; results unchanged): None = as many as fill the
+    # backend's latency-bound propagation size (1 for backends without one)
+    trials_per_round: int = None
     cond_threshold: float = 1e8
     event_rtol: float = 1e-12
     event_atol: float = 1e-12
@@ -58,13 +62,19 @@ class HaloCorrectionOptions:
 
 
 class GpuShootingBackend:
-    """The two propagations single shooting needs, batched on the GPU."""
+    """The two propagations single shooting needs, batched on the GPU.
+
+    ``spec_traj``: the event-leg size that still runs at the per-step latency
+    floor (six lanes per trajectory, one warp per SM sub-partition)."""
 
     def __init__(self, mu, options=None, device=None):
         self.mu = float(mu)
         self.o = options or HaloCorrectionOptions()
         self.device = device
         self.launches = 0
+        import torch
+        dev = P._device(device)
+        self.spec_traj = 20 * torch.cuda.get_device_properties(dev).multi_processor_count
 
     def events(self, x_full):
         """First y = 0 crossing of every state: (t_event, x_event, found)."""
@@ -214,30 +224,52 @@ def correct_halo(guesses, mu, options=None, backend=None, device=None):
         failed = np.zeros(active.size, dtype=bool)
         while pending.any():
             idx = np.nonzero(pending)[0]
-            trial = x0p[idx] + alpha[idx, None] * delta[idx]
-            rt, nt, tt, xt, ft = residual(trial, active[idx])
-            # an evaluation without a crossing is a failed residual: try a smaller step
-            ok = ft & (nt <= (1.0 - o.armijo_c * alpha[idx]) * rn[idx])
-            # accepted trials
-            a_i = idx[ok]
-            for dst, src in zip(new, (trial, nt, rt, tt, xt)):
-                dst[a_i] = src[ok]
-            pending[a_i] = False
-            # rejected ones: remember the best finite trial, halve alpha
-            rej = ~ok
-            r_i = idx[rej]
-            better = ft[rej] & (nt[rej] < best[1][r_i])
-            b_i = r_i[better]
-            best[2][b_i] = alpha[b_i]
-            for dst, src in zip((best[0], best[1], best[3], best[4], best[5]), (trial, nt, rt, tt, xt)):
-                dst[b_i] = src[rej][better]
-            alpha[r_i] *= o.alpha_reduction
-            s_i = r_i[alpha[r_i] < o.min_alpha]
-            pending[s_i] = False
-            g_i = s_i[best[2][s_i] > 0]
-            for dst, src in zip(new, (best[0], best[1], best[3], best[4], best[5])):
-                dst[g_i] = src[g_i]
-            failed[s_i[best[2][s_i] <= 0]] = True
+            # the next S step fractions of every pending orbit in one
+            # propagation (alpha, alpha r, ... by the same repeated products),
+            # consumed below in the sequential order
+            S = o.trials_per_round or max(1, min(8, getattr(be, "spec_traj", 1) // idx.size))
+            A = np.empty((idx.size, S))
+            a = alpha[idx].copy()
+            for j in range(S):
+                A[:, j] = a
+                a = a * o.alpha_reduction
+            trials = x0p[idx][:, None, :] + A[:, :, None] * delta[idx][:, None, :]
+            rt, nt, tt, xt, ft = residual(trials.reshape(-1, 2), np.repeat(active[idx], S))
+            rt, nt, tt, ft = rt.reshape(idx.size, S, 2), nt.reshape(idx.size, S), tt.reshape(idx.size, S), \
+                ft.reshape(idx.size, S)
+            xt = xt.reshape(idx.size, S, 6)
+            deciding = np.ones(idx.size, dtype=bool)
+            for j in range(S):
+                u = np.nonzero(deciding)[0]
+                if u.size == 0:
+                    break
+                q = idx[u]
+                trial, nj, rj, tj, xj, fj = trials[u, j], nt[u, j], rt[u, j], tt[u, j], xt[u, j], ft[u, j]
+                # an evaluation without a crossing is a failed residual: try a smaller step
+                ok = fj & (nj <= (1.0 - o.armijo_c * alpha[q]) * rn[q])
+                # accepted trials
+                a_i = q[ok]
+                for dst, src in zip(new, (trial, nj, rj, tj, xj)):
+                    dst[a_i] = src[ok]
+                pending[a_i] = False
+                deciding[u[ok]] = False
+                # rejected ones: remember the best finite trial, halve alpha
+                rej = ~ok
+                r_i = q[rej]
+                better = fj[rej] & (nj[rej] < best[1][r_i])
+                b_i = r_i[better]
+                best[2][b_i] = alpha[b_i]
+                for dst, src in zip((best[0], best[1], best[3], best[4], best[5]), (trial, nj, rj, tj, xj)):
+                    dst[b_i] = src[rej][better]
+                alpha[r_i] *= o.alpha_reduction
+                stop = alpha[r_i] < o.min_alpha
+                s_i = r_i[stop]
+                pending[s_i] = False
+                deciding[u[rej][stop]] = False
+                g_i = s_i[best[2][s_i] > 0]
+                for dst, src in zip(new, (best[0], best[1], best[3], best[4], best[5])):
+                    dst[g_i] = src[g_i]
+                failed[s_i[best[2][s_i] <= 0]] = True
         status[active[failed]] = STATUS_LINE_SEARCH
         iters[active[failed]] = k
         keep = ~failed

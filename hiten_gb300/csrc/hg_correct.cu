@@ -23,12 +23,9 @@
 
 namespace {
 
+// A view into the call's single device allocation (Shooter::arena).
 struct DevBuf {
   void* p = nullptr;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
-  bool alloc(size_t bytes) { return cudaMalloc(&p, bytes ? bytes : 8) == cudaSuccess; }
   double* d() const { return (double*)p; }
   int* i() const { return (int*)p; }
 };
@@ -41,15 +38,36 @@ struct Shooter {
   int cap;
   // event leg (6-dim), STM leg (42-dim)
   DevBuf y6, ye6, te, ht, hy, nh, na, nr, st, y42, ye42, te42, tm, smp, na42, nr42, st42;
+  void* arena = nullptr;  // one cudaMalloc per call, carved into the buffers above
   std::vector<double> hbuf;
   std::vector<int> ibuf;
 
+  ~Shooter() {
+    if (arena) cudaFree(arena);
+  }
+
   bool init() {
     const size_t n = (size_t)cap;
-    return y6.alloc(6 * n * 8) && ye6.alloc(6 * n * 8) && te.alloc(n * 8) && ht.alloc(n * 8) &&
-           hy.alloc(6 * n * 8) && nh.alloc(n * 4) && na.alloc(n * 4) && nr.alloc(n * 4) && st.alloc(n * 4) &&
-           y42.alloc(42 * n * 8) && ye42.alloc(42 * n * 8) && te42.alloc(n * 8) && tm.alloc(n * 8) &&
-           smp.alloc(42 * n * 8) && na42.alloc(n * 4) && nr42.alloc(n * 4) && st42.alloc(n * 4);
+    struct Part {
+      DevBuf* b;
+      size_t bytes;
+    } parts[] = {{&y6, 6 * n * 8},   {&ye6, 6 * n * 8},   {&te, n * 8},      {&ht, n * 8},     {&hy, 6 * n * 8},
+                 {&nh, n * 4},       {&na, n * 4},        {&nr, n * 4},      {&st, n * 4},     {&y42, 42 * n * 8},
+                 {&ye42, 42 * n * 8}, {&te42, n * 8},     {&tm, n * 8},      {&smp, 42 * n * 8}, {&na42, n * 4},
+                 {&nr42, n * 4},     {&st42, n * 4}};
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    size_t total = 0;
+    for (const Part& q : parts) total += up(q.bytes ? q.bytes : 8);
+    if (cudaMalloc(&arena, total) != cudaSuccess) {
+      arena = nullptr;
+      return false;
+    }
+    size_t off = 0;
+    for (const Part& q : parts) {
+      q.b->p = (char*)arena + off;
+      off += up(q.bytes ? q.bytes : 8);
+    }
+    return true;
   }
 
   // First y = 0 crossing of every state x (M x 6, row-major): t_event = 1e-12 +
@@ -247,6 +265,15 @@ int hg_correct_halo(hg_handle* h, double mu, int N, double* x, long long ld, dou
     return HG_OK;
   };
 
+  // trajectories an event leg takes at its per-step latency floor (six lanes
+  // per trajectory, one warp per SM sub-partition: 4 x SMs x 5), at most N
+  // (the buffers' capacity)
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                 cudaSuccess || sms < 1)
+    sms = 1;
+  const int spec_traj = std::max(1, std::min(N, 20 * sms));
+  constexpr int kMaxSpec = 8;
   std::vector<int> active(N);
   for (int i = 0; i < N; ++i) active[i] = i;
   Res cur;
@@ -339,59 +366,76 @@ int hg_correct_halo(hg_handle* h, double mu, int N, double* x, long long ld, dou
     std::vector<double> new_p = pa, new_n = cur.rn, new_r = cur.r, new_t = cur.tev, new_x = cur.xev;
     std::vector<char> pending(M, 1), failed(M, 0);
     for (;;) {
-      std::vector<int> idx, rows;
+      std::vector<int> idx;
       for (int q = 0; q < M; ++q)
-        if (pending[q]) {
-          idx.push_back(q);
-          rows.push_back(active[q]);
-        }
+        if (pending[q]) idx.push_back(q);
       if (idx.empty()) break;
-      std::vector<double> trial(idx.size() * 2);
-      for (size_t u = 0; u < idx.size(); ++u) {
+      // Each round evaluates the next S step fractions alpha, alpha r, ...,
+      // alpha r^(S-1) of every pending orbit in one propagation: the event
+      // legs of up to spec_traj trajectories run at their per-step latency
+      // floor, so the extra trials come almost free, and the decisions below
+      // consume them in the sequential order (each trial is the same
+      // computation whenever it runs): the results are those of one trial per
+      // round, in fewer rounds.
+      const int P = (int)idx.size();
+      const int S = std::max(1, std::min(kMaxSpec, spec_traj / P));
+      std::vector<int> rows((size_t)P * S);
+      std::vector<double> trial((size_t)P * S * 2), ta((size_t)P * S);
+      for (int u = 0; u < P; ++u) {
         const int q = idx[u];
-        trial[2 * u] = pa[2 * q] + alpha[q] * delta[2 * q];
-        trial[2 * u + 1] = pa[2 * q + 1] + alpha[q] * delta[2 * q + 1];
+        double a = alpha[q];
+        for (int j = 0; j < S; ++j) {
+          const size_t v = (size_t)u * S + j;
+          rows[v] = active[q];
+          ta[v] = a;
+          trial[2 * v] = pa[2 * q] + a * delta[2 * q];
+          trial[2 * v + 1] = pa[2 * q + 1] + a * delta[2 * q + 1];
+          a *= o.alpha_reduction;
+        }
       }
       Res T;
       rc = residual_of(trial, rows, T);
       if (rc != HG_OK) return rc;
-      for (size_t u = 0; u < idx.size(); ++u) {
+      for (int u = 0; u < P; ++u) {
         const int q = idx[u];
-        const bool ft = T.found[u];
-        if (ft && T.rn[u] <= (1.0 - o.armijo_c * alpha[q]) * cur.rn[q]) {
-          new_p[2 * q] = trial[2 * u];
-          new_p[2 * q + 1] = trial[2 * u + 1];
-          new_n[q] = T.rn[u];
-          new_r[2 * q] = T.r[2 * u];
-          new_r[2 * q + 1] = T.r[2 * u + 1];
-          new_t[q] = T.tev[u];
-          memcpy(&new_x[(size_t)q * 6], &T.xev[u * 6], 6 * 8);
-          pending[q] = 0;
-          continue;
-        }
-        if (ft && T.rn[u] < best_n[q]) {
-          best_p[2 * q] = trial[2 * u];
-          best_p[2 * q + 1] = trial[2 * u + 1];
-          best_n[q] = T.rn[u];
-          best_a[q] = alpha[q];
-          best_r[2 * q] = T.r[2 * u];
-          best_r[2 * q + 1] = T.r[2 * u + 1];
-          best_t[q] = T.tev[u];
-          memcpy(&best_x[(size_t)q * 6], &T.xev[u * 6], 6 * 8);
-        }
-        alpha[q] *= o.alpha_reduction;
-        if (alpha[q] < o.min_alpha) {
-          pending[q] = 0;
-          if (best_a[q] > 0) {
-            new_p[2 * q] = best_p[2 * q];
-            new_p[2 * q + 1] = best_p[2 * q + 1];
-            new_n[q] = best_n[q];
-            new_r[2 * q] = best_r[2 * q];
-            new_r[2 * q + 1] = best_r[2 * q + 1];
-            new_t[q] = best_t[q];
-            memcpy(&new_x[(size_t)q * 6], &best_x[(size_t)q * 6], 6 * 8);
-          } else {
-            failed[q] = 1;
+        for (int j = 0; j < S && pending[q]; ++j) {
+          const size_t v = (size_t)u * S + j;
+          const bool ft = T.found[v];
+          if (ft && T.rn[v] <= (1.0 - o.armijo_c * alpha[q]) * cur.rn[q]) {
+            new_p[2 * q] = trial[2 * v];
+            new_p[2 * q + 1] = trial[2 * v + 1];
+            new_n[q] = T.rn[v];
+            new_r[2 * q] = T.r[2 * v];
+            new_r[2 * q + 1] = T.r[2 * v + 1];
+            new_t[q] = T.tev[v];
+            memcpy(&new_x[(size_t)q * 6], &T.xev[v * 6], 6 * 8);
+            pending[q] = 0;
+            break;
+          }
+          if (ft && T.rn[v] < best_n[q]) {
+            best_p[2 * q] = trial[2 * v];
+            best_p[2 * q + 1] = trial[2 * v + 1];
+            best_n[q] = T.rn[v];
+            best_a[q] = alpha[q];
+            best_r[2 * q] = T.r[2 * v];
+            best_r[2 * q + 1] = T.r[2 * v + 1];
+            best_t[q] = T.tev[v];
+            memcpy(&best_x[(size_t)q * 6], &T.xev[v * 6], 6 * 8);
+          }
+          alpha[q] *= o.alpha_reduction;
+          if (alpha[q] < o.min_alpha) {
+            pending[q] = 0;
+            if (best_a[q] > 0) {
+              new_p[2 * q] = best_p[2 * q];
+              new_p[2 * q + 1] = best_p[2 * q + 1];
+              new_n[q] = best_n[q];
+              new_r[2 * q] = best_r[2 * q];
+              new_r[2 * q + 1] = best_r[2 * q + 1];
+              new_t[q] = best_t[q];
+              memcpy(&new_x[(size_t)q * 6], &best_x[(size_t)q * 6], 6 * 8);
+            } else {
+              failed[q] = 1;
+            }
           }
         }
       }

@@ -103,8 +103,11 @@ def scalar_reference(be, guesses, o):
     return out
 
 
+@pytest.mark.parametrize("trials", [None, 1, 3, 8])
 @pytest.mark.parametrize("seed", [0, 1, 2])
-def test_batched_armijo_matches_per_orbit_loop(seed, monkeypatch):
+def test_batched_armijo_matches_per_orbit_loop(seed, trials, monkeypatch):
+    """trials: step fractions evaluated per round and orbit (speculative
+    rounds must decide exactly as one trial per round)."""
     monkeypatch.setattr(C, "halo_quadratic_term", lambda x_ev, Phi, mu: np.zeros((x_ev.shape[0], 2, 2)))
     rng = np.random.default_rng(seed)
     n = 40
@@ -117,7 +120,7 @@ def test_batched_armijo_matches_per_orbit_loop(seed, monkeypatch):
     guesses[:, 0] = pstar[:, 0] + rng.uniform(-1, 1, n) * window * 0.9
     guesses[:, 4] = pstar[:, 1] + rng.uniform(-5e-3, 5e-3, n)
     guesses[:, 1] = np.arange(n) * 1e-6
-    o = C.HaloCorrectionOptions(max_attempts=12)
+    o = C.HaloCorrectionOptions(max_attempts=12, trials_per_round=trials)
     got = C.correct_halo(guesses, 0.0121505856, options=o, backend=FakeBackend(pstar, A, c, window, jac_scale))
     ref = scalar_reference(FakeBackend(pstar, A, c, window, jac_scale), guesses, o)
     statuses = set()

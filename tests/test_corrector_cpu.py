@@ -16,11 +16,13 @@ def halo():
     return np.load(os.path.join(GOLDEN, "halo.npz"))
 
 
-def test_corrector_logic_reproduces_reference(oracle, halo):
+@pytest.mark.parametrize("trials", [None, 4])
+def test_corrector_logic_reproduces_reference(oracle, halo, trials):
     from hiten_gb300 import corrector
     mu = float(halo["mu"])
     be = OracleShootingBackend(oracle, mu, oracle.MODE_PYTHON)
-    res = corrector.correct_halo(halo["guess"], mu, backend=be)
+    res = corrector.correct_halo(halo["guess"], mu, options=corrector.HaloCorrectionOptions(trials_per_round=trials),
+                                 backend=be)
     oracle.set_mode(oracle.MODE_PYTHON)
     assert np.all(res.status == 0)
     assert np.array_equal(res.iterations, halo["iterations"])
