@@ -406,10 +406,26 @@ def bench_connections(args):
         torch.cuda.synchronize()
         ts.append(time.perf_counter() - t0)
     sec = statistics.median(ts)
+    # the four all-pairs searches alone (device arrays resident, CUDA events)
+    from hiten_gb300.connections import GpuSectionMatcher
+    m = GpuSectionMatcher()
+    R = float(max(np.abs(pu).max(), np.abs(ps).max()))
+    qu, qs = torch.as_tensor(pu, device="cuda"), torch.as_tensor(ps, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    search = []
+    for _ in range(3):
+        ev[0].record()
+        m.radius_best(qu, qs, 1e-4, R)
+        m.radius_best(qs, qu, 1e-4, R)
+        m.nearest(qu, R)
+        m.nearest(qs, R)
+        ev[1].record()
+        torch.cuda.synchronize()
+        search.append(ev[0].elapsed_time(ev[1]))
     pair_tests = 4.0 * n * n
     _line("connections, 65536 x 65536 section points, eps 1e-4", "pair tests/s", pair_tests / sec, "pairs/s",
           sec * 1e3, {"points_u": n, "points_s": n, "eps": 1e-4}, connections=len(res),
-          pairs_considered=meta.get("pairs_considered", 0))
+          pairs_considered=meta.get("pairs_considered", 0), gpu_search_ms=statistics.median(search))
 
 
 EXTRA = {"fixed_stm": bench_fixed_stm, "section": bench_section, "synodic_detect": bench_synodic_detect,

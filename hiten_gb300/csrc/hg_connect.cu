@@ -25,25 +25,58 @@ namespace {
 constexpr int kTile = 256;
 constexpr int kBlock = 128;
 
-struct P2 {
-  double x, y;
+// One tile of reference points in shared memory: FP32 copies for the screen,
+// the FP64 values for the exact decisions.
+struct Tile {
+  float2 f[kTile];
+  double2 d[kTile];
 };
 
-__device__ __forceinline__ float err_bound(float d2f, float adx, float ady, float R, float R2c) {
-  return 0x1p-20f * (d2f + R * (adx + ady)) + R2c;
+__device__ __forceinline__ void load_tile(Tile& T, const double* __restrict__ x, const double* __restrict__ y, int base,
+                                          int n) {
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const double a = x[base + t], b = y[base + t];
+    T.d[t] = make_double2(a, b);
+    T.f[t] = make_float2((float)a, (float)b);
+  }
+}
+
+// (d2, j) lexicographic minimum of two candidates (j < 0: none).  A scan in
+// increasing j that keeps the first strict minimum ends at the lowest index
+// of the minimal distance, which is this minimum over any split of the scan.
+__device__ __forceinline__ void take_best(double& bd, int& bj, double d2, int j) {
+  if (j >= 0 && (bj < 0 || d2 < bd || (d2 == bd && j < bj))) {
+    bd = d2;
+    bj = j;
+  }
+}
+
+// The S lanes of a query are consecutive lanes of one warp: lane s of the
+// query scans tile entries s, s + S, s + 2S, ...; every lane of the warp
+// reaches the shuffles (no early exit).
+template <int S>
+__device__ __forceinline__ void combine_best(double& bd, int& bj) {
+#pragma unroll
+  for (int o = 1; o < S; o <<= 1) {
+    const double d2 = __shfl_xor_sync(0xFFFFFFFFu, bd, o);
+    const int j = __shfl_xor_sync(0xFFFFFFFFu, bj, o);
+    take_best(bd, bj, d2, j);
+  }
 }
 
 // For each query point: number of reference points within eps (exact FP64
 // test), and the nearest of them (strict <: the lowest index wins ties).
-__global__ void __launch_bounds__(kBlock) radius_best_kernel(int nq, const double* __restrict__ qx,
+template <int S>
+__global__ void __launch_bounds__(kBlock, 16) radius_best_kernel(int nq, const double* __restrict__ qx,
                                                               const double* __restrict__ qy, int nr,
                                                               const double* __restrict__ rx,
                                                               const double* __restrict__ ry, double r2, float T,
                                                               int* __restrict__ count, int* __restrict__ best_idx,
                                                               double* __restrict__ best_d2) {
-  __shared__ float sfx[kTile], sfy[kTile];
-  __shared__ double sdx[kTile], sdy[kTile];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ Tile tile;
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = (int)(g % S);
+  const long long i = g / S;
   const bool active = i < nq;
   const double xi = active ? qx[i] : 0.0, yi = active ? qy[i] : 0.0;
   const float xf = (float)xi, yf = (float)yi;
@@ -52,19 +85,15 @@ __global__ void __launch_bounds__(kBlock) radius_best_kernel(int nq, const doubl
   for (int base = 0; base < nr; base += kTile) {
     const int n = min(kTile, nr - base);
     __syncthreads();
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-      const double a = rx[base + t], b = ry[base + t];
-      sdx[t] = a;
-      sdy[t] = b;
-      sfx[t] = (float)a;
-      sfy[t] = (float)b;
-    }
+    load_tile(tile, rx, ry, base, n);
     __syncthreads();
     if (active) {
-      for (int t = 0; t < n; ++t) {
-        const float dxf = xf - sfx[t], dyf = yf - sfy[t];
+      for (int t = s; t < n; t += S) {
+        const float2 pf = tile.f[t];
+        const float dxf = xf - pf.x, dyf = yf - pf.y;
         if (fabsf(dxf) > T || fabsf(dyf) > T) continue;
-        const double dx = xi - sdx[t], dy = yi - sdy[t];
+        const double2 pd = tile.d[t];
+        const double dx = xi - pd.x, dy = yi - pd.y;
         const double d2 = dx * dx + dy * dy;
         if (d2 <= r2) {
           ++c;
@@ -76,64 +105,112 @@ __global__ void __launch_bounds__(kBlock) radius_best_kernel(int nq, const doubl
       }
     }
   }
-  if (active) {
+#pragma unroll
+  for (int o = 1; o < S; o <<= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+  combine_best<S>(bd, bj);
+  if (active && s == 0) {
     count[i] = c;
     best_idx[i] = bj;
     best_d2[i] = bj < 0 ? 0.0 : bd;
   }
 }
 
+// Pass-1 screen of the nearest-neighbour search.  With D the smallest FP32
+// distance d2_f of the query (pass 0), the true minimum is at most
+// M = D + E(D), where E(x) = 2^-20 (x + R (sqrt(2x)/(1 - u) + 2^-62)) + R2c
+// bounds e for any pair with d2_f = x (|dx_f| + |dy_f| <= sqrt(2 (dx_f^2 +
+// dy_f^2)) <= sqrt(2 d2_f)/(1 - u), the 2^-62 covering FP32 underflow of the
+// squares).  A point can be the exact minimiser only if d2_f - E(d2_f) <= M,
+// i.e. sqrt(d2_f) <= (c1 + sqrt(c1^2 + 4a(c0 + M)))/(2a) with a = 1 - 2^-20,
+// c1 = 2^-20 R sqrt2/(1 - u), c0 = 2^-82 R + R2c.  Everything is evaluated
+// rounding upward (each quantity only grows), so the returned FP32 threshold
+// admits every possible minimiser.
+__device__ __forceinline__ float nearest_threshold(float D, double R, double R2c) {
+  if (!(D < INFINITY)) return INFINITY;
+  const double u1 = 1.0 / (1.0 - 0x1p-24) * (1.0 + 0x1p-50);  // >= 1/(1 - u)
+  const double d = (double)D;
+  const double c1 = __dmul_ru(__dmul_ru(0x1p-20 * R, 1.4142135623730952), u1);  // sqrt2 rounded up
+  const double c0 = __dadd_ru(0x1p-82 * R, R2c);
+  const double E = __dadd_ru(__dadd_ru(0x1p-20 * d, __dmul_ru(c1, __dsqrt_ru(d))), c0);
+  const double M = __dadd_ru(d, E);
+  const double a = 1.0 - 0x1p-20;
+  const double disc = __dadd_ru(__dmul_ru(c1, c1), __dmul_ru(4.0 * a, __dadd_ru(c0, M)));
+  const double smax = __ddiv_ru(__dadd_ru(c1, __dsqrt_ru(disc)), 2.0 * a);
+  return __double2float_ru(__dmul_ru(smax, smax));
+}
+
 // Nearest neighbour of every point within its own set (excluding itself;
-// strict <, the lowest index wins ties).  Pass 1 finds m = min_j (d2_f + e),
-// an upper bound on the true minimum; pass 2 decides in FP64 among the j
-// with d2_f - e <= m, which contain every j whose true distance can be
-// minimal.
-__global__ void __launch_bounds__(kBlock) nearest_kernel(int n, const double* __restrict__ px,
-                                                          const double* __restrict__ py, float R, float R2c,
+// strict <, the lowest index wins ties).  Pass 0 finds the smallest FP32
+// distance, pass 1 decides in FP64 among the points under the threshold
+// above, which contain every point whose true distance can be minimal.
+template <int S>
+__global__ void __launch_bounds__(kBlock, 16) nearest_kernel(int n, const double* __restrict__ px,
+                                                          const double* __restrict__ py, double R, double R2c,
                                                           int* __restrict__ out) {
-  __shared__ float sfx[kTile], sfy[kTile];
-  __shared__ double sdx[kTile], sdy[kTile];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ Tile tile;
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = (int)(g % S);
+  const long long i = g / S;
   const bool active = i < n;
   const double xi = active ? px[i] : 0.0, yi = active ? py[i] : 0.0;
   const float xf = (float)xi, yf = (float)yi;
-  float m = INFINITY;
-  for (int pass = 0; pass < 2; ++pass) {
-    int bj = -1;
-    double bd = 1e300;
-    for (int base = 0; base < n; base += kTile) {
-      const int cnt = min(kTile, n - base);
-      __syncthreads();
-      for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-        const double a = px[base + t], b = py[base + t];
-        sdx[t] = a;
-        sdy[t] = b;
-        sfx[t] = (float)a;
-        sfy[t] = (float)b;
+  float D = INFINITY;
+  for (int base = 0; base < n; base += kTile) {
+    const int cnt = min(kTile, n - base);
+    __syncthreads();
+    load_tile(tile, px, py, base, cnt);
+    __syncthreads();
+    if (active) {
+      for (int t = s; t < cnt; t += S) {
+        if (base + t == i) continue;
+        const float2 pf = tile.f[t];
+        const float dxf = xf - pf.x, dyf = yf - pf.y;
+        D = fminf(D, __fadd_rn(__fmul_rn(dxf, dxf), __fmul_rn(dyf, dyf)));
       }
-      __syncthreads();
-      if (active) {
-        for (int t = 0; t < cnt; ++t) {
-          const int j = base + t;
-          if (j == i) continue;
-          const float dxf = xf - sfx[t], dyf = yf - sfy[t];
-          const float d2f = __fadd_rn(__fmul_rn(dxf, dxf), __fmul_rn(dyf, dyf));
-          const float e = err_bound(d2f, fabsf(dxf), fabsf(dyf), R, R2c);
-          if (pass == 0) {
-            m = fminf(m, __fadd_ru(d2f, e));
-          } else if (__fsub_rd(d2f, e) <= m) {
-            const double dx = xi - sdx[t], dy = yi - sdy[t];
-            const double d2 = dx * dx + dy * dy;
-            if (d2 < bd) {
-              bd = d2;
-              bj = j;
-            }
-          }
+    }
+  }
+#pragma unroll
+  for (int o = 1; o < S; o <<= 1) D = fminf(D, __shfl_xor_sync(0xFFFFFFFFu, D, o));
+  const float thr = nearest_threshold(D, R, R2c);
+  int bj = -1;
+  double bd = 0.0;
+  for (int base = 0; base < n; base += kTile) {
+    const int cnt = min(kTile, n - base);
+    __syncthreads();
+    load_tile(tile, px, py, base, cnt);
+    __syncthreads();
+    if (active) {
+      for (int t = s; t < cnt; t += S) {
+        const float2 pf = tile.f[t];
+        const float dxf = xf - pf.x, dyf = yf - pf.y;
+        if (!(__fadd_rn(__fmul_rn(dxf, dxf), __fmul_rn(dyf, dyf)) <= thr) || base + t == i) continue;
+        const double2 pd = tile.d[t];
+        const double dx = xi - pd.x, dy = yi - pd.y;
+        const double d2 = dx * dx + dy * dy;
+        if (bj < 0 ? d2 < 1e300 : d2 < bd) {
+          bd = d2;
+          bj = base + t;
         }
       }
     }
-    if (pass == 1 && active) out[i] = bj;
   }
+  combine_best<S>(bd, bj);
+  if (active && s == 0) out[i] = bj;
+}
+
+// Lanes per query: the largest of 8, 4, 2, 1 whose grid still fits in one
+// wave of resident blocks (more lanes per query shorten each lane's scan;
+// a second partial wave would cost a whole extra scan).
+template <class K>
+int lanes_per_query(K k8, long long n) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k8, kBlock, 0) != cudaSuccess)
+    return 1;
+  const long long resident = (long long)sms * per_sm * kBlock;
+  for (int S = 8; S > 1; S >>= 1)
+    if (n * S <= resident) return S;
+  return 1;
 }
 
 int check(const char* what) {
@@ -152,8 +229,17 @@ int hg_radius_best(int nq, const double* qx, const double* qy, int nr, const dou
   if (!qx || !qy || !count || !best_idx || !best_d2 || (nr > 0 && (!rx || !ry))) return HG_ERR_ARGS;
   const double T = (eps + 0x1p-22 * coord_max) * (1.0 + 0x1p-20);
   const float Tf = nextafterf((float)T, INFINITY);
-  radius_best_kernel<<<(nq + kBlock - 1) / kBlock, kBlock, 0, (cudaStream_t)stream>>>(
-      nq, qx, qy, nr, rx, ry, eps * eps, Tf, count, best_idx, best_d2);
+  const cudaStream_t st = (cudaStream_t)stream;
+  const int S = lanes_per_query(radius_best_kernel<8>, nq);
+  const long long blocks = ((long long)nq * S + kBlock - 1) / kBlock;
+  if (S == 8)
+    radius_best_kernel<8><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, eps * eps, Tf, count, best_idx, best_d2);
+  else if (S == 4)
+    radius_best_kernel<4><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, eps * eps, Tf, count, best_idx, best_d2);
+  else if (S == 2)
+    radius_best_kernel<2><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, eps * eps, Tf, count, best_idx, best_d2);
+  else
+    radius_best_kernel<1><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, eps * eps, Tf, count, best_idx, best_d2);
   return check("radius_best_kernel");
 }
 
@@ -161,9 +247,20 @@ int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_ma
   if (n < 0 || !(coord_max >= 0.0)) return HG_ERR_ARGS;
   if (n == 0) return HG_OK;
   if (!x || !y || !out) return HG_ERR_ARGS;
-  const float R = nextafterf((float)coord_max, INFINITY);
-  const float R2c = nextafterf((float)(0x1p-43 * coord_max * coord_max), INFINITY);
-  nearest_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, (cudaStream_t)stream>>>(n, x, y, R, R2c, out);
+  // R and 2^-43 R^2 as FP32 values rounded up (the bound's constants), passed in FP64
+  const double R = (double)nextafterf((float)coord_max, INFINITY);
+  const double R2c = (double)nextafterf((float)(0x1p-43 * coord_max * coord_max), INFINITY);
+  const cudaStream_t st = (cudaStream_t)stream;
+  const int S = lanes_per_query(nearest_kernel<8>, n);
+  const long long blocks = ((long long)n * S + kBlock - 1) / kBlock;
+  if (S == 8)
+    nearest_kernel<8><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, R, R2c, out);
+  else if (S == 4)
+    nearest_kernel<4><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, R, R2c, out);
+  else if (S == 2)
+    nearest_kernel<2><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, R, R2c, out);
+  else
+    nearest_kernel<1><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, R, R2c, out);
   return check("nearest_kernel");
 }
 

@@ -40,3 +40,15 @@ def test_connections_reproduce_reference(gold, c):
                                  gold[f"{c}/tu"], gold[f"{c}/ts"], eps=eps, dv_tol=dvt, bal_tol=bt,
                                  matcher=OracleSectionMatcher())
     _check(res, meta, gold, c)
+
+
+def test_velocity_jumps_equal_per_row_norm():
+    """The batched |dv| is the per-row np.linalg.norm bit for bit (the
+    reference takes the norm of each pair's 3-vector)."""
+    from hiten_gb300.connections import velocity_jumps
+    rng = np.random.default_rng(3)
+    for scale in (1e-9, 1e-3, 1.0, 1e7):
+        v = rng.normal(0, scale, (20000, 3)) * np.exp(rng.normal(0, 2, (20000, 1)))
+        v[:5] = [[0, 0, 0], [1e-300, 0, 0], [3, 4, 0], [np.inf, 0, 1], [-0.0, 2, -2]]
+        ref = np.array([np.linalg.norm(r) for r in v])
+        assert np.array_equal(velocity_jumps(v), ref)

@@ -55,3 +55,36 @@ def test_gpu_matcher_equals_fp64_oracle(gpu, seed, n, m, eps):
             assert np.array_equal(x, y)
     for p in (pu, ps):
         assert np.array_equal(G.nearest(p, R), O.nearest(p, R))
+
+
+def _structured(kind):
+    rng = np.random.default_rng(11)
+    if kind == "grid":
+        # a regular grid: every interior point has four neighbours at exactly
+        # the same distance (the lowest index must win), shuffled order
+        g = np.stack(np.meshgrid(np.arange(64) / 256.0, np.arange(48) / 256.0), -1).reshape(-1, 2) - 0.1
+        return g[rng.permutation(g.shape[0])]
+    if kind == "cluster":
+        # micro-clusters below FP32 resolution of the coordinates (their FP32
+        # distances collapse to 0) inside a wide cloud
+        c = rng.uniform(-0.3, 0.3, (300, 2))
+        pts = [c + rng.normal(0, 10.0 ** -e, c.shape) for e in (9, 11, 13)]
+        return np.concatenate([rng.uniform(-0.3, 0.3, (3000, 2))] + pts)
+    if kind == "large":
+        # large coordinates: the FP32 screen's absolute error terms dominate
+        return rng.uniform(-2e3, 2e3, (4000, 2)) * np.exp(rng.normal(0, 2, (4000, 1))) * 1e-3
+    return rng.uniform(-1, 1, (int(kind), 2))
+
+
+@pytest.mark.parametrize("kind", ["1", "2", "33", "grid", "cluster", "large"])
+def test_gpu_nearest_structured_equals_fp64_oracle(gpu, kind):
+    from hiten_gb300.connections import GpuSectionMatcher
+    from oracle.connect import OracleSectionMatcher
+    p = _structured(kind)
+    R = float(np.abs(p).max())
+    G, O = GpuSectionMatcher(), OracleSectionMatcher()
+    assert np.array_equal(G.nearest(p, R), O.nearest(p, R))
+    q = p[::-1].copy()
+    eps = float(np.median(np.abs(np.diff(p[:, 0])))) if p.shape[0] > 1 else 0.5
+    for a, b in zip(G.radius_best(p, q, eps, R), O.radius_best(p, q, eps, R)):
+        assert np.array_equal(a, b)
