@@ -10,6 +10,7 @@ a set) run on the GPU (``hg_radius_best``, ``hg_nearest_neighbor``); the
 per-pair refinement is the reference's scalar arithmetic on the host.
 """
 import ctypes as C
+import gc
 from dataclasses import dataclass
 
 import numpy as np
@@ -215,8 +216,17 @@ def find_connections(points_u, points_s, states_u, states_s, traj_indices_u=None
     ts = np.asarray(traj_indices_s)[J[order]].astype(np.int64).tolist() if traj_indices_s is not None else [0] * order.size
     xu_o, xs_o = xu[order], xs[order]
     # positional fields (kind, delta_v, point2d, state_u, state_s, index_u, index_s, trajectory_index_u,
-    # trajectory_index_s): several times cheaper than keywords at tens of thousands of results
-    results = [ConnectionResult("ballistic" if d <= bal_tol else "impulsive", d, (x, y), su, ss, i, j, a, b)
-               for d, x, y, su, ss, i, j, a, b in zip(dv[order].tolist(), ptx[order].tolist(), pty[order].tolist(),
-                                                       xu_o, xs_o, I[order].tolist(), J[order].tolist(), tu, ts)]
+    # trajectory_index_s): several times cheaper than keywords at tens of thousands of results.  The
+    # cyclic collector is paused while they are made (they hold no cycles): otherwise the allocations
+    # trigger full collections that rescan every live result list, several times the build itself.
+    gc_was_on = gc.isenabled()
+    gc.disable()
+    try:
+        results = [ConnectionResult("ballistic" if d <= bal_tol else "impulsive", d, (x, y), su, ss, i, j, a, b)
+                   for d, x, y, su, ss, i, j, a, b in zip(dv[order].tolist(), ptx[order].tolist(),
+                                                           pty[order].tolist(), xu_o, xs_o, I[order].tolist(),
+                                                           J[order].tolist(), tu, ts)]
+    finally:
+        if gc_was_on:
+            gc.enable()
     return results, {"pairs_considered": total, "accepted": len(results)}

@@ -18,6 +18,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
+
 #include "hitengpu.h"
 
 namespace {
@@ -25,20 +27,23 @@ namespace {
 constexpr int kTile = 256;
 constexpr int kBlock = 128;
 
-// One tile of reference points in shared memory: FP32 copies for the screen,
-// the FP64 values for the exact decisions.
+// One tile of reference points in shared memory: their FP32 copies for the
+// screen (converted once per call by to_float2_kernel: a double-to-float
+// conversion holds GB300's FP64 pipe, so converting in every block's tile load
+// costs as much as the screen).  The exact FP64 decisions read the rare
+// surviving points from global memory.
 struct Tile {
   float2 f[kTile];
-  double2 d[kTile];
 };
 
-__device__ __forceinline__ void load_tile(Tile& T, const double* __restrict__ x, const double* __restrict__ y, int base,
-                                          int n) {
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    const double a = x[base + t], b = y[base + t];
-    T.d[t] = make_double2(a, b);
-    T.f[t] = make_float2((float)a, (float)b);
-  }
+__device__ __forceinline__ void load_tile(Tile& T, const float2* __restrict__ pf, int base, int n) {
+  for (int t = threadIdx.x; t < n; t += blockDim.x) T.f[t] = pf[base + t];
+}
+
+__global__ void to_float2_kernel(int n, const double* __restrict__ x, const double* __restrict__ y,
+                                 float2* __restrict__ out) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = make_float2((float)x[i], (float)y[i]);
 }
 
 // (d2, j) lexicographic minimum of two candidates (j < 0: none).  A scan in
@@ -64,13 +69,37 @@ __device__ __forceinline__ void combine_best(double& bd, int& bj) {
   }
 }
 
+// Radius scan of one tile (entries s, s + S, ...): the FP32 box screen, then
+// the exact FP64 test and the running strict minimum.
+template <int S>
+__device__ __forceinline__ void tile_radius(const Tile& T, const double* __restrict__ rx, const double* __restrict__ ry,
+                                            int n, int s, int base, double xi, double yi, float xf, float yf, float Tf,
+                                            double r2, int& c, double& bd, int& bj) {
+#pragma unroll 4
+  for (int t = s; t < n; t += S) {
+    const float2 pf = T.f[t];
+    const float dxf = xf - pf.x, dyf = yf - pf.y;
+    if (fmaxf(fabsf(dxf), fabsf(dyf)) > Tf) continue;
+    const double dx = xi - rx[base + t], dy = yi - ry[base + t];
+    const double d2 = dx * dx + dy * dy;
+    if (d2 <= r2) {
+      ++c;
+      if (bj < 0 || d2 < bd) {
+        bd = d2;
+        bj = base + t;
+      }
+    }
+  }
+}
+
 // For each query point: number of reference points within eps (exact FP64
 // test), and the nearest of them (strict <: the lowest index wins ties).
 template <int S>
 __global__ void __launch_bounds__(kBlock, 16) radius_best_kernel(int nq, const double* __restrict__ qx,
                                                               const double* __restrict__ qy, int nr,
                                                               const double* __restrict__ rx,
-                                                              const double* __restrict__ ry, double r2, float T,
+                                                              const double* __restrict__ ry,
+                                                              const float2* __restrict__ rf, double r2, float T,
                                                               int* __restrict__ count, int* __restrict__ best_idx,
                                                               double* __restrict__ best_d2) {
   __shared__ Tile tile;
@@ -85,24 +114,13 @@ __global__ void __launch_bounds__(kBlock, 16) radius_best_kernel(int nq, const d
   for (int base = 0; base < nr; base += kTile) {
     const int n = min(kTile, nr - base);
     __syncthreads();
-    load_tile(tile, rx, ry, base, n);
+    load_tile(tile, rf, base, n);
     __syncthreads();
     if (active) {
-      for (int t = s; t < n; t += S) {
-        const float2 pf = tile.f[t];
-        const float dxf = xf - pf.x, dyf = yf - pf.y;
-        if (fabsf(dxf) > T || fabsf(dyf) > T) continue;
-        const double2 pd = tile.d[t];
-        const double dx = xi - pd.x, dy = yi - pd.y;
-        const double d2 = dx * dx + dy * dy;
-        if (d2 <= r2) {
-          ++c;
-          if (bj < 0 || d2 < bd) {
-            bd = d2;
-            bj = base + t;
-          }
-        }
-      }
+      if (n == kTile)
+        tile_radius<S>(tile, rx, ry, kTile, s, base, xi, yi, xf, yf, T, r2, c, bd, bj);
+      else
+        tile_radius<S>(tile, rx, ry, n, s, base, xi, yi, xf, yf, T, r2, c, bd, bj);
     }
   }
 #pragma unroll
@@ -139,14 +157,50 @@ __device__ __forceinline__ float nearest_threshold(float D, double R, double R2c
   return __double2float_ru(__dmul_ru(smax, smax));
 }
 
+// Pass-0 scan of one tile: the smallest FP32 distance over entries s, s + S,
+// ... (self excluded when the query's own index lies in the tile).
+template <int S, bool SELF>
+__device__ __forceinline__ float tile_min(const Tile& T, int cnt, int s, int self, float xf, float yf, float D) {
+#pragma unroll 4
+  for (int t = s; t < cnt; t += S) {
+    if (SELF && t == self) continue;
+    const float2 pf = T.f[t];
+    const float dxf = xf - pf.x, dyf = yf - pf.y;
+    D = fminf(D, __fadd_rn(__fmul_rn(dxf, dxf), __fmul_rn(dyf, dyf)));
+  }
+  return D;
+}
+
+// Pass-1 scan of one tile: exact FP64 distances of the entries under thr.
+template <int S, bool SELF>
+__device__ __forceinline__ void tile_best(const Tile& T, const double* __restrict__ px, const double* __restrict__ py,
+                                          int cnt, int s, int self, int base, double xi, double yi, float xf, float yf,
+                                          float thr, double& bd, int& bj) {
+#pragma unroll 4
+  for (int t = s; t < cnt; t += S) {
+    const float2 pf = T.f[t];
+    const float dxf = xf - pf.x, dyf = yf - pf.y;
+    if (!(__fadd_rn(__fmul_rn(dxf, dxf), __fmul_rn(dyf, dyf)) <= thr) || (SELF && t == self)) continue;
+    const double dx = xi - px[base + t], dy = yi - py[base + t];
+    const double d2 = dx * dx + dy * dy;
+    if (bj < 0 ? d2 < 1e300 : d2 < bd) {
+      bd = d2;
+      bj = base + t;
+    }
+  }
+}
+
 // Nearest neighbour of every point within its own set (excluding itself;
 // strict <, the lowest index wins ties).  Pass 0 finds the smallest FP32
 // distance, pass 1 decides in FP64 among the points under the threshold
 // above, which contain every point whose true distance can be minimal.
+// The query's own index is tested only in the tile that holds it; full tiles
+// run a fixed trip count.
 template <int S>
 __global__ void __launch_bounds__(kBlock, 16) nearest_kernel(int n, const double* __restrict__ px,
-                                                          const double* __restrict__ py, double R, double R2c,
-                                                          int* __restrict__ out) {
+                                                              const double* __restrict__ py,
+                                                              const float2* __restrict__ pf, double R, double R2c,
+                                                              int* __restrict__ out) {
   __shared__ Tile tile;
   const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int s = (int)(g % S);
@@ -158,15 +212,16 @@ __global__ void __launch_bounds__(kBlock, 16) nearest_kernel(int n, const double
   for (int base = 0; base < n; base += kTile) {
     const int cnt = min(kTile, n - base);
     __syncthreads();
-    load_tile(tile, px, py, base, cnt);
+    load_tile(tile, pf, base, cnt);
     __syncthreads();
     if (active) {
-      for (int t = s; t < cnt; t += S) {
-        if (base + t == i) continue;
-        const float2 pf = tile.f[t];
-        const float dxf = xf - pf.x, dyf = yf - pf.y;
-        D = fminf(D, __fadd_rn(__fmul_rn(dxf, dxf), __fmul_rn(dyf, dyf)));
-      }
+      const long long self = i - base;
+      if (self >= 0 && self < cnt)
+        D = tile_min<S, true>(tile, cnt, s, (int)self, xf, yf, D);
+      else if (cnt == kTile)
+        D = tile_min<S, false>(tile, kTile, s, -1, xf, yf, D);
+      else
+        D = tile_min<S, false>(tile, cnt, s, -1, xf, yf, D);
     }
   }
 #pragma unroll
@@ -177,21 +232,16 @@ __global__ void __launch_bounds__(kBlock, 16) nearest_kernel(int n, const double
   for (int base = 0; base < n; base += kTile) {
     const int cnt = min(kTile, n - base);
     __syncthreads();
-    load_tile(tile, px, py, base, cnt);
+    load_tile(tile, pf, base, cnt);
     __syncthreads();
     if (active) {
-      for (int t = s; t < cnt; t += S) {
-        const float2 pf = tile.f[t];
-        const float dxf = xf - pf.x, dyf = yf - pf.y;
-        if (!(__fadd_rn(__fmul_rn(dxf, dxf), __fmul_rn(dyf, dyf)) <= thr) || base + t == i) continue;
-        const double2 pd = tile.d[t];
-        const double dx = xi - pd.x, dy = yi - pd.y;
-        const double d2 = dx * dx + dy * dy;
-        if (bj < 0 ? d2 < 1e300 : d2 < bd) {
-          bd = d2;
-          bj = base + t;
-        }
-      }
+      const long long self = i - base;
+      if (self >= 0 && self < cnt)
+        tile_best<S, true>(tile, px, py, cnt, s, (int)self, base, xi, yi, xf, yf, thr, bd, bj);
+      else if (cnt == kTile)
+        tile_best<S, false>(tile, px, py, kTile, s, -1, base, xi, yi, xf, yf, thr, bd, bj);
+      else
+        tile_best<S, false>(tile, px, py, cnt, s, -1, base, xi, yi, xf, yf, thr, bd, bj);
     }
   }
   combine_best<S>(bd, bj);
@@ -218,6 +268,16 @@ int check(const char* what) {
   return cudaGetLastError() == cudaSuccess ? HG_OK : HG_ERR_CUDA;
 }
 
+// FP32 copy of a point set in stream-ordered scratch (freed on the stream
+// after the search); nullptr on failure.
+float2* float2_copy(int n, const double* x, const double* y, cudaStream_t st) {
+  void* p = nullptr;
+  if (cudaMallocAsync(&p, (size_t)n * sizeof(float2), st) != cudaSuccess) return nullptr;
+  const int blocks = (int)std::min<long long>(((long long)n + 255) / 256, 4096);
+  to_float2_kernel<<<blocks, 256, 0, st>>>(n, x, y, (float2*)p);
+  return (float2*)p;
+}
+
 }  // namespace
 
 extern "C" {
@@ -230,16 +290,19 @@ int hg_radius_best(int nq, const double* qx, const double* qy, int nr, const dou
   const double T = (eps + 0x1p-22 * coord_max) * (1.0 + 0x1p-20);
   const float Tf = nextafterf((float)T, INFINITY);
   const cudaStream_t st = (cudaStream_t)stream;
+  float2* rf = nr > 0 ? float2_copy(nr, rx, ry, st) : nullptr;
+  if (nr > 0 && !rf) return HG_ERR_CUDA;
   const int S = lanes_per_query(radius_best_kernel<8>, nq);
   const long long blocks = ((long long)nq * S + kBlock - 1) / kBlock;
   if (S == 8)
-    radius_best_kernel<8><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, eps * eps, Tf, count, best_idx, best_d2);
+    radius_best_kernel<8><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, rf, eps * eps, Tf, count, best_idx, best_d2);
   else if (S == 4)
-    radius_best_kernel<4><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, eps * eps, Tf, count, best_idx, best_d2);
+    radius_best_kernel<4><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, rf, eps * eps, Tf, count, best_idx, best_d2);
   else if (S == 2)
-    radius_best_kernel<2><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, eps * eps, Tf, count, best_idx, best_d2);
+    radius_best_kernel<2><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, rf, eps * eps, Tf, count, best_idx, best_d2);
   else
-    radius_best_kernel<1><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, eps * eps, Tf, count, best_idx, best_d2);
+    radius_best_kernel<1><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, rf, eps * eps, Tf, count, best_idx, best_d2);
+  if (rf) cudaFreeAsync(rf, st);
   return check("radius_best_kernel");
 }
 
@@ -251,16 +314,19 @@ int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_ma
   const double R = (double)nextafterf((float)coord_max, INFINITY);
   const double R2c = (double)nextafterf((float)(0x1p-43 * coord_max * coord_max), INFINITY);
   const cudaStream_t st = (cudaStream_t)stream;
+  float2* pf = float2_copy(n, x, y, st);
+  if (!pf) return HG_ERR_CUDA;
   const int S = lanes_per_query(nearest_kernel<8>, n);
   const long long blocks = ((long long)n * S + kBlock - 1) / kBlock;
   if (S == 8)
-    nearest_kernel<8><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, R, R2c, out);
+    nearest_kernel<8><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, pf, R, R2c, out);
   else if (S == 4)
-    nearest_kernel<4><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, R, R2c, out);
+    nearest_kernel<4><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, pf, R, R2c, out);
   else if (S == 2)
-    nearest_kernel<2><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, R, R2c, out);
+    nearest_kernel<2><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, pf, R, R2c, out);
   else
-    nearest_kernel<1><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, R, R2c, out);
+    nearest_kernel<1><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, pf, R, R2c, out);
+  cudaFreeAsync(pf, st);
   return check("nearest_kernel");
 }
 
