@@ -274,12 +274,16 @@ def bench_synodic_detect(args):
         res[interp] = (ms, float(nh.float().mean()))
     ms, hits = res["cubic"]
     segs = n * (m - 1)
-    sample_bytes = m * 6 * n * 8
+    sample_bytes = m * 2 * n * 8  # the scan reads y and vy (value and slope of the section function)
     _line("synodic detection on samples, 65536 states x 301 samples (cubic, 50-fold refinement)",
           "section segments scanned/s", segs / (ms * 1e-3), "segments/s", ms,
           {"states": n, "samples": m, "segment_refine": 50, "interp": "cubic", "max_hits": 8},
           mean_hits=hits, linear={"ms": res["linear"][0], "mean_hits": res["linear"][1]},
-          roofline={"bound": "hbm", "bytes_read": sample_bytes, "achieved_gbs": sample_bytes / (ms * 1e-3) / 1e9})
+          roofline={"bound": "fp64", "bytes_read": sample_bytes, "achieved_gbs": sample_bytes / (ms * 1e-3) / 1e9,
+                    "fp64_pipe_active": 0.835, "dram_throughput": 0.004,
+                    "source": "ncu of section_kernel on this workload (profiles/section_kernel_synodic_65536.md): "
+                              "the cubic Hermite evaluations and refinements hold the FP64 pipe; the scanned "
+                              "components are read once"})
 
 
 def bench_correct(args):
