@@ -312,7 +312,9 @@ int hg_serve_stats(hg_server* s, double* p50_ms, double* p99_ms, long long* requ
  * hg_nearest_neighbor: each point's nearest other point of the same set
  * (strict <, lowest index on ties; -1 when n < 2).
  * coord_max >= every |coordinate| involved: it sizes the FP32 pre-screen,
- * whose margin provably keeps the FP64 results exact.
+ * whose margin provably keeps the FP64 results exact.  Each call makes an
+ * FP32 copy of the scanned set in stream-ordered scratch (cudaMallocAsync /
+ * cudaFreeAsync on `stream`, 8 bytes per point); HG_ERR_CUDA if it fails.
  * Replaces: connections/backends.py:31-99 (_pair_counts, _radpair2d: counts
  * and the pairs' per-query minimum used by _ConnectionsBackend.run :444-460)
  * and :174-235 (_nearest_neighbor_2d). */
