@@ -1628,11 +1628,24 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
   const EvCtx<G> ev(L, has_event ? p.ev_index : -1);
   auto cf = dop_coef<G>(L, sm_coef);
 
+  const int slot0 = traj;
   int slot = traj;
   while (true) {
+    // attempted-step budget of this slot in a segmented launch: a lane (group)
+    // holds slots slot0, slot0 + stride, ...; one with fewer slots than the
+    // busiest lane (M of them) gives its last slot the difference, so every
+    // lane spends the M * seg_steps steps its warp runs anyway (a warp's FP64
+    // instructions cost the same whatever lanes are active) and the
+    // trajectories advance further; pausing and resuming keep every bit.
+    int seg_budget = p.seg_steps;
     if (p.seg) {
-      if (slot >= *p.n_in) break;
+      const int n_in = *p.n_in;
+      if (slot >= n_in) break;
       traj = p.active_in[slot];
+      if (slot + p.stride >= n_in) {
+        const int busiest = (n_in + p.stride - 1) / p.stride;
+        seg_budget = p.seg_steps * (busiest - (slot - slot0) / p.stride);
+      }
     } else if (traj >= p.N) {
       break;
     }
@@ -1695,7 +1708,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
     // integrators/rk.py loop test (t - t_end) * direction < 0 with direction
     // +1; the product by 1 is exact, so it is left out
     while (t - tmax < 0.0) {
-      if (p.seg && seg_count >= p.seg_steps) {
+      if (p.seg && seg_count >= seg_budget) {
         paused = true;
         break;
       }
