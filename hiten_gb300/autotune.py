@@ -33,6 +33,8 @@ DOP853_PLANS = (
     {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 32},
     {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 16, "sm_capacity": 4.5},
     {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 32, "sm_capacity": 4.5},
+    {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 48, "sm_capacity": 4.5},
+    {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 64, "sm_capacity": 4.5},
 )
 _plan_cache = {}
 
