@@ -62,3 +62,15 @@ def test_segmented_workspace_query():
                 assert b % 256 == 0 and b >= prev
                 assert b >= n * (3 * 4 + 3 * 8) + n * hits * ((15 * dim + 3) * 8 + 8)
                 prev = b
+
+
+def test_integration_table_names_every_entry_point():
+    """Every entry point of the header has a row (its reference counterpart or
+    none) in the integration notes."""
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    hdr = open(os.path.join(root, "include", "hitengpu.h")).read()
+    notes = open(os.path.join(root, "INTEGRATION.md")).read()
+    names = sorted(set(re.findall(r"\b(hg_[a-z0-9_]+)\s*\(", hdr)))
+    assert names
+    assert [n for n in names if f"`{n}`" not in notes] == []
