@@ -114,7 +114,7 @@ __global__ void bounded_wait_selftest_kernel(int* out, unsigned long long limit_
 
 // Shared-memory hand-off of one warp pair.
 struct PairLink {
-  double H[kPairSlots][kPairTraj][8];  // slot, trajectory, (xx, yy, zz, sxy, qa + qb, y, z, -)
+  double H[kPairSlots][kPairTraj][8];  // slot, trajectory, (xx, yy, zz, xy, yz, xz, -, -)
   unsigned long long full[kPairSlots];
   unsigned long long empty[kPairSlots];
   int fin[kPairTraj];     // STM columns finite, per trajectory
@@ -161,17 +161,15 @@ struct PairState {
       broken = !__all_sync(0xFFFFFFFFu, ok);
     }
     if (!broken) {
-      if (role < 6) {
-        // xx, yy, zz, sxy, qa + qb; the sixth lane adds the stage's y and z
-        const double e = role == 0   ? H.xx
-                         : role == 1 ? H.yy
-                         : role == 2 ? H.zz
-                         : role == 3 ? H.xy
-                         : role == 4 ? H.yz
-                                     : y;
-        link->H[b][t][role] = e;
-        if (role == 5) link->H[b][t][6] = z;
-      }
+      // the six Hessian entries xx, yy, zz, xy, yz, xz, the off-diagonal ones
+      // as hessian42 forms them: xy = (3y) sxy, yz = ((3y) z)(qa + qb),
+      // xz = (3z) sxy, one product ((3a) b) c on lanes 3..5 (c = 1.0 where
+      // two factors suffice: exact); H.xy holds sxy and H.yz qa + qb here
+      const double fa = role == 5 ? z : y;
+      const double fb = role == 4 ? z : H.xy;
+      const double fc = role == 4 ? H.yz : 1.0;
+      const double off = ((3.0 * fa) * fb) * fc;
+      if (role < 6) link->H[b][t][role] = role == 0 ? H.xx : (role == 1 ? H.yy : (role == 2 ? H.zz : off));
       mbar_arrive(&link->full[b]);
     }
     ++seq;
@@ -207,12 +205,10 @@ struct PairStm {
       xx = e[0];
       yy = e[1];
       zz = e[2];
-      const double sxy = e[3], qab = e[4], y = e[5], z = e[6];
+      xy = e[3];
+      yz = e[4];
+      xz = e[5];
       mbar_arrive(&link->empty[b]);
-      // the off-diagonal entries, as hessian42 forms them
-      xy = (3.0 * y) * sxy;
-      xz = (3.0 * z) * sxy;
-      yz = ((3.0 * y) * z) * qab;
     }
     ++seq;
     // rows of F(x) @ Phi[:, col] (dynamics/rtbp.py:204-209), as Layout<7>
@@ -266,11 +262,10 @@ struct PairStmHalf {
       xx = e[0];
       yy = e[1];
       zz = e[2];
-      const double sxy = e[3], qab = e[4], y = e[5], z = e[6];
+      xy = e[3];
+      yz = e[4];
+      xz = e[5];
       mbar_arrive(&link->empty[b]);
-      xy = (3.0 * y) * sxy;
-      xz = (3.0 * z) * sxy;
-      yz = ((3.0 * y) * z) * qab;
     }
     ++seq;
     // the partner lane (lane ^ 1) holds the other rows of the column
