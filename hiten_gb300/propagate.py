@@ -141,7 +141,7 @@ class Dop853Result:
 def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min_step=None,
                      max_steps=100_000, fwd=1, flip=None, event=None, n_samples=0, sample_last_only=False,
                      device=None, stream=None, segmented=False, seg_steps=16, max_segments=8,
-                     scheduled=None):
+                     scheduled=None, finish=True):
     """Adaptive DOP853 for N states from t0 to tmax (scalars or (N,) arrays).
 
     Mirrors integrators/rk.py:2375-2549 / :2678-2803 step for step.
@@ -150,7 +150,8 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
     ``segmented``: run in launches of at most ``seg_steps`` attempted steps per
     trajectory (``max_segments`` launches per asynchronous call, repeated until
     every trajectory finished), compacting the live trajectories between
-    launches; results are bit-identical.  ``scheduled``: host-scheduled
+    launches; results are bit-identical; ``finish=False`` returns after one
+    call, the unfinished trajectories with status HG_RUNNING.  ``scheduled``: host-scheduled
     segments (``hg_propagate_dop853_scheduled``): the layout of each segment
     follows the number of trajectories still running; synchronous.  The
     default (None) schedules 6-dim batches of at least SCHEDULE_MIN states
@@ -221,8 +222,8 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
                 H.check(H.lib.hg_propagate_dop853_segmented(*args, int(seg_steps), segs, resume,
                                                             _ptr(ws), ws_bytes, st))
                 # the caller's step budget bounds the total work; stop once no
-                # trajectory is left running
-                if N == 0 or not bool((status[:N] == _lib.HG_RUNNING).any()):
+                # trajectory is left running (or after one call: finish=False)
+                if not finish or N == 0 or not bool((status[:N] == _lib.HG_RUNNING).any()):
                     break
                 resume = 1
     res = Dop853Result(y_end=y_end[:, :N].t(), t_end=t_end[:N], n_accept=n_acc[:N], n_reject=n_rej[:N],
