@@ -130,3 +130,25 @@ def test_scheduled_stm_dense_and_max_steps(gpu):
         sch = gpu.propagate_dop853(y6, 0.0, 20.0, MU, rtol=1e-11, atol=1e-11, max_steps=7, scheduled=True)
     _same(ref, sch)
     assert np.all(_np(sch.status) == 1)
+
+
+def test_single_call_partial_state(gpu):
+    """finish=False: one segmented call, then return.  With every slot in one
+    wave each trajectory has attempted at most seg_steps steps; the unfinished
+    ones report HG_RUNNING and the finished ones equal a complete run."""
+    from hiten_gb300 import _lib
+    y0 = W.section_states(300, seed=4)
+    tmax = np.where(np.arange(300) % 2 == 0, 0.02, 3.0)  # half finish within a few steps
+    ev = gpu.EventSpec(index=1, offset=0.0, direction=-1, max_hits=2)
+    full = gpu.propagate_dop853(y0, 0.0, tmax, MU, rtol=1e-11, atol=1e-11, event=ev, scheduled=False)
+    part = gpu.propagate_dop853(y0, 0.0, tmax, MU, rtol=1e-11, atol=1e-11, event=ev, scheduled=False,
+                                segmented=True, seg_steps=20, max_segments=1, finish=False)
+    att = _np(part.n_accept) + _np(part.n_reject)
+    st = _np(part.status)
+    assert att.max() <= 20
+    assert np.any(st == _lib.HG_RUNNING)
+    done = st != _lib.HG_RUNNING
+    assert np.any(done)
+    assert np.array_equal(_np(part.y_end)[done], _np(full.y_end)[done])
+    assert np.array_equal(_np(part.t_end)[done], _np(full.t_end)[done])
+    assert np.array_equal(att[done], (_np(full.n_accept) + _np(full.n_reject))[done])
