@@ -86,7 +86,8 @@ def dominant_launch(run_segment, plan, n, sm_count, stream, reps=3):
         torch.cuda.synchronize()
         # a bounded device sleep (~1 ms) while the host enqueues the call, so
         # that the events time the device work, not the host's issue latency
-        torch.cuda._sleep(2_000_000)
+        if hasattr(torch.cuda, "_sleep"):  # private; without it the host latency stays in
+            torch.cuda._sleep(2_000_000)
         e0.record(stream)
         r = run_segment(g, seg)
         e1.record(stream)
