@@ -272,23 +272,26 @@ def bench_fixed_stm(args):
 
 def bench_section(args):
     """Synodic section: 65536 Jacobi-matched states near L1/L2, DOP853 1e-11 to t = 20, up to 8 y = 0
-    crossings (direction -1) each; single pass and host-scheduled plans (same bits)."""
+    crossings (direction -1) each; the execution plan (single pass or host-scheduled segments, same bits)
+    chosen by the autotuner on this workload."""
     import torch
+    from hiten_gb300 import autotune
     from hiten_gb300 import propagate as P
     from hiten_gb300 import workloads as W
     dev = torch.device("cuda", 0)
     y = torch.as_tensor(W.section_states(65536, seed=0), device=dev)
     ev = P.EventSpec(index=1, offset=0.0, direction=-1, max_hits=8)
-    res = {}
-    for plan, kw in (("single", {"scheduled": False}), ("scheduled", {"scheduled": True})):
-        ms, r = _event_ms(lambda: P.propagate_dop853(y, 0.0, 20.0, W.MU_EM, rtol=1e-11, atol=1e-11, event=ev,
-                                                     device=dev, **kw), max(2, args.steps // 4))
-        res[plan] = (ms, int(r.n_accept.sum()), int(r.n_accept.sum() + r.n_reject.sum()), float(r.n_hits.float().mean()))
-    best = min(res, key=lambda k: res[k][0])
-    ms, acc, att, hits = res[best]
+
+    def run(scheduled):
+        return P.propagate_dop853(y, 0.0, 20.0, W.MU_EM, rtol=1e-11, atol=1e-11, event=ev, device=dev,
+                                  scheduled=scheduled)
+
+    plan, plan_ms = autotune.tune_dop853("section_65536", run, device=dev)
+    ms, r = _event_ms(lambda: run(plan["scheduled"]), max(2, args.steps // 4))
+    acc, att = int(r.n_accept.sum()), int(r.n_accept.sum() + r.n_reject.sum())
     _line("synodic section, 65536 states, DOP853 1e-11 to t=20, <= 8 crossings", METRIC, acc / (ms * 1e-3), UNIT, ms,
-          {"states": 65536, "max_hits": 8, "plan": best},
-          plans_ms={k: v[0] for k, v in res.items()}, mean_hits=hits,
+          {"states": 65536, "max_hits": 8, "plan": autotune.plan_name(plan)},
+          autotune_ms=plan_ms, mean_hits=float(r.n_hits.float().mean()),
           roofline={"achieved_tflops": FLOPS_PER_ATTEMPT_D6 * att / (ms * 1e-3) / 1e12})
 
 
