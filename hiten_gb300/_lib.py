@@ -30,7 +30,7 @@ EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg
             "hg_propagate_dop853", "hg_probe_fp64_peak", "hg_propagate_dop853_noalloc", "hg_set_tuning",
             "hg_get_tuning", "hg_section_detect", "hg_trajectory_filters", "hg_propagate_fixed_event",
             "hg_dop853_segmented_workspace_bytes", "hg_propagate_dop853_segmented",
-            "hg_propagate_dop853_scheduled", "hg_get_counter", "hg_radius_best", "hg_nearest_neighbor",
+            "hg_propagate_dop853_scheduled", "hg_get_counter", "hg_radius_best", "hg_nearest_neighbor", "hg_connection_refine",
             "hg_newton_opts_default", "hg_correct_halo", "hg_serve_config_default", "hg_serve_create",
             "hg_serve_destroy", "hg_serve_submit", "hg_serve_poll", "hg_serve_wait", "hg_serve_fetch",
             "hg_serve_cancel", "hg_serve_stats", "hg_selftest_bounded_wait", "hg_host_pow")
@@ -139,6 +139,9 @@ def load(build_if_missing=True):
         L.hg_radius_best.restype = C.c_int
         L.hg_nearest_neighbor.argtypes = [C.c_int, _P, _P, C.c_double, _P, _P]
         L.hg_nearest_neighbor.restype = C.c_int
+        L.hg_connection_refine.argtypes = [C.c_int, _P, _P, _P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, _P, _P, _P,
+                                           _P]
+        L.hg_connection_refine.restype = C.c_int
         L.hg_newton_opts_default.argtypes = [C.POINTER(hg_newton_opts)]
         L.hg_newton_opts_default.restype = None
         L.hg_correct_halo.argtypes = [_P, C.c_double, C.c_int, _P, C.c_longlong, _P, _P, _P, _P,

@@ -6,8 +6,11 @@ keep mutual nearest pairs, refine each on the segments to the points' own
 nearest neighbours (the closest points of two 2-D segments), interpolate
 the states there and classify the velocity jump.  The two all-pairs searches
 (radius pairing with each point's nearest partner, nearest neighbours within
-a set) run on the GPU (``hg_radius_best``, ``hg_nearest_neighbor``); the
-per-pair refinement is the reference's scalar arithmetic on the host.
+a set) and the per-pair segment refinement run on the GPU (``hg_radius_best``,
+``hg_nearest_neighbor``, ``hg_connection_refine``); the velocity jumps (numpy's
+norm, whose BLAS dot order is the host's) and the result records are made on
+the host.  A matcher without ``refine`` (the CPU oracle's, in the tests) takes
+the same arithmetic in numpy.
 """
 import ctypes as C
 import gc
@@ -36,7 +39,7 @@ class ConnectionResult:
 
 
 class GpuSectionMatcher:
-    """The two all-pairs searches on the GPU."""
+    """The two all-pairs searches and the segment refinement on the GPU."""
 
     def __init__(self, device=None):
         self.device = P._device(device)
@@ -75,6 +78,33 @@ class GpuSectionMatcher:
         if rc != _lib.HG_OK:
             raise _lib.HitenGpuError(rc, "hg_nearest_neighbor failed")
         return out.cpu().numpy().astype(np.int64)
+
+
+    def refine(self, pu, ps, Xu, Xs, I, IU, J, JS, ok):
+        """Closest points, interpolated states and midpoints of the pairs
+        (``hg_connection_refine``): (xu (n, 6), xs (n, 6), ptx, pty) on the host."""
+        L = _lib.load()
+        n = int(I.shape[0])
+        dev = self.device
+
+        def up(a, dt):
+            return torch.as_tensor(np.ascontiguousarray(a, dtype=dt), device=dev)
+
+        ti, tiu, tj, tjs = (up(a, np.int32) for a in (I, IU, J, JS))
+        tok = up(ok, np.uint8)
+        tpu, tps, tXu, tXs = (up(a, np.float64) for a in (pu, ps, Xu, Xs))
+        xu = torch.empty((max(n, 1), 6), dtype=torch.float64, device=dev)
+        xs = torch.empty_like(xu)
+        pt = torch.empty((max(n, 1), 2), dtype=torch.float64, device=dev)
+        st = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        with torch.cuda.device(dev):
+            rc = L.hg_connection_refine(n, P._ptr(ti), P._ptr(tiu), P._ptr(tj), P._ptr(tjs), P._ptr(tok),
+                                        int(pu.shape[0]), P._ptr(tpu), P._ptr(tXu), int(ps.shape[0]), P._ptr(tps),
+                                        P._ptr(tXs), P._ptr(xu), P._ptr(xs), P._ptr(pt), st)
+        if rc != _lib.HG_OK:
+            raise _lib.HitenGpuError(rc, "hg_connection_refine failed")
+        pt = pt[:n].cpu().numpy()
+        return xu[:n].cpu().numpy(), xs[:n].cpu().numpy(), pt[:, 0].copy(), pt[:, 1].copy()
 
 
 def closest_points_on_segments_2d(a0x, a0y, a1x, a1y, b0x, b0y, b1x, b1y):
@@ -198,14 +228,18 @@ def find_connections(points_u, points_s, states_u, states_s, traj_indices_u=None
     du = np.hypot(pu[iu_c, 0] - pu[I, 0], pu[iu_c, 1] - pu[I, 1])
     ds = np.hypot(ps[js_c, 0] - ps[J, 0], ps[js_c, 1] - ps[J, 1])
     ok &= ~((du > max_seg_len) | (ds > max_seg_len))
-    s, t, px, py, qx, qy = closest_points_on_segments_2d_batch(
-        pu[I, 0], pu[I, 1], pu[iu_c, 0], pu[iu_c, 1], ps[J, 0], ps[J, 1], ps[js_c, 0], ps[js_c, 1])
-    s = np.where(ok, s, 0.0)
-    t = np.where(ok, t, 0.0)
-    xu = np.where(ok[:, None], (1.0 - s)[:, None] * Xu[I] + s[:, None] * Xu[iu_c], Xu[I])
-    xs = np.where(ok[:, None], (1.0 - t)[:, None] * Xs[J] + t[:, None] * Xs[js_c], Xs[J])
-    ptx = np.where(ok, 0.5 * (px + qx), pu[I, 0])
-    pty = np.where(ok, 0.5 * (py + qy), pu[I, 1])
+    if hasattr(m, "refine"):
+        # on the device: the same scalar arithmetic per pair
+        xu, xs, ptx, pty = m.refine(pu, ps, Xu, Xs, I, iu_c, J, js_c, ok)
+    else:
+        s, t, px, py, qx, qy = closest_points_on_segments_2d_batch(
+            pu[I, 0], pu[I, 1], pu[iu_c, 0], pu[iu_c, 1], ps[J, 0], ps[J, 1], ps[js_c, 0], ps[js_c, 1])
+        s = np.where(ok, s, 0.0)
+        t = np.where(ok, t, 0.0)
+        xu = np.where(ok[:, None], (1.0 - s)[:, None] * Xu[I] + s[:, None] * Xu[iu_c], Xu[I])
+        xs = np.where(ok[:, None], (1.0 - t)[:, None] * Xs[J] + t[:, None] * Xs[js_c], Xs[J])
+        ptx = np.where(ok, 0.5 * (px + qx), pu[I, 0])
+        pty = np.where(ok, 0.5 * (py + qy), pu[I, 1])
     dvv = xu[:, 3:6] - xs[:, 3:6]
     dv = velocity_jumps(dvv)
     # accepted pairs in the order of a stable sort on delta_v (the reference

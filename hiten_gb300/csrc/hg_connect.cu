@@ -268,6 +268,79 @@ int check(const char* what) {
   return cudaGetLastError() == cudaSuccess ? HG_OK : HG_ERR_CUDA;
 }
 
+// Segment refinement of the connection pairs (connections/backends.py:237-320,
+// _closest_points_on_segments_2d, and the interpolation of :480-520): pair k
+// joins a0 = pu[I], a1 = pu[IU] with b0 = ps[J], b1 = ps[JS]; where ok[k] its
+// closest-point parameters s, t (the reference's scalar arithmetic and
+// clamping order, every product and sum rounded on its own) give the states
+// (1 - s) Xu[I] + s Xu[IU], (1 - t) Xs[J] + t Xs[JS] and the midpoint of the
+// two closest points; elsewhere Xu[I], Xs[J] and pu[I].  An index outside its
+// set writes NaN (it cannot come from the searches).
+__global__ void refine_pairs_kernel(int n, const int* __restrict__ I, const int* __restrict__ IU,
+                                    const int* __restrict__ J, const int* __restrict__ JS,
+                                    const unsigned char* __restrict__ ok, int nu, const double* __restrict__ pu,
+                                    const double* __restrict__ Xu, int ns, const double* __restrict__ ps,
+                                    const double* __restrict__ Xs, double* __restrict__ xu, double* __restrict__ xs,
+                                    double* __restrict__ pt) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int i = I[k], j = J[k];
+    const bool use = ok[k] != 0;
+    const int iu = use ? IU[k] : i, js = use ? JS[k] : j;
+    if (i < 0 || i >= nu || iu < 0 || iu >= nu || j < 0 || j >= ns || js < 0 || js >= ns) {
+      for (int c = 0; c < 6; ++c) xu[6 * k + c] = xs[6 * k + c] = nan("");
+      pt[2 * k] = pt[2 * k + 1] = nan("");
+      continue;
+    }
+    if (!use) {
+      for (int c = 0; c < 6; ++c) {
+        xu[6 * k + c] = Xu[6LL * i + c];
+        xs[6 * k + c] = Xs[6LL * j + c];
+      }
+      pt[2 * k] = pu[2LL * i];
+      pt[2 * k + 1] = pu[2LL * i + 1];
+      continue;
+    }
+    const double a0x = pu[2LL * i], a0y = pu[2LL * i + 1], a1x = pu[2LL * iu], a1y = pu[2LL * iu + 1];
+    const double b0x = ps[2LL * j], b0y = ps[2LL * j + 1], b1x = ps[2LL * js], b1y = ps[2LL * js + 1];
+    const double ux = a1x - a0x, uy = a1y - a0y, vx = b1x - b0x, vy = b1y - b0y;
+    const double wx = a0x - b0x, wy = a0y - b0y;
+    const double A = ux * ux + uy * uy, B = ux * vx + uy * vy, Cc = vx * vx + vy * vy;
+    const double D = ux * wx + uy * wy, E = vx * wx + vy * wy;
+    const double den = A * Cc - B * B;
+    double s = 0.0, t = 0.0;
+    if (den > 0.0) {
+      s = (B * E - Cc * D) / den;
+      t = (A * E - B * D) / den;
+    }
+    if (s < 0.0) {
+      s = 0.0;
+      if (Cc > 0.0) t = E / Cc;
+    } else if (s > 1.0) {
+      s = 1.0;
+      if (Cc > 0.0) t = (E + B) / Cc;
+    }
+    if (t < 0.0) {
+      t = 0.0;
+      if (A > 0.0) {
+        s = -D / A;
+        s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+      }
+    } else if (t > 1.0) {
+      t = 1.0;
+      if (A > 0.0) {
+        s = (B - D) / A;
+        s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+      }
+    }
+    for (int c = 0; c < 6; ++c) {
+      xu[6 * k + c] = (1.0 - s) * Xu[6LL * i + c] + s * Xu[6LL * iu + c];
+      xs[6 * k + c] = (1.0 - t) * Xs[6LL * j + c] + t * Xs[6LL * js + c];
+    }
+    pt[2 * k] = 0.5 * ((a0x + s * ux) + (b0x + t * vx));
+    pt[2 * k + 1] = 0.5 * ((a0y + s * uy) + (b0y + t * vy));
+  }
+}
+
 // FP32 copy of a point set in stream-ordered scratch (freed on the stream
 // after the search); nullptr on failure.
 float2* float2_copy(int n, const double* x, const double* y, cudaStream_t st) {
@@ -328,6 +401,18 @@ int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_ma
     nearest_kernel<1><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, pf, R, R2c, out);
   cudaFreeAsync(pf, st);
   return check("nearest_kernel");
+}
+
+int hg_connection_refine(int n, const int* I, const int* IU, const int* J, const int* JS, const unsigned char* ok,
+                         int nu, const double* pu, const double* Xu, int ns, const double* ps, const double* Xs,
+                         double* xu, double* xs, double* pt, void* stream) {
+  if (n < 0 || nu < 0 || ns < 0) return HG_ERR_ARGS;
+  if (n == 0) return HG_OK;
+  if (!I || !IU || !J || !JS || !ok || !pu || !Xu || !ps || !Xs || !xu || !xs || !pt) return HG_ERR_ARGS;
+  const int blocks = (int)std::min<long long>(((long long)n + 127) / 128, 4096);
+  refine_pairs_kernel<<<blocks, 128, 0, (cudaStream_t)stream>>>(n, I, IU, J, JS, ok, nu, pu, Xu, ns, ps, Xs, xu, xs,
+                                                                 pt);
+  return check("refine_pairs_kernel");
 }
 
 }  // extern "C"

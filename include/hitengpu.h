@@ -322,6 +322,20 @@ int hg_radius_best(int nq, const double* qx, const double* qy, int nr, const dou
                    double eps, double coord_max, int* count, int* best_idx, double* best_d2, void* stream);
 int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_max, int* out, void* stream);
 
+/* Segment refinement of n connection pairs (handle-free, asynchronous on
+ * `stream`): pair k joins the unstable-side points pu[I[k]], pu[IU[k]] and the
+ * stable-side points ps[J[k]], ps[JS[k]] (pu, ps row-major [n_set][2]; Xu, Xs
+ * row-major [n_set][6] states).  Where ok[k] != 0: the closest points of the
+ * two segments (the reference's scalar arithmetic and clamping), the states
+ * xu = (1 - s) Xu[I] + s Xu[IU], xs = (1 - t) Xs[J] + t Xs[JS] and their
+ * midpoint pt; elsewhere Xu[I], Xs[J] and pu[I].  Outputs xu, xs [n][6], pt
+ * [n][2]; an index outside [0, nu) / [0, ns) gives NaN rows.
+ * Replaces: connections/backends.py:237-320 (_closest_points_on_segments_2d)
+ * and the per-pair interpolation of _ConnectionsBackend.run :480-520. */
+int hg_connection_refine(int n, const int* I, const int* IU, const int* J, const int* JS, const unsigned char* ok,
+                         int nu, const double* pu, const double* Xu, int ns, const double* ps, const double* Xs,
+                         double* xu, double* xs, double* pt, void* stream);
+
 /* Launch-shape tuning of a handle (set by hiten_gb300.autotune).
  * HG_TUNE_BLOCK_THREADS: threads per block, 32 (default), 64 or 128.
  * HG_TUNE_DOP853_LANES_D6: lanes per 6-dim DOP853 trajectory: 1 (one

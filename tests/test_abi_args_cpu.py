@@ -38,6 +38,14 @@ def test_connection_search_args(L):
     assert L.hg_nearest_neighbor(3, None, x, 1.0, i, None) == bad
     assert L.hg_nearest_neighbor(3, x, x, 1.0, None, None) == bad
     assert L.hg_nearest_neighbor(0, None, None, 1.0, None, None) == ok
+    b = _buf(t=C.c_ubyte)
+    assert L.hg_connection_refine(-1, i, i, i, i, b, 1, x, x, 1, x, x, x, x, x, None) == bad
+    assert L.hg_connection_refine(1, i, i, i, i, b, -1, x, x, 1, x, x, x, x, x, None) == bad
+    assert L.hg_connection_refine(1, None, i, i, i, b, 1, x, x, 1, x, x, x, x, x, None) == bad
+    assert L.hg_connection_refine(1, i, i, i, i, None, 1, x, x, 1, x, x, x, x, x, None) == bad
+    assert L.hg_connection_refine(1, i, i, i, i, b, 1, x, x, 1, x, x, x, x, None, None) == bad
+    assert L.hg_connection_refine(0, None, None, None, None, None, 0, None, None, 0, None, None, None, None, None,
+                                  None) == ok
 
 
 def test_section_and_filter_args(L):

@@ -88,3 +88,37 @@ def test_gpu_nearest_structured_equals_fp64_oracle(gpu, kind):
     eps = float(np.median(np.abs(np.diff(p[:, 0])))) if p.shape[0] > 1 else 0.5
     for a, b in zip(G.radius_best(p, q, eps, R), O.radius_best(p, q, eps, R)):
         assert np.array_equal(a, b)
+
+
+def test_gpu_refinement_equals_host_arithmetic(gpu):
+    """hg_connection_refine gives the numpy refinement's bits: the same cloud
+    through the GPU matcher with and without its refine step (a wrapper that
+    hides it sends find_connections down the numpy path)."""
+    from hiten_gb300.connections import GpuSectionMatcher, find_connections
+    rng = np.random.default_rng(21)
+    n = 20000
+
+    def curve(ph):
+        s = rng.uniform(0, 1, n)
+        return np.c_[0.1 * np.cos(2 * np.pi * s + ph) + rng.normal(0, 1e-4, n),
+                     0.3 * np.sin(2 * np.pi * s + ph) + rng.normal(0, 1e-4, n)]
+
+    pu, ps = curve(0.0), curve(0.3)
+    Xu = np.c_[pu[:, :1] * 0 + 0.85, pu[:, 0], rng.normal(0, 1e-3, n), rng.normal(0, 1e-3, n), pu[:, 1],
+               rng.normal(0, 1e-3, n)]
+    Xs = np.c_[ps[:, :1] * 0 + 0.85, ps[:, 0], rng.normal(0, 1e-3, n), rng.normal(0, 1e-3, n), ps[:, 1],
+               rng.normal(0, 1e-3, n)]
+    g = GpuSectionMatcher()
+
+    class SearchOnly:
+        radius_best = g.radius_best
+        nearest = g.nearest
+
+    kw = dict(eps=3e-4, dv_tol=1e-2, bal_tol=1e-4, max_seg_len=1e-4)  # some segments too long: both branches
+    a, ma = find_connections(pu, ps, Xu, Xs, matcher=g, **kw)
+    b, mb = find_connections(pu, ps, Xu, Xs, matcher=SearchOnly(), **kw)
+    assert ma == mb and len(a) == len(b) > 1000
+    for x, y in zip(a, b):
+        assert (x.kind, x.delta_v, x.point2d, x.index_u, x.index_s) == (y.kind, y.delta_v, y.point2d, y.index_u,
+                                                                         y.index_s)
+        assert np.array_equal(x.state_u, y.state_u) and np.array_equal(x.state_s, y.state_s)
