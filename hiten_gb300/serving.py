@@ -84,6 +84,26 @@ def _split(kind, res, sizes):
     return out
 
 
+def admit(waiting, in_use, budget, free_streams):
+    """One admission pass over `waiting` (in arrival order): a request joins
+    the batch of its kind while its footprint fits the budget (the first one
+    always fits an idle device, so an oversized request cannot starve), and a
+    new kind opens a batch only while a stream is free for it.  Returns
+    ({kind: [requests]}, still waiting, bytes in use); admitted requests get
+    their admission time."""
+    admitted = {}
+    keep = []
+    for r in waiting:
+        fits = in_use + r.footprint <= budget or (in_use == 0 and not admitted)
+        if fits and (r.kind in admitted or len(admitted) < free_streams):
+            admitted.setdefault(r.kind, []).append(r)
+            in_use += r.footprint
+            r.admitted = time.perf_counter()
+        else:
+            keep.append(r)
+    return admitted, keep, in_use
+
+
 @dataclass
 class ServingStats:
     n: int = 0
@@ -149,17 +169,7 @@ class ServingEngine:
             futures -= done
             # admit in arrival order while the footprint fits; merge per kind
             if waiting and self.free_streams:
-                admitted = {}
-                keep = []
-                for r in waiting:
-                    fits = self.in_use + r.footprint <= self.budget or (self.in_use == 0 and not admitted)
-                    if fits and (r.kind in admitted or len(admitted) < len(self.free_streams)):
-                        admitted.setdefault(r.kind, []).append(r)
-                        self.in_use += r.footprint
-                        r.admitted = time.perf_counter()
-                    else:
-                        keep.append(r)
-                waiting = keep
+                admitted, waiting, self.in_use = admit(waiting, self.in_use, self.budget, len(self.free_streams))
                 for kind, reqs in admitted.items():
                     sidx = self.free_streams.pop()
                     futures.add(self.pool.submit(self._run_batch, kind, reqs, sidx))
