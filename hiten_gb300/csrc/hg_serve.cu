@@ -302,14 +302,20 @@ int hg_serve_create(const hg_serve_config* cfg, hg_server** out) {
   std::unique_ptr<hg_server> s(new hg_server());
   s->cfg = c;
   if (cudaSetDevice(c.device) != cudaSuccess) return HG_ERR_NO_DEVICE;
+  // a failure part way releases the streams and handles made so far (no worker runs yet)
+  auto release = [&s](int rc) {
+    for (auto h : s->handles) hg_destroy(h);
+    for (auto st : s->streams) cudaStreamDestroy(st);
+    return rc;
+  };
   for (int i = 0; i < c.max_concurrent; ++i) {
     cudaStream_t st;
-    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return HG_ERR_CUDA;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return release(HG_ERR_CUDA);
     s->streams.push_back(st);
     hg_handle* h = nullptr;
     hg_config hc{c.device};
     const int rc = hg_create(&hc, &h);
-    if (rc != HG_OK) return rc;
+    if (rc != HG_OK) return release(rc);
     s->handles.push_back(h);
   }
   s->slot_busy.assign(c.max_concurrent, 0);

@@ -92,3 +92,28 @@ def test_noalloc_propagation_args(L):
     assert run() == bad
     o.rtol, o.max_steps = 1e-12, 0
     assert run() == bad
+
+
+def test_native_server_host_checks(L):
+    """The request server's defaults and argument checks; on a machine
+    without a device its creation fails with HG_ERR_NO_DEVICE (no worker)."""
+    import torch
+    c = _lib.hg_serve_config()
+    L.hg_serve_config_default(C.byref(c))
+    assert (c.device, c.hbm_budget_bytes, c.max_concurrent) == (0, 8 << 30, 4)
+    out = C.c_void_p(123)
+    assert L.hg_serve_create(C.byref(c), None) == _lib.HG_ERR_ARGS
+    for field, bad in (("max_concurrent", 0), ("max_concurrent", 65), ("hbm_budget_bytes", 0)):
+        d = _lib.hg_serve_config()
+        L.hg_serve_config_default(C.byref(d))
+        setattr(d, field, bad)
+        assert L.hg_serve_create(C.byref(d), C.byref(out)) == _lib.HG_ERR_ARGS
+        assert out.value is None  # cleared on every failure
+        out = C.c_void_p(123)
+    assert L.hg_serve_destroy(None) == _lib.HG_OK
+    y, i = _buf(6), C.c_longlong(0)
+    o = _lib.hg_dop853_opts()
+    assert L.hg_serve_submit(None, 0.01, 6, 1, y, 0.0, 1.0, C.byref(o), None, C.byref(i)) == _lib.HG_ERR_ARGS
+    if not torch.cuda.is_available():
+        assert L.hg_serve_create(C.byref(c), C.byref(out)) == _lib.HG_ERR_NO_DEVICE
+        assert out.value is None
