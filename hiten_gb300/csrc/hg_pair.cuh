@@ -19,9 +19,9 @@
 //   * the STM warp: lane 6t + c holds column c of Phi (components 6r + c,
 //     r = 0..5); lanes 30 and 31 shadow column 5 of trajectory 4.
 // At every right-hand-side evaluation the state warp forms the Hessian's
-// diagonal from its stage state and hands it, with the two sums and the
-// stage's y and z the off-diagonal entries are products of, to the STM warp
-// (which forms those products) through shared memory: a ring of kPairSlots
+// six entries from its stage state (the off-diagonal ones as the products
+// hessian42 takes) and hands them to the STM warp through shared memory: a
+// ring of kPairSlots
 // slots with an mbarrier pair per slot, "full" after the state warp wrote
 // it, "empty" after the STM warp read it; meanwhile the STM warp forms its
 // stage columns.  Every operation and operand is the one the 7-lane layout
