@@ -21,8 +21,7 @@
 // At every right-hand-side evaluation the state warp forms the Hessian's
 // six entries from its stage state (the off-diagonal ones as the products
 // hessian42 takes) and hands them to the STM warp through shared memory: a
-// ring of kPairSlots
-// slots with an mbarrier pair per slot, "full" after the state warp wrote
+// ring of kPairSlots slots with an mbarrier pair per slot, "full" after the state warp wrote
 // it, "empty" after the STM warp read it; meanwhile the STM warp forms its
 // stage columns.  Every operation and operand is the one the 7-lane layout
 // uses (Layout<7>), so the results are bit-identical.
