@@ -16,13 +16,18 @@
 // array's name to a kernel (on the host it is only a stand-in symbol, not a
 // device address), so the first call on each device resolves the real
 // device address with cudaGetSymbolAddress, with that device current, and
-// caches it.  Make that first call before any stream capture begins.
+// caches it.  Make that first call before any stream capture begins.  The
+// cached address is tagged with the CUDA context it was resolved in; when the
+// current context differs (after cudaDeviceReset, the module and its array
+// are loaded again, possibly elsewhere) the next call resolves it again
+// before any device work, so a reset never leaves a stale address behind.
 //
 // All calls share the one counter: it is cleared (cudaMemsetAsync on the
 // caller's stream) at the start of every call, so calls that overlap on the
 // GPU -- on different streams, or from different host threads -- race on it
 // and must be serialized by the caller.  N is limited to HG_NOALLOC_MAX_N so
 // that the 32-bit counter cannot overflow.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -38,18 +43,53 @@ constexpr int kBlock = 32;  // one warp per block: spreads small batches over al
 static __device__ __align__(256) int hg_noalloc_scratch[HG_NOALLOC_SCRATCH_BYTES / sizeof(int)];
 
 std::mutex g_setup_mutex;
-int* g_scratch_addr[kMaxDevices] = {nullptr};
+struct ScratchEntry {
+  int* ptr = nullptr;
+  unsigned long long ctx_id = 0;  // context the address was resolved in
+};
+ScratchEntry g_scratch[kMaxDevices];
 
-// Device address of the scratch array on `device` (the current device).
+// Identity of the calling thread's current CUDA context (driver entry points
+// looked up through the runtime, so the library needs no link to libcuda); 0
+// when no context is current yet or the driver lacks cuCtxGetId.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)f;
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Device address of the scratch array on `device` (the current device),
+// resolved once per context.
 int scratch_address(int device, int** out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[device]) {
+  ScratchEntry& e = g_scratch[device];
+  const unsigned long long id = current_context_id();
+  if (!e.ptr || id == 0 || id != e.ctx_id) {
     int* ptr = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, hg_noalloc_scratch);
-    if (e != cudaSuccess || !ptr) return HG_ERR_CUDA;
-    g_scratch_addr[device] = ptr;
+    const cudaError_t err = cudaGetSymbolAddress((void**)&ptr, hg_noalloc_scratch);
+    if (err != cudaSuccess || !ptr) return HG_ERR_CUDA;
+    e.ptr = ptr;
+    e.ctx_id = current_context_id();  // the lookup made the device's context current
   }
-  *out = g_scratch_addr[device];
+  *out = e.ptr;
   return HG_OK;
 }
 
@@ -57,10 +97,14 @@ template <int G>
 int launch(hg::DopParams p, int device, int* counter, cudaStream_t s) {
   int sm_count = 0;
   if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return HG_ERR_CUDA;
+  // launches without dense samples run the kernel built without that path
+  // (fewer registers), as the handle entry point does
+  auto kern = p.m >= 2 ? hg::dop853_kernel<G, true> : hg::dop853_kernel<G, false>;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hg::dop853_kernel<G>, kBlock, 0) != cudaSuccess ||
-      per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
     per_sm = 1;
+  }
   const int tpb = (kBlock / 32) * hg::Layout<G>::TPW;
   const int need = (p.N + tpb - 1) / tpb;
   const int cap = per_sm * sm_count;
@@ -71,7 +115,7 @@ int launch(hg::DopParams p, int device, int* counter, cudaStream_t s) {
     if (cudaMemsetAsync(counter, 0, sizeof(int), s) != cudaSuccess) return HG_ERR_CUDA;
     p.next_traj = counter;
   }
-  hg::dop853_kernel<G><<<grid, kBlock, 0, s>>>(p);
+  kern<<<grid, kBlock, 0, s>>>(p);
   return cudaGetLastError() == cudaSuccess ? HG_OK : HG_ERR_CUDA;
 }
 

@@ -168,7 +168,16 @@ __global__ void __launch_bounds__(128) section_kernel(SecParams p) {
       c.dt = dt;
       const bool near = fabs(gk) < p.tol_on_surface;
       const bool same_sign = (gk > 0.0 && gk1 > 0.0) || (gk < 0.0 && gk1 < 0.0);
-      const bool tiny = fabs(gk) < 1e-280 || fabs(gk1) < 1e-280;
+      // Segments with an end value this small are always scanned.  Without a
+      // direction the reference tests g_lo * g_hi <= 0, and that product
+      // underflows to zero (a reported crossing) once both factors fall below
+      // about 2^-537; 2^-490 keeps every sub-interval value of a skipped
+      // segment (linear: at least the smaller end; cubic: above the skip
+      // margin 2^-46 (|g0| + |g1| + ...) >= 2^-535) far from that range.
+      // With a direction the tests compare g itself with zero, and 1e-280
+      // only keeps (1 - s) g away from underflow.
+      const double tiny_end = dir_any ? 0x1p-490 : 1e-280;
+      const bool tiny = fabs(gk) < tiny_end || fabs(gk1) < tiny_end;
       cand = true;
       if (!near && same_sign && !tiny && !p.cubic) cand = false;
       if (cand) {

@@ -194,10 +194,14 @@ int hg_propagate_dop853_scheduled(hg_handle* h, double mu, int dim, int N,
  * file-scope __device__ array of HG_NOALLOC_SCRATCH_BYTES per device, held
  * until the process exits.  Runs on the current device.  The first call on a
  * device looks up that array's device address (cudaGetSymbolAddress); make
- * it before any stream capture.  The counter is cleared at the start of each
- * call and shared by all calls: calls that overlap on the GPU race, so
- * serialize them.  N > HG_NOALLOC_MAX_N (the 32-bit counter's safe range) is
- * rejected with HG_ERR_ARGS; errors are reported by return code only. */
+ * it before any stream capture.  The address is looked up again when the
+ * calling thread's CUDA context changes (after cudaDeviceReset), so make the
+ * first call after a reset outside stream capture too.  The counter is
+ * cleared at the start of each call and shared by all calls: calls that
+ * overlap on the GPU race, so serialize them.  Arguments, nullable outputs
+ * and results are those of hg_propagate_dop853; N > HG_NOALLOC_MAX_N (the
+ * 32-bit counter's safe range) is rejected with HG_ERR_ARGS; errors are
+ * reported by return code only. */
 #define HG_NOALLOC_SCRATCH_BYTES 256
 #define HG_NOALLOC_MAX_N (1 << 30)
 int hg_propagate_dop853_noalloc(double mu, int dim, int N,

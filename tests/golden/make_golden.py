@@ -17,7 +17,7 @@ fixture below is produced through the reference's own call sites:
 Inputs come from ``hiten_gb300.workloads`` (seeded).  Run only where the
 reference tree is available:
 
-    python tests/golden/make_golden.py /root/reference/src
+    python tests/golden/make_golden.py /path/to/hiten/src
 """
 import multiprocessing as mp
 import os
@@ -234,4 +234,6 @@ def main(ref_src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path to the hiten source tree, the directory holding hiten/>")
+    main(sys.argv[1])

@@ -5,7 +5,7 @@ refinement, delta-v classification) run in pure-Python mode through
 ``refshim`` on seeded synthetic section point clouds.  Writes
 ``connections.npz``.  Run only where the reference tree is available:
 
-    python tests/golden/make_golden_connections.py /root/reference/src
+    python tests/golden/make_golden_connections.py /path/to/hiten/src
 """
 import os
 import sys
@@ -78,4 +78,6 @@ def main(ref_src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path to the hiten source tree, the directory holding hiten/>")
+    main(sys.argv[1])

@@ -5,7 +5,7 @@ stepper, continuation/stepping/) run in pure-Python mode through
 ``refshim``, from seed orbits corrected by the reference.  Writes
 ``family.npz``.  Run only where the reference tree is available:
 
-    python tests/golden/make_golden_family.py /root/reference/src
+    python tests/golden/make_golden_family.py /path/to/hiten/src
 """
 import multiprocessing as mp
 import os
@@ -73,4 +73,6 @@ def main(ref_src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path to the hiten source tree, the directory holding hiten/>")
+    main(sys.argv[1])

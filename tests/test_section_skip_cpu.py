@@ -67,3 +67,59 @@ def test_skipped_segments_never_change_sign():
         assert np.all(np.sign(v) == np.sign(g0[sk])), "a skipped segment changes sign"
     # the adversarial draws reach the skip often enough to mean something
     assert skipped > total // 4
+
+
+def _skips_scan(g0, g1, d0, d1, dt, cubic, dir_any, tiny_any=2.0 ** -490):
+    """The kernel's decision to skip a segment's sub-interval scan (no end value
+    near the surface): same-signed ends, neither below the tiny threshold and,
+    for cubic segments, the hull or basis bound."""
+    tiny_end = tiny_any if dir_any else 1e-280
+    same = ((g0 > 0) & (g1 > 0)) | ((g0 < 0) & (g1 < 0))
+    ok = same & (np.abs(g0) >= tiny_end) & (np.abs(g1) >= tiny_end)
+    if cubic:
+        ok &= _skip(g0, g1, d0, d1, dt)
+    return ok
+
+
+def _reference_crosses_any(g0, g1, d0, d1, dt, cubic, r=50):
+    """Whether the reference's direction=None test (g_lo * g_hi <= 0 and
+    g_lo != g_hi, synodic/backend.py:588) fires on any sub-interval."""
+    step = 1.0 / (r + 1)
+    s = np.arange(r + 2) * step
+    if cubic:
+        v = _herm(s[:, None], g0, g1, d0, d1, dt)
+    else:
+        v = (1.0 - s[:, None]) * g0 + s[:, None] * g1
+    lo, hi = v[:-1], v[1:]
+    return np.any((lo * hi <= 0.0) & (lo != hi), axis=0)
+
+
+def _tiny_segments(rng, n):
+    sign = rng.choice([-1.0, 1.0], n)
+    g0 = sign * 2.0 ** rng.uniform(-560, -380, n)
+    g1 = sign * 2.0 ** rng.uniform(-560, -380, n)
+    dt = 10.0 ** rng.uniform(-3, 0, n)
+    m0 = np.abs(g0) * rng.normal(0, 1, n)
+    m1 = np.abs(g1) * rng.normal(0, 1, n)
+    return g0, g1, m0 / dt, m1 / dt, dt
+
+
+def test_direction_free_skip_never_hides_an_underflowing_product():
+    """Without a direction the reference's product g_lo * g_hi underflows to
+    zero for same-signed values below about 2^-537 and reports a crossing:
+    no segment the kernel skips may be one of those (linear and cubic)."""
+    rng = np.random.default_rng(5)
+    for cubic in (False, True):
+        g0, g1, d0, d1, dt = _tiny_segments(rng, 40000)
+        sk = _skips_scan(g0, g1, d0, d1, dt, cubic, dir_any=True)
+        assert sk.sum() > 1000
+        assert not np.any(_reference_crosses_any(g0[sk], g1[sk], d0[sk], d1[sk], dt[sk], cubic))
+
+
+def test_direction_free_skip_check_catches_a_loose_threshold():
+    """The check above fails for the threshold used with a direction (1e-280):
+    the reference does report crossings on segments that rule would skip."""
+    rng = np.random.default_rng(5)
+    g0, g1, d0, d1, dt = _tiny_segments(rng, 40000)
+    sk = _skips_scan(g0, g1, d0, d1, dt, False, dir_any=True, tiny_any=1e-280)
+    assert np.any(_reference_crosses_any(g0[sk], g1[sk], d0[sk], d1[sk], dt[sk], False))
