@@ -19,6 +19,12 @@ beside it).  `value`: throughput with the seeds resident in HBM;
 host seeds, H2D and D2H copies inside the timed region.  `gpu_launches`:
 kernels launched in the timed region, read from the library's counter.
 
+`secondary`: the other BASELINE configs measured in the same run after the
+headline -- config 1 (RK8 + STM), config 3 (synodic section), config 4 (halo
+correction, ||r|| and ||dx||) and config 5 (serving mix, p50/p99) -- each with
+its time, roofline fraction of the FP64 peak, plain-GPU form and CPU oracle
+baseline (`--no-secondary` skips them; `--workload W` runs one alone).
+
 `--impl reference`: the reference's algorithm on the host cores (the CPU
 oracle in numba-lowering mode, one trajectory per task, all host threads),
 on a bounded sample of the same seeds.
@@ -254,45 +260,131 @@ def _line(name, metric, value, unit, ms, cfg, **extra):
     print(json.dumps(out))
 
 
-def bench_fixed_stm(args):
-    """Fixed-step RK8 with the 42-dim variational system: 1024 states (STM = I), t in [0, 3], 3000 steps,
-    every 100th state written."""
+def _print_secondary(d):
+    """One JSON line for a secondary workload run on its own (--workload)."""
+    extra = {k: v for k, v in d.items() if k not in ("workload", "metric", "value", "unit", "ms", "config")}
+    _line(d["workload"], d["metric"], d["value"], d["unit"], d["ms"], d.get("config", {}), **extra)
+
+
+def _roofline(flops, ms, peak, note):
+    achieved = flops / (ms * 1e-3) / 1e12
+    return {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if peak else None, "flops": flops, "work": note,
+            "peak_source": "measured: DFMA throughput probe (hg_probe_fp64_peak) on this GPU"}
+
+
+def _cpu_loop(fn, min_seconds):
+    """Repeat fn() (returning units of work) until min_seconds of wall time; (units/s, seconds, units)."""
+    units = 0
+    t0 = time.perf_counter()
+    while True:
+        units += fn()
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            return units / dt, dt, units
+
+
+def _peak(dev):
+    from hiten_gb300 import propagate as P
+    return P.fp64_peak_tflops(dev)
+
+
+FLOPS_PER_STEP_RK8_D42 = 7870.0
+FLOPS_PER_ATTEMPT_D42 = 8586.0
+
+
+def sec_fixed_stm(steps, dev, peak, cpu=True):
+    """BASELINE config 1: fixed-step RK8 with the 42-dim variational system, 1024 states (STM = I),
+    t in [0, 3], 3000 steps, every 100th state written."""
     import torch
     from hiten_gb300 import propagate as P
     from hiten_gb300 import workloads as W
-    dev = torch.device("cuda", 0)
-    y = torch.as_tensor(W.stm_fixed_batch(1024, seed=0), device=dev)
+    y_host = W.stm_fixed_batch(1024, seed=0)
+    y = torch.as_tensor(y_host, device=dev)
     t = np.linspace(0.0, 3.0, 3001)
-    ms, _ = _event_ms(lambda: P.propagate_fixed(y, t, W.MU_EM, order=8, out_every=100, device=dev), args.steps)
-    steps = 1024 * 3000
-    _line("RK8 + STM, 1024 states x 3000 steps (42-dim)", METRIC, steps / (ms * 1e-3), UNIT, ms,
-          {"states": 1024, "steps": 3000, "dim": 42},
-          roofline={"achieved_tflops": 7870 * steps / (ms * 1e-3) / 1e12, "flops_per_step": 7870})
+    ms, _ = _event_ms(lambda: P.propagate_fixed(y, t, W.MU_EM, order=8, out_every=100, device=dev), max(3, steps // 4))
+    units = 1024 * 3000
+    n_plain = 8
+    pms, _ = _event_ms(lambda: [P.propagate_fixed(y[i:i + 1], t, W.MU_EM, order=8, out_every=100, device=dev)
+                                for i in range(n_plain)], 1)
+    out = {"workload": "RK8 + STM, 1024 states x 3000 steps (42-dim)", "metric": METRIC,
+           "value": units / (ms * 1e-3), "unit": UNIT, "ms": ms, "config": {"states": 1024, "steps": 3000, "dim": 42},
+           "timing": "CUDA events on the launching stream, median",
+           "roofline": _roofline(FLOPS_PER_STEP_RK8_D42 * units, ms, peak, "7870 flops per 42-dim RK8 step"),
+           "plain_gpu": {"value": n_plain * 3000 / (pms * 1e-3), "unit": UNIT,
+                         "form": f"one call per trajectory, {n_plain}-trajectory sample"}}
+    if cpu:
+        from oracle import hgo
+        hgo.set_mode(hgo.MODE_NUMBA)
+        th = os.cpu_count() or 1
+        v, dt, n = _cpu_loop(lambda: (hgo.fixed_rk_batch(8, y_host, t, W.MU_EM, out_every=100, threads=th), 1024 * 3000)[1],
+                             2.0)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
+                               "sample": f"all 1024 states x 3000 steps, repeated: {n} steps in {dt:.1f} s "
+                                         f"(CPU oracle, numba lowering of powers, libm pow)"}
+    return out
 
 
-def bench_section(args):
-    """Synodic section: 65536 Jacobi-matched states near L1/L2, DOP853 1e-11 to t = 20, up to 8 y = 0
+def bench_fixed_stm(args):
+    import torch
+    dev = torch.device("cuda", 0)
+    _print_secondary(sec_fixed_stm(args.steps, dev, _peak(dev), cpu=not args.no_cpu_baseline))
+
+
+def sec_section(steps, dev, peak, cpu=True):
+    """BASELINE config 3: 65536 Jacobi-matched states near L1/L2, DOP853 1e-11 to t = 20, up to 8 y = 0
     crossings (direction -1) each; the execution plan (single pass or host-scheduled segments, same bits)
     chosen by the autotuner on this workload."""
     import torch
     from hiten_gb300 import autotune
     from hiten_gb300 import propagate as P
     from hiten_gb300 import workloads as W
-    dev = torch.device("cuda", 0)
-    y = torch.as_tensor(W.section_states(65536, seed=0), device=dev)
+    y_host = W.section_states(65536, seed=0)
+    y = torch.as_tensor(y_host, device=dev)
     ev = P.EventSpec(index=1, offset=0.0, direction=-1, max_hits=8)
 
-    def run(scheduled):
-        return P.propagate_dop853(y, 0.0, 20.0, W.MU_EM, rtol=1e-11, atol=1e-11, event=ev, device=dev,
+    def run(scheduled, yy=y):
+        return P.propagate_dop853(yy, 0.0, 20.0, W.MU_EM, rtol=1e-11, atol=1e-11, event=ev, device=dev,
                                   scheduled=scheduled)
 
     plan, plan_ms = autotune.tune_dop853("section_65536", run, device=dev)
-    ms, r = _event_ms(lambda: run(plan["scheduled"]), max(2, args.steps // 4))
+    ms, r = _event_ms(lambda: run(plan["scheduled"]), max(2, steps // 4))
     acc, att = int(r.n_accept.sum()), int(r.n_accept.sum() + r.n_reject.sum())
-    _line("synodic section, 65536 states, DOP853 1e-11 to t=20, <= 8 crossings", METRIC, acc / (ms * 1e-3), UNIT, ms,
-          {"states": 65536, "max_hits": 8, "plan": autotune.plan_name(plan)},
-          autotune_ms=plan_ms, mean_hits=float(r.n_hits.float().mean()),
-          roofline={"achieved_tflops": FLOPS_PER_ATTEMPT_D6 * att / (ms * 1e-3) / 1e12})
+    n_plain = 16
+    plain = []
+    pms, _ = _event_ms(lambda: plain.extend(run(False, y[i:i + 1]) for i in range(n_plain)), 1)
+    plain_acc = sum(int(x.n_accept.sum()) for x in plain[-n_plain:])
+    out = {"workload": "synodic section, 65536 states, DOP853 1e-11 to t=20, <= 8 crossings", "metric": METRIC,
+           "value": acc / (ms * 1e-3), "unit": UNIT, "ms": ms,
+           "config": {"states": 65536, "max_hits": 8, "plan": autotune.plan_name(plan)},
+           "timing": "CUDA events on the launching stream, median (the scheduled driver reads the live count "
+                     "back between segments inside the timed region)",
+           "attempted_steps_per_s": att / (ms * 1e-3), "autotune_ms": plan_ms,
+           "mean_hits": float(r.n_hits.float().mean()),
+           "roofline": _roofline(FLOPS_PER_ATTEMPT_D6 * att, ms, peak, "1314 flops per attempted 6-dim DOP853 step"),
+           "plain_gpu": {"value": plain_acc / (pms * 1e-3), "unit": UNIT,
+                         "form": f"one single-pass call per trajectory, {n_plain}-trajectory sample"}}
+    if cpu:
+        from oracle import hgo
+        hgo.set_mode(hgo.MODE_NUMBA)
+        th = os.cpu_count() or 1
+        sub = y_host[np.random.default_rng(1).choice(len(y_host), 1024, replace=False)]
+
+        def one():
+            rr = hgo.dop853_event_batch(sub, 0.0, 20.0, W.MU_EM, 1, 0.0, -1, 8, rtol=1e-11, atol=1e-11, max_step=1e4,
+                                        threads=th)
+            return int(rr["n_accept"].sum())
+        v, dt, n = _cpu_loop(one, 2.0)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
+                               "sample": f"1024 seeded states of the 65536, repeated: {n} accepted steps in "
+                                         f"{dt:.1f} s (CPU oracle, numba lowering, libm pow)"}
+    return out
+
+
+def bench_section(args):
+    import torch
+    dev = torch.device("cuda", 0)
+    _print_secondary(sec_section(args.steps, dev, _peak(dev), cpu=not args.no_cpu_baseline))
 
 
 def bench_synodic_detect(args):
@@ -333,9 +425,11 @@ def bench_synodic_detect(args):
                               "components are read once"})
 
 
-def bench_correct(args):
-    """Batched halo correction: 2048 third-order guesses (half L1, half L2, Az ~ U[0.01, 0.4]), single
-    shooting on the half-period y = 0 crossing to ||r|| < 1e-12."""
+def sec_correct(steps, dev, peak, cpu=True):
+    """BASELINE config 4: batched halo correction, 2048 third-order guesses (half L1, half L2,
+    Az ~ U[0.01, 0.4], zenith 50/50 seeded), single shooting on the half-period y = 0 crossing until
+    ||r||_inf < 1e-12 (the reference's criterion); ||dx||_inf of one more Newton step at the result is
+    reported beside it."""
     import torch
     from hiten_gb300 import corrector, halo
     from hiten_gb300 import workloads as W
@@ -343,42 +437,85 @@ def bench_correct(args):
     pt, az, zen = W.halo_guess_params(2048, seed=0)
     g = np.concatenate([halo.third_order_guess(mu, 1, az[pt == 1], zen[pt == 1]),
                         halo.third_order_guess(mu, 2, az[pt == 2], zen[pt == 2])])
-    corrector.correct_halo(g[:64], mu)
+    corrector.correct_halo_native(g[:64], mu)
     torch.cuda.synchronize()
-    ts = []
-    for _ in range(max(1, args.steps // 4)):
-        t0 = time.perf_counter()
-        res = corrector.correct_halo(g, mu)
-        torch.cuda.synchronize()
-        ts.append(time.perf_counter() - t0)
-    s = statistics.median(ts)
+    reps = max(2, steps // 4)
     tn = []
-    for _ in range(max(1, args.steps // 4)):
+    for _ in range(reps):
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         nat = corrector.correct_halo_native(g, mu)
         torch.cuda.synchronize()
         tn.append(time.perf_counter() - t0)
     sn = statistics.median(tn)
-    _line("halo correction, 2048 guesses (L1/L2, Az 0.01-0.4)", "orbits corrected/s", len(g) / sn, "orbits/s",
-          sn * 1e3, {"orbits": len(g), "driver": "native C-ABI hg_correct_halo"},
-          converged=int((nat.status == 0).sum()), iterations_hist=np.bincount(nat.iterations).tolist(),
-          python_host_loop={"ms": s * 1e3, "orbits_per_s": len(g) / s, "converged": int((res.status == 0).sum()),
-                            "gpu_launches": res.launches,
-                            "iterations_hist": np.bincount(res.iterations).tolist()})
+    # the Python host loop over the same kernels, with its attempted-step count for the roofline
+    be = corrector.GpuShootingBackend(mu, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = corrector.correct_halo(g, mu, backend=be)
+    torch.cuda.synchronize()
+    sp = time.perf_counter() - t0
+    flops = FLOPS_PER_ATTEMPT_D6 * be.attempts[6] + FLOPS_PER_ATTEMPT_D42 * be.attempts[42]
+    ok = nat.status == 0
+    dx = corrector.newton_step_norms(nat.x0[ok], mu, device=dev)
+    n_plain = 8
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(n_plain):
+        corrector.correct_halo(g[i:i + 1], mu)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    out = {"workload": "halo correction, 2048 guesses (L1/L2, Az 0.01-0.4)", "metric": "orbits corrected/s",
+           "value": len(g) / sn, "unit": "orbits/s", "ms": sn * 1e3,
+           "config": {"orbits": len(g), "driver": "native C-ABI hg_correct_halo", "zenith": "seeded 50/50"},
+           "timing": "host wall clock around the synchronous call (device work and host Newton/Armijo "
+                     "bookkeeping), median",
+           "converged": int(ok.sum()), "iterations_hist": np.bincount(nat.iterations).tolist(),
+           "convergence": {"residual_inf_max": float(np.max(nat.residual_norm[ok])),
+                           "dx_inf_max": float(np.nanmax(dx)), "dx_inf_median": float(np.nanmedian(dx)),
+                           "dx_below_1e-12": int(np.sum(dx < 1e-12)),
+                           "criterion": "stop when ||r||_inf < 1e-12 (the reference's test); ||dx||_inf is the "
+                                        "next Newton correction at the corrected state"},
+           "roofline": _roofline(flops, sp * 1e3, peak,
+                                 f"Python host loop over the same kernels: {be.attempts[6]} attempted 6-dim steps "
+                                 f"x 1314 + {be.attempts[42]} attempted 42-dim steps x 8586 flops, over its "
+                                 f"wall time {sp * 1e3:.1f} ms (legs are latency-bound)"),
+           "python_host_loop": {"ms": sp * 1e3, "orbits_per_s": len(g) / sp, "converged": int((res.status == 0).sum()),
+                                "gpu_launches": res.launches},
+           "plain_gpu": {"value": n_plain / plain_s, "unit": "orbits/s",
+                         "form": f"one correction call per orbit, {n_plain}-orbit sample"}}
+    if cpu:
+        from oracle import hgo
+        from oracle.shooting import OracleShootingBackend
+        th = os.cpu_count() or 1
+        sub = g[:32]
+        v, dt, n = _cpu_loop(lambda: int(np.sum(corrector.correct_halo(
+            sub, mu, backend=OracleShootingBackend(hgo, mu, hgo.MODE_NUMBA, threads=th)).status >= 0)), 2.0)
+        out["cpu_baseline"] = {"value": v, "unit": "orbits/s", "cores": th, "kind": "port",
+                               "sample": f"32 of the guesses, repeated: {n} corrections in {dt:.1f} s (the same "
+                                         f"Newton/Armijo host loop over the CPU oracle's propagations, numba lowering; "
+                                         f"event legs threaded, STM legs one orbit at a time)"}
+    return out
 
 
-def bench_serving(args):
-    """Serving mix: seeded Poisson stream (200 req/s for 1 s) of manifold (64-4096 seeds), correction
+def bench_correct(args):
+    import torch
+    dev = torch.device("cuda", 0)
+    _print_secondary(sec_correct(args.steps, dev, _peak(dev), cpu=not args.no_cpu_baseline))
+
+
+def sec_serving(steps, dev, peak, cpu=True, seeds=None):
+    """BASELINE config 5: seeded Poisson stream (200 req/s for 1 s) of manifold (64-4096 seeds), correction
     (1-256 guesses) and synodic (1k-32k states) requests; continuous batching vs the same stream run
     sequentially in the plain form (one single-pass call per request)."""
-    import torch
     from hiten_gb300 import serving
     from hiten_gb300 import workloads as W
     mu = W.MU_EM
-    dev = torch.device("cuda", 0)
-    seeds = make_seeds(dev)
+    if seeds is None:
+        seeds = make_seeds(dev)
     serving.run_sequential(serving.poisson_requests(200.0, 0.05, mu, seed=2, manifold_seeds=seeds,
                                                     size_scale=0.05), mu)
+
     def stream(burst=False):
         reqs = serving.poisson_requests(200.0, 1.0, mu, seed=1, manifold_seeds=seeds)
         if burst:  # every request present at t = 0: throughput without waiting for arrivals
@@ -392,11 +529,46 @@ def bench_serving(args):
     eng.close()
     seq = serving.run_sequential(stream(), mu).summary()
     seq_burst = serving.run_sequential(stream(burst=True), mu).summary()
-    _line("serving mix, Poisson 200 req/s x 1 s (manifold / correct / synodic)", METRIC,
-          served_burst["traj_steps_per_s"], UNIT, served_burst["wall_s"] * 1e3, {"rate_hz": 200, "window_s": 1.0},
-          served_poisson=served, sequential_plain_poisson=seq, served_burst=served_burst,
-          sequential_plain_burst=seq_burst,
-          speedup_vs_plain=served_burst["traj_steps_per_s"] / seq_burst["traj_steps_per_s"])
+    out = {"workload": "serving mix, Poisson 200 req/s x 1 s (manifold / correct / synodic)", "metric": METRIC,
+           "value": served_burst["traj_steps_per_s"], "unit": UNIT, "ms": served_burst["wall_s"] * 1e3,
+           "config": {"rate_hz": 200, "window_s": 1.0},
+           "p50_ms": served["p50_ms"], "p99_ms": served["p99_ms"],
+           "timing": "host wall clock of the served stream (arrival to completion per request for p50/p99)",
+           "served_poisson": served, "sequential_plain_poisson": seq, "served_burst": served_burst,
+           "sequential_plain_burst": seq_burst,
+           "speedup_vs_plain": served_burst["traj_steps_per_s"] / seq_burst["traj_steps_per_s"],
+           "roofline": {"bound": "fp64", "note": "the served batches run the kernels of configs 2-4; see their "
+                                                  "roofline entries"}}
+    if cpu:
+        from oracle import hgo
+        hgo.set_mode(hgo.MODE_NUMBA)
+        th = os.cpu_count() or 1
+        reqs = stream()
+        rng = np.random.default_rng(7)
+        man = np.concatenate([r.payload for r in reqs if r.kind == "manifold"])
+        syn = np.concatenate([r.payload for r in reqs if r.kind == "synodic"])
+        man = man[rng.choice(len(man), min(len(man), 256), replace=False)]
+        syn = syn[rng.choice(len(syn), min(len(syn), 256), replace=False)]
+
+        def one():
+            a = hgo.dop853_event_batch(man, 0.0, TF, mu, 0, 1 - mu, 0, 1, max_step=1e4, fwd=-1, flip=(0, 6),
+                                       threads=th)
+            b = hgo.dop853_event_batch(syn, 0.0, 20.0, mu, 1, 0.0, -1, 8, rtol=1e-11, atol=1e-11, max_step=1e4,
+                                       threads=th)
+            return int(a["n_accept"].sum() + b["n_accept"].sum())
+        v, dt, n = _cpu_loop(one, 2.0)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
+                               "sample": f"256 manifold seeds + 256 synodic states drawn from the stream's requests, "
+                                         f"repeated: {n} accepted steps in {dt:.1f} s (CPU oracle, numba lowering; "
+                                         f"the CPU path has no serving form, so this is its propagation rate on "
+                                         f"the mix's trajectories)"}
+    return out
+
+
+def bench_serving(args):
+    import torch
+    dev = torch.device("cuda", 0)
+    _print_secondary(sec_serving(args.steps, dev, _peak(dev), cpu=not args.no_cpu_baseline))
 
 
 def bench_continuation(args):
@@ -491,6 +663,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the other BASELINE configs (1, 3, 4, 5) measured after the headline")
     ap.add_argument("--plan", default=None,
                     help="force an execution plan by name (autotune.plan_name), e.g. scheduled_seg16")
     ap.add_argument("--workload", default="manifold", choices=["manifold"] + sorted(EXTRA),
@@ -637,6 +811,23 @@ def main():
     dom = dominant_launch(run_segment, plan, N, torch.cuda.get_device_properties(dev).multi_processor_count,
                           stream)
 
+    # the other BASELINE configs, each measured in this run after the headline
+    # (rank 0 of a single-GPU run; replicas add nothing to them)
+    secondary = None
+    if rank == 0 and world == 1 and not args.no_secondary:
+        cpu_ok = not args.no_cpu_baseline
+        secondary = {}
+        for key, fn in (("config1_fixed_stm", lambda: sec_fixed_stm(args.steps, dev, peak, cpu_ok)),
+                        ("config3_section", lambda: sec_section(args.steps, dev, peak, cpu_ok)),
+                        ("config4_correct", lambda: sec_correct(args.steps, dev, peak, cpu_ok)),
+                        ("config5_serving", lambda: sec_serving(args.steps, dev, peak, cpu_ok, seeds=seeds))):
+            t0 = time.perf_counter()
+            try:
+                secondary[key] = fn()
+            except Exception as e:  # a failing secondary must not hide the headline
+                secondary[key] = {"error": f"{type(e).__name__}: {e}"}
+            secondary[key]["wall_s"] = time.perf_counter() - t0
+
     if rank == 0:
         prof = os.path.join(HERE, "profiles", "traffic_dop853_manifold.json")
         traffic, pipe = None, None
@@ -645,7 +836,8 @@ def main():
                 rec = json.load(f)
             traffic = rec.get("dram_bytes_per_launch")
             pipe = {k: rec[k] for k in ("fp64_pipe_active", "fp64_issue_frac", "threads_per_instruction") if k in rec}
-            pipe["source"] = "ncu, dominant launch (profiles/dop853_manifold_16384.md)"
+            pipe["source"] = ("from profiles/traffic_dop853_manifold.json (ncu of the dominant launch, "
+                              "profiles/dop853_manifold_16384.md), not measured in this run")
         step_achieved = flops / (kernel_ms * 1e-3) / 1e12
         if dom is not None:
             g, dom_ms, dom_att = dom
@@ -665,7 +857,8 @@ def main():
                "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                             "frac": achieved / peak if peak else None, "traffic": traffic,
                             "traffic_scope": "DRAM bytes of one launch of the dominant kernel (the timed launch "
-                                             "above, captured by ncu through its NVTX range)",
+                                             "above, captured by ncu through its NVTX range); from "
+                                             "profiles/traffic_dop853_manifold.json, not measured in this run",
                             "peak_source": "measured: DFMA throughput probe (hg_probe_fp64_peak) on this GPU; "
                                            "MEASURED_PEAKS.json has no FP64 entry",
                             "flops_per_attempted_step": FLOPS_PER_ATTEMPT_D6,
@@ -678,6 +871,8 @@ def main():
                              "form": f"one kernel call per trajectory (reference call granularity), "
                                      f"{n_plain}-trajectory sample"},
                "library": os.path.basename(_lib.load()._name)}
+        if secondary is not None:
+            out["secondary"] = secondary
         print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()

@@ -33,8 +33,10 @@ EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg
             "hg_propagate_dop853_scheduled", "hg_get_counter", "hg_radius_best", "hg_nearest_neighbor", "hg_connection_refine",
             "hg_newton_opts_default", "hg_correct_halo", "hg_serve_config_default", "hg_serve_create",
             "hg_serve_destroy", "hg_serve_submit", "hg_serve_poll", "hg_serve_wait", "hg_serve_fetch",
-            "hg_serve_cancel", "hg_serve_stats", "hg_selftest_bounded_wait", "hg_host_pow")
+            "hg_serve_cancel", "hg_serve_stats", "hg_selftest_bounded_wait", "hg_host_pow", "hg_reserve",
+            "hg_reserve_correct", "hg_points_workspace_bytes")
 HG_COUNTER_KERNEL_LAUNCHES = 1
+HG_COUNTER_ALLOCATIONS = 2
 HG_RUNNING = -1
 HG_TUNE_BLOCK_THREADS = 1
 HG_TUNE_DOP853_LANES_D6 = 2
@@ -71,7 +73,8 @@ class hg_newton_opts(C.Structure):
 
 
 class hg_serve_config(C.Structure):
-    _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_longlong), ("max_concurrent", C.c_int)]
+    _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_longlong), ("max_concurrent", C.c_int),
+                ("staging_bytes", C.c_longlong)]
 
 
 class hg_config(C.Structure):
@@ -135,9 +138,12 @@ def load(build_if_missing=True):
         L.hg_set_tuning.restype = C.c_int
         L.hg_get_tuning.argtypes = [_P, C.c_int, C.POINTER(C.c_int)]
         L.hg_get_tuning.restype = C.c_int
-        L.hg_radius_best.argtypes = [C.c_int, _P, _P, C.c_int, _P, _P, C.c_double, C.c_double, _P, _P, _P, _P]
+        L.hg_points_workspace_bytes.argtypes = [C.c_int]
+        L.hg_points_workspace_bytes.restype = C.c_longlong
+        L.hg_radius_best.argtypes = [C.c_int, _P, _P, C.c_int, _P, _P, C.c_double, C.c_double, _P, _P, _P, _P,
+                                     C.c_longlong, _P]
         L.hg_radius_best.restype = C.c_int
-        L.hg_nearest_neighbor.argtypes = [C.c_int, _P, _P, C.c_double, _P, _P]
+        L.hg_nearest_neighbor.argtypes = [C.c_int, _P, _P, C.c_double, _P, _P, C.c_longlong, _P]
         L.hg_nearest_neighbor.restype = C.c_int
         L.hg_connection_refine.argtypes = [C.c_int, _P, _P, _P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, _P, _P, _P,
                                            _P]
@@ -163,6 +169,10 @@ def load(build_if_missing=True):
                   "hg_serve_fetch", "hg_serve_cancel", "hg_serve_stats"):
             getattr(L, f).restype = C.c_int
         L.hg_get_counter.argtypes = [_P, C.c_int, C.POINTER(C.c_longlong)]
+        L.hg_reserve.argtypes = [_P, C.c_int, C.c_int, C.c_int]
+        L.hg_reserve.restype = C.c_int
+        L.hg_reserve_correct.argtypes = [_P, C.c_int]
+        L.hg_reserve_correct.restype = C.c_int
         L.hg_selftest_bounded_wait.argtypes = [_P, C.c_int, _P, _P]
         L.hg_selftest_bounded_wait.restype = C.c_int
         L.hg_host_pow.argtypes = [C.c_longlong, _P, C.c_double, _P]
@@ -205,6 +215,20 @@ class Handle:
         v = C.c_longlong(0)
         self.check(self.lib.hg_get_counter(self.ptr, HG_COUNTER_KERNEL_LAUNCHES, C.byref(v)))
         return v.value
+
+    def allocations(self):
+        """Device and pinned-host allocations made for this handle so far."""
+        v = C.c_longlong(0)
+        self.check(self.lib.hg_get_counter(self.ptr, HG_COUNTER_ALLOCATIONS, C.byref(v)))
+        return v.value
+
+    def reserve(self, max_n, dim, max_hits):
+        """Size the event-refinement pool for calls up to these sizes (hg_reserve)."""
+        self.check(self.lib.hg_reserve(self.ptr, int(max_n), int(dim), int(max_hits)))
+
+    def reserve_correct(self, max_orbits):
+        """Size the corrector's buffers for up to max_orbits orbits (hg_reserve_correct)."""
+        self.check(self.lib.hg_reserve_correct(self.ptr, int(max_orbits)))
 
     def close(self):
         if getattr(self, "ptr", None):

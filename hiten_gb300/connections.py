@@ -51,6 +51,15 @@ class GpuSectionMatcher:
             t = torch.as_tensor(np.ascontiguousarray(pts, dtype=np.float64), device=self.device)
         return t[:, 0].contiguous(), t[:, 1].contiguous()
 
+    def _workspace(self, L, n):
+        """The FP32 point copy's workspace for n points (grown, then reused)."""
+        need = int(L.hg_points_workspace_bytes(int(n)))
+        ws = getattr(self, "_ws", None)
+        if ws is None or ws.numel() < max(need, 256):
+            ws = torch.empty(max(need, 256), dtype=torch.uint8, device=self.device)
+            self._ws = ws
+        return ws, ws.numel()
+
     def radius_best(self, q, r, eps, coord_max):
         L = _lib.load()
         nq, nr = q.shape[0], r.shape[0]
@@ -60,9 +69,10 @@ class GpuSectionMatcher:
         bi = torch.empty(nq, dtype=torch.int32, device=self.device)
         bd = torch.empty(nq, dtype=torch.float64, device=self.device)
         st = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        ws, wsb = self._workspace(L, nr)
         with torch.cuda.device(self.device):
             rc = L.hg_radius_best(nq, P._ptr(qx), P._ptr(qy), nr, P._ptr(rx), P._ptr(ry), float(eps), float(coord_max),
-                                  P._ptr(cnt), P._ptr(bi), P._ptr(bd), st)
+                                  P._ptr(cnt), P._ptr(bi), P._ptr(bd), P._ptr(ws), wsb, st)
         if rc != _lib.HG_OK:
             raise _lib.HitenGpuError(rc, "hg_radius_best failed")
         return cnt.cpu().numpy().astype(np.int64), bi.cpu().numpy().astype(np.int64), bd.cpu().numpy()
@@ -73,8 +83,9 @@ class GpuSectionMatcher:
         x, y = self._xy(p)
         out = torch.empty(n, dtype=torch.int32, device=self.device)
         st = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        ws, wsb = self._workspace(L, n)
         with torch.cuda.device(self.device):
-            rc = L.hg_nearest_neighbor(n, P._ptr(x), P._ptr(y), float(coord_max), P._ptr(out), st)
+            rc = L.hg_nearest_neighbor(n, P._ptr(x), P._ptr(y), float(coord_max), P._ptr(out), P._ptr(ws), wsb, st)
         if rc != _lib.HG_OK:
             raise _lib.HitenGpuError(rc, "hg_nearest_neighbor failed")
         return out.cpu().numpy().astype(np.int64)

@@ -72,6 +72,7 @@ class GpuShootingBackend:
         self.o = options or HaloCorrectionOptions()
         self.device = device
         self.launches = 0
+        self.attempts = {6: 0, 42: 0}  # attempted DOP853 steps of the event and STM legs
         import torch
         dev = P._device(device)
         self.spec_traj = 20 * torch.cuda.get_device_properties(dev).multi_processor_count
@@ -83,6 +84,7 @@ class GpuShootingBackend:
         r = P.propagate_dop853(x_full, 0.0, span, self.mu, rtol=self.o.event_rtol, atol=self.o.event_atol,
                                max_step=np.inf, event=ev, device=self.device)
         self.launches += 1
+        self.attempts[6] += int((r.n_accept + r.n_reject).sum())
         n = r.n_hits.cpu().numpy()
         t_rel = r.hit_t[:, 0].cpu().numpy()
         x_ev = r.hit_y[:, 0, :].cpu().numpy()
@@ -96,6 +98,7 @@ class GpuShootingBackend:
                                atol=self.o.stm_atol, max_step=1e4, flip=(36, 42), n_samples=int(self.o.steps),
                                sample_last_only=True, device=self.device)
         self.launches += 1
+        self.attempts[42] += int((r.n_accept + r.n_reject).sum())
         return r.samples[0, :, :36].cpu().numpy().reshape(-1, 6, 6)
 
 
@@ -289,6 +292,27 @@ def correct_halo(guesses, mu, options=None, backend=None, device=None):
     x0[:, ctrl] = params
     return HaloCorrectionResult(x0=x0, half_period=tev_out, period=2.0 * tev_out, iterations=iters,
                                 residual_norm=rnorm_out, status=status, launches=getattr(be, "launches", 0))
+
+
+def newton_step_norms(x0, mu, options=None, backend=None, device=None):
+    """||dx||_inf of the Newton correction one more iteration would take at
+    each state x0 (N, 6): the residual at the half-period crossing, the STM
+    there and the step of the 2x2 solve (uncapped), as in correct_halo.  At a
+    converged orbit this is the distance the iteration still sees to its
+    fixed point; NaN where the crossing is not found."""
+    o = options or HaloCorrectionOptions()
+    be = backend or GpuShootingBackend(mu, o, device=device)
+    x = np.atleast_2d(np.asarray(x0, dtype=np.float64))
+    t_ev, x_ev, found = be.events(x)
+    out = np.full(len(x), np.nan)
+    if not found.any():
+        return out
+    xs, te, xe = x[found], t_ev[found], x_ev[found]
+    r = xe[:, [3, 5]]
+    Phi = be.stm(xs, te)
+    J = Phi[:, [3, 5], :][:, :, [0, 4]] - halo_quadratic_term(xe, Phi, mu)
+    out[found] = np.max(np.abs(solve_delta(J, r, o.cond_threshold)), axis=1)
+    return out
 
 
 def correct_halo_native(guesses, mu, options=None, device=None):

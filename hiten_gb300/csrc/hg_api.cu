@@ -1,6 +1,9 @@
 // C ABI of the propagation library (declarations and contracts in
-// include/hitengpu.h).  Owns the per-handle scratch (the lane-refill counter)
-// so that no hot call allocates.
+// include/hitengpu.h).  Owns the per-handle scratch: the lane-refill
+// counters and the pinned live-count word (allocated in hg_create), the
+// record pool of deferred event refinement and the corrector's buffers
+// (sized by hg_reserve / hg_reserve_correct, or grown on first use); every
+// allocation is counted (HG_COUNTER_ALLOCATIONS).
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -8,6 +11,7 @@
 
 #include <new>
 
+#include "hg_internal.h"
 #include "hg_kernels.cuh"
 #include "hg_pair.cuh"
 #include "hitengpu.h"
@@ -27,7 +31,10 @@ struct hg_handle {
   int* host_count = nullptr;  // pinned: live-trajectory count read back between segments
   char* scratch = nullptr;    // grow-only: saved crossing steps of single-pass calls
   long long scratch_bytes = 0;
+  char* corr = nullptr;       // grow-only: device buffers of hg_correct_halo
+  long long corr_bytes = 0;
   long long launches = 0;   // kernels launched through this handle
+  long long allocs = 0;     // device and pinned-host allocations made for this handle
   char err[512] = {0};
 };
 
@@ -253,18 +260,25 @@ int refine_pending(hg_handle* h, const hg::DopParams& p, int dim, cudaStream_t s
   return dim == 6 ? launch_refine<1>(h, p, s) : launch_refine<7>(h, p, s);
 }
 
-int ensure_scratch(hg_handle* h, long long bytes) {
-  if (bytes <= h->scratch_bytes) return HG_OK;
-  if (h->scratch) cudaFree(h->scratch);
-  h->scratch = nullptr;
-  h->scratch_bytes = 0;
-  const long long want = bytes + bytes / 4;
-  if (cudaMalloc(&h->scratch, (size_t)want) != cudaSuccess) {
-    h->scratch = nullptr;
-    return fail(h, HG_ERR_CUDA, "cudaMalloc of %lld bytes of refinement scratch failed", want);
+// Grow-only device buffer of the handle: a no-op (no allocation) when it
+// already holds `bytes`.  `slack` adds a quarter for buffers sized per call.
+int grow(hg_handle* h, char** buf, long long* have, long long bytes, bool slack, const char* what) {
+  if (bytes <= *have) return HG_OK;
+  if (*buf) cudaFree(*buf);
+  *buf = nullptr;
+  *have = 0;
+  const long long want = slack ? bytes + bytes / 4 : bytes;
+  if (cudaMalloc(buf, (size_t)want) != cudaSuccess) {
+    *buf = nullptr;
+    return fail(h, HG_ERR_CUDA, "cudaMalloc of %lld bytes of %s failed", want, what);
   }
-  h->scratch_bytes = want;
+  ++h->allocs;
+  *have = want;
   return HG_OK;
+}
+
+int ensure_scratch(hg_handle* h, long long bytes) {
+  return grow(h, &h->scratch, &h->scratch_bytes, bytes, true, "refinement scratch");
 }
 
 // Launch shape of a DOP853 kernel: threads per block, dynamic shared memory
@@ -499,9 +513,16 @@ int hg_create(const hg_config* cfg, hg_handle** out) {
   cudaSetDevice(h->device);
   cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
   cudaDeviceGetAttribute(&h->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, h->device);
-  const cudaError_t e = cudaMalloc(&h->counters, 64 * sizeof(int));
+  cudaError_t e = cudaMalloc(&h->counters, 64 * sizeof(int));
+  if (e == cudaSuccess) {
+    ++h->allocs;
+    e = cudaHostAlloc(&h->host_count, sizeof(int), cudaHostAllocDefault);
+    if (e == cudaSuccess) ++h->allocs;
+    else h->host_count = nullptr;
+  }
   cudaSetDevice(prev);
   if (e != cudaSuccess) {
+    if (h->counters) cudaFree(h->counters);
     delete h;
     return HG_ERR_CUDA;
   }
@@ -514,8 +535,19 @@ int hg_destroy(hg_handle* h) {
   if (h->counters) cudaFree(h->counters);
   if (h->host_count) cudaFreeHost(h->host_count);
   if (h->scratch) cudaFree(h->scratch);
+  if (h->corr) cudaFree(h->corr);
   delete h;
   return HG_OK;
+}
+
+int hg_reserve(hg_handle* h, int max_N, int dim, int max_hits) {
+  if (!h) return HG_ERR_ARGS;
+  if (max_N < 0 || (dim != 6 && dim != 42) || max_hits < 0)
+    return fail(h, HG_ERR_ARGS, "hg_reserve: bad sizes (N %d, dim %d, max_hits %d)", max_N, dim, max_hits);
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, HG_ERR_CUDA, "cudaSetDevice");
+  const long long bytes = refine_area_bytes(max_N, dim, max_hits);
+  if (bytes > h->refine_pool_max) return HG_OK;  // such calls refine inline and use no pool
+  return grow(h, &h->scratch, &h->scratch_bytes, bytes, false, "refinement scratch");
 }
 
 const char* hg_last_error_string(hg_handle* h) { return h ? h->err : "null handle"; }
@@ -730,12 +762,6 @@ int hg_propagate_dop853_scheduled(hg_handle* h, double mu, int dim, int N, const
   int rc = dop853_setup(h, mu, dim, N, y0, ld, t0_arr, tmax_arr, t0, tmax, opts, ev, n_samples, sample_last_only,
                         y_samples, y_end, t_end, hit_t, hit_y, n_hits, n_accept, n_reject, status, p);
   if (rc != HG_OK || N == 0) return rc;
-  if (!h->host_count) {
-    if (cudaHostAlloc(&h->host_count, sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
-      h->host_count = nullptr;
-      return fail(h, HG_ERR_CUDA, "cudaHostAlloc failed");
-    }
-  }
   SegWs w;
   seg_ws_layout(N, dim, ws_hits, (char*)workspace, &w);
   cudaStream_t s = (cudaStream_t)stream;
@@ -820,6 +846,7 @@ int hg_set_tuning(hg_handle* h, int key, int value) {
 int hg_get_counter(hg_handle* h, int key, long long* value) {
   if (!h || !value) return HG_ERR_ARGS;
   if (key == HG_COUNTER_KERNEL_LAUNCHES) *value = h->launches;
+  else if (key == HG_COUNTER_ALLOCATIONS) *value = h->allocs;
   else return fail(h, HG_ERR_ARGS, "unknown counter %d", key);
   return HG_OK;
 }
@@ -868,3 +895,21 @@ int hg_probe_fp64_peak(hg_handle* h, double* tflops) {
 }
 
 }  // extern "C"
+
+// Library-internal access to the handle for the other translation units
+// (hg_internal.h): not part of the C ABI.
+namespace hg_internal {
+
+int correct_buffers(hg_handle* h, long long bytes, void** out) {
+  *out = nullptr;
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, HG_ERR_CUDA, "cudaSetDevice");
+  const int rc = grow(h, &h->corr, &h->corr_bytes, bytes, false, "corrector buffers");
+  *out = rc == HG_OK ? h->corr : nullptr;
+  return rc;
+}
+
+int reserve_refine(hg_handle* h, int N, int dim, int max_hits) { return hg_reserve(h, N, dim, max_hits); }
+
+int fail_msg(hg_handle* h, int code, const char* msg) { return fail(h, code, "%s", msg); }
+
+}  // namespace hg_internal

@@ -16,6 +16,7 @@
 // the factor-two slack absorbing its own rounding).  Radius screen: a pair
 // needs |dx|, |dy| <= eps, hence |dx_f|, |dy_f| <= T = (eps + 2^-22 R)(1 + 2^-20).
 #include <cuda_runtime.h>
+#include <stdint.h>
 #include <math.h>
 
 #include <algorithm>
@@ -341,11 +342,21 @@ __global__ void refine_pairs_kernel(int n, const int* __restrict__ I, const int*
   }
 }
 
-// FP32 copy of a point set in stream-ordered scratch (freed on the stream
-// after the search); nullptr on failure.
-float2* float2_copy(int n, const double* x, const double* y, cudaStream_t st) {
-  void* p = nullptr;
-  if (cudaMallocAsync(&p, (size_t)n * sizeof(float2), st) != cudaSuccess) return nullptr;
+long long points_ws_bytes(long long n) { return ((n * (long long)sizeof(float2)) + 255) & ~255LL; }
+
+// FP32 copy of a point set: into the caller's workspace when one is given
+// (*owned = false), else into stream-ordered scratch that the caller frees on
+// the stream after the search (*owned = true); nullptr on failure.
+float2* float2_copy(int n, const double* x, const double* y, void* ws, long long ws_bytes, bool* owned,
+                    cudaStream_t st) {
+  void* p = ws;
+  *owned = false;
+  if (p) {
+    if (ws_bytes < points_ws_bytes(n) || ((uintptr_t)p & 15) != 0) return nullptr;
+  } else {
+    if (cudaMallocAsync(&p, (size_t)n * sizeof(float2), st) != cudaSuccess) return nullptr;
+    *owned = true;
+  }
   const int blocks = (int)std::min<long long>(((long long)n + 255) / 256, 4096);
   to_float2_kernel<<<blocks, 256, 0, st>>>(n, x, y, (float2*)p);
   return (float2*)p;
@@ -355,15 +366,20 @@ float2* float2_copy(int n, const double* x, const double* y, cudaStream_t st) {
 
 extern "C" {
 
+long long hg_points_workspace_bytes(int n) { return n < 0 ? -1 : points_ws_bytes(n); }
+
 int hg_radius_best(int nq, const double* qx, const double* qy, int nr, const double* rx, const double* ry, double eps,
-                   double coord_max, int* count, int* best_idx, double* best_d2, void* stream) {
+                   double coord_max, int* count, int* best_idx, double* best_d2, void* workspace,
+                   long long workspace_bytes, void* stream) {
   if (nq < 0 || nr < 0 || !(eps >= 0.0) || !(coord_max >= 0.0)) return HG_ERR_ARGS;
+  if (workspace && (workspace_bytes < points_ws_bytes(nr) || ((uintptr_t)workspace & 15) != 0)) return HG_ERR_ARGS;
   if (nq == 0) return HG_OK;
   if (!qx || !qy || !count || !best_idx || !best_d2 || (nr > 0 && (!rx || !ry))) return HG_ERR_ARGS;
   const double T = (eps + 0x1p-22 * coord_max) * (1.0 + 0x1p-20);
   const float Tf = nextafterf((float)T, INFINITY);
   const cudaStream_t st = (cudaStream_t)stream;
-  float2* rf = nr > 0 ? float2_copy(nr, rx, ry, st) : nullptr;
+  bool owned = false;
+  float2* rf = nr > 0 ? float2_copy(nr, rx, ry, workspace, workspace_bytes, &owned, st) : nullptr;
   if (nr > 0 && !rf) return HG_ERR_CUDA;
   const int S = lanes_per_query(radius_best_kernel<8>, nq);
   const long long blocks = ((long long)nq * S + kBlock - 1) / kBlock;
@@ -375,19 +391,22 @@ int hg_radius_best(int nq, const double* qx, const double* qy, int nr, const dou
     radius_best_kernel<2><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, rf, eps * eps, Tf, count, best_idx, best_d2);
   else
     radius_best_kernel<1><<<(unsigned)blocks, kBlock, 0, st>>>(nq, qx, qy, nr, rx, ry, rf, eps * eps, Tf, count, best_idx, best_d2);
-  if (rf) cudaFreeAsync(rf, st);
+  if (owned) cudaFreeAsync(rf, st);
   return check("radius_best_kernel");
 }
 
-int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_max, int* out, void* stream) {
+int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_max, int* out, void* workspace,
+                        long long workspace_bytes, void* stream) {
   if (n < 0 || !(coord_max >= 0.0)) return HG_ERR_ARGS;
+  if (workspace && (workspace_bytes < points_ws_bytes(n) || ((uintptr_t)workspace & 15) != 0)) return HG_ERR_ARGS;
   if (n == 0) return HG_OK;
   if (!x || !y || !out) return HG_ERR_ARGS;
   // R and 2^-43 R^2 as FP32 values rounded up (the bound's constants), passed in FP64
   const double R = (double)nextafterf((float)coord_max, INFINITY);
   const double R2c = (double)nextafterf((float)(0x1p-43 * coord_max * coord_max), INFINITY);
   const cudaStream_t st = (cudaStream_t)stream;
-  float2* pf = float2_copy(n, x, y, st);
+  bool owned = false;
+  float2* pf = float2_copy(n, x, y, workspace, workspace_bytes, &owned, st);
   if (!pf) return HG_ERR_CUDA;
   const int S = lanes_per_query(nearest_kernel<8>, n);
   const long long blocks = ((long long)n * S + kBlock - 1) / kBlock;
@@ -399,7 +418,7 @@ int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_ma
     nearest_kernel<2><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, pf, R, R2c, out);
   else
     nearest_kernel<1><<<(unsigned)blocks, kBlock, 0, st>>>(n, x, y, pf, R, R2c, out);
-  cudaFreeAsync(pf, st);
+  if (owned) cudaFreeAsync(pf, st);
   return check("nearest_kernel");
 }
 

@@ -19,11 +19,12 @@
 #include <algorithm>
 #include <vector>
 
+#include "hg_internal.h"
 #include "hitengpu.h"
 
 namespace {
 
-// A view into the call's single device allocation (Shooter::arena).
+// A view into the handle's corrector buffers (Shooter::arena).
 struct DevBuf {
   void* p = nullptr;
   double* d() const { return (double*)p; }
@@ -38,15 +39,14 @@ struct Shooter {
   int cap;
   // event leg (6-dim), STM leg (42-dim)
   DevBuf y6, ye6, te, ht, hy, nh, na, nr, st, y42, ye42, te42, tm, smp, na42, nr42, st42;
-  void* arena = nullptr;  // one cudaMalloc per call, carved into the buffers above
+  void* arena = nullptr;  // the handle's corrector buffers, carved into the views above
   std::vector<double> hbuf;
   std::vector<int> ibuf;
 
-  ~Shooter() {
-    if (arena) cudaFree(arena);
-  }
-
-  bool init() {
+  // Byte sizes of the views for `cap` orbits, in carving order; returns the
+  // total (256-byte aligned parts).  With `carve` the views are set from
+  // `base`.
+  size_t layout(char* base, bool carve) {
     const size_t n = (size_t)cap;
     struct Part {
       DevBuf* b;
@@ -56,18 +56,22 @@ struct Shooter {
                  {&ye42, 42 * n * 8}, {&te42, n * 8},     {&tm, n * 8},      {&smp, 42 * n * 8}, {&na42, n * 4},
                  {&nr42, n * 4},     {&st42, n * 4}};
     auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    size_t total = 0;
-    for (const Part& q : parts) total += up(q.bytes ? q.bytes : 8);
-    if (cudaMalloc(&arena, total) != cudaSuccess) {
-      arena = nullptr;
-      return false;
-    }
     size_t off = 0;
     for (const Part& q : parts) {
-      q.b->p = (char*)arena + off;
+      if (carve) q.b->p = base + off;
       off += up(q.bytes ? q.bytes : 8);
     }
-    return true;
+    return off;
+  }
+
+  // Buffers from the handle (no allocation once hg_reserve_correct covered
+  // `cap` orbits).
+  int init() {
+    const size_t total = layout(nullptr, false);
+    const int rc = hg_internal::correct_buffers(h, (long long)total, &arena);
+    if (rc != HG_OK) return rc;
+    layout((char*)arena, true);
+    return HG_OK;
   }
 
   // First y = 0 crossing of every state x (M x 6, row-major): t_event = 1e-12 +
@@ -207,6 +211,18 @@ void hg_newton_opts_default(hg_newton_opts* o) {
   o->steps = 500;
 }
 
+int hg_reserve_correct(hg_handle* h, int max_orbits) {
+  if (!h) return HG_ERR_ARGS;
+  if (max_orbits < 0) return hg_internal::fail_msg(h, HG_ERR_ARGS, "hg_reserve_correct: max_orbits < 0");
+  hg_newton_opts o;
+  hg_newton_opts_default(&o);
+  Shooter sh{h, 0.0, o, nullptr, max_orbits};
+  int rc = sh.init();
+  if (rc != HG_OK) return rc;
+  // the half-period legs refine one crossing per orbit
+  return hg_internal::reserve_refine(h, max_orbits, 6, 1);
+}
+
 int hg_correct_halo(hg_handle* h, double mu, int N, double* x, long long ld, double* half_period, int* iterations,
                     double* residual, int* status, const hg_newton_opts* opts, void* stream) {
   if (!h || N < 0 || (N > 0 && (!x || !half_period || !iterations || !residual || !status)) || ld < N)
@@ -218,7 +234,10 @@ int hg_correct_halo(hg_handle* h, double mu, int N, double* x, long long ld, dou
   if (o.max_attempts < 1 || !(o.tol > 0) || o.steps < 2) return HG_ERR_ARGS;
   cudaStream_t s = (cudaStream_t)stream;
   Shooter sh{h, mu, o, s, N};
-  if (!sh.init()) return HG_ERR_CUDA;
+  {
+    const int rc0 = sh.init();
+    if (rc0 != HG_OK) return rc0;
+  }
   // inputs: SoA [6][ld] on the device
   std::vector<double> soa((size_t)6 * N), base((size_t)N * 6);
   for (int c = 0; c < 6; ++c)

@@ -1,0 +1,17 @@
+// Library-internal functions shared between translation units; not part of
+// the C ABI (include/hitengpu.h).
+#pragma once
+
+#include "hitengpu.h"
+
+namespace hg_internal {
+
+// The handle's grow-only device buffer of hg_correct_halo: at least `bytes`
+// (allocated, and counted, only when the buffer is smaller).
+int correct_buffers(hg_handle* h, long long bytes, void** out);
+// hg_reserve from inside the library.
+int reserve_refine(hg_handle* h, int N, int dim, int max_hits);
+// Record `msg` as the handle's last error and return `code`.
+int fail_msg(hg_handle* h, int code, const char* msg);
+
+}  // namespace hg_internal

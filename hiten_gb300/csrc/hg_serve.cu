@@ -1,12 +1,21 @@
 // Native request server for DOP853 propagation requests (continuous
 // batching).  Requests are host arrays; a worker thread merges every pending
 // request that shares a problem (mu, dim, span, options, event) into one
-// batch, admits batches while their device footprint fits the budget, runs
-// them concurrently on its own streams and handles (host-scheduled segments
-// for wide 6-dim batches), and parks each request's results on the host
-// until it is fetched.  Results are those of a direct hg_propagate_dop853
-// call on the request alone: trajectories never interact.
+// batch, admits batches while their device footprint fits the device arena,
+// runs them concurrently on its own streams and handles (host-scheduled
+// segments for wide 6-dim batches, one segment that finishes every
+// trajectory otherwise), and parks each request's results on the host until
+// it is fetched.  Results are those of a direct hg_propagate_dop853 call on
+// the request alone: trajectories never interact.
+//
+// Memory: hg_serve_create allocates a device arena of hbm_budget_bytes and a
+// pinned host staging arena of staging_bytes; every batch takes one block of
+// each (its inputs, outputs and segment workspace on the device; its inputs
+// and outputs in pinned memory, so its copies run asynchronously on its
+// stream) and returns them when it finishes, on success or failure.  Nothing
+// is allocated after creation.
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <string.h>
 
 #include <algorithm>
@@ -48,24 +57,86 @@ struct Request {
   Clock::time_point submitted, finished;
 };
 
+// First-fit allocator over one fixed block of memory (offsets only).
+class Arena {
+ public:
+  void reset(long long size) {
+    size_ = size;
+    free_.clear();
+    if (size > 0) free_[0] = size;
+  }
+  long long size() const { return size_; }
+  // offset of a block of `bytes` (256-byte aligned), or -1
+  long long alloc(long long bytes) {
+    bytes = up(bytes);
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= bytes) {
+        const long long off = it->first, len = it->second;
+        free_.erase(it);
+        if (len > bytes) free_[off + bytes] = len - bytes;
+        return off;
+      }
+    }
+    return -1;
+  }
+  void release(long long off, long long bytes) {
+    bytes = up(bytes);
+    auto it = free_.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+  static long long up(long long x) { return (x + 255) & ~255LL; }
+  long long free_bytes() const {
+    long long t = 0;
+    for (const auto& f : free_) t += f.second;
+    return t;
+  }
+
+ private:
+  long long size_ = 0;
+  std::map<long long, long long> free_;  // offset -> length, disjoint, not adjacent
+};
+
+// Layout of a batch of n trajectories: the inputs and outputs (the same
+// layout on the device and in pinned staging) and, on the device only, the
+// segment workspace.  y0 [d][n]; outputs y_end [d][n], t_end [n],
+// hit_t [hits][n], hit_y [hits][d][n], then four int arrays [n].
+struct Layout {
+  long long off_ye, off_te, off_ht, off_hy, off_i, io_bytes, ws_bytes;
+  Layout(int d, int n, int hits) {
+    const long long nn = n;
+    off_ye = Arena::up(8 * d * nn);
+    off_te = off_ye + 8 * d * nn;
+    off_ht = off_te + 8 * nn;
+    off_hy = off_ht + 8 * hits * nn;
+    off_i = off_hy + 8 * (long long)hits * d * nn;
+    io_bytes = Arena::up(off_i + 16 * nn);
+    ws_bytes = Arena::up(hg_dop853_segmented_workspace_bytes(n, d, hits));
+  }
+  long long device_bytes() const { return io_bytes + ws_bytes; }
+  long long out_bytes() const { return io_bytes - off_ye; }
+};
+
 struct Batch {
   Key key;
   std::vector<std::shared_ptr<Request>> reqs;
   int n = 0;
-  long long bytes = 0;
   int slot = -1;
-  void* dev = nullptr;
-  std::vector<double> h_y0, h_yend, h_tend, h_hitt, h_hity;
-  std::vector<int> h_nh, h_na, h_nr, h_st;
+  long long dev_off = -1, dev_len = 0, stg_off = -1, stg_len = 0;  // arena blocks
   std::atomic<int> finished{0};
   std::thread runner;
   int rc = HG_OK;
 };
-
-long long batch_bytes(int dim, int n, int hits) {
-  const long long per = 8LL * dim * 2 + 8 + 4 * 4 + (hits > 0 ? (8LL + 8LL * dim) * hits : 0);
-  return per * n + (hits > 0 ? (15LL * dim + 3) * 8 * (long long)n * hits : 0) + 4096;
-}
 
 }  // namespace
 
@@ -80,90 +151,84 @@ struct hg_server {
   std::vector<hg_handle*> handles;
   std::vector<char> slot_busy;
   long long next_id = 1;
-  long long in_use = 0;
+  char* dev_base = nullptr;  // device arena (hbm_budget_bytes)
+  char* stg_base = nullptr;  // pinned staging arena (staging_bytes)
+  Arena dev_arena, stg_arena;
   bool stop = false;
   std::thread worker;
   std::vector<double> latencies_ms;
   long long batches = 0;
 
+  // Copies in, propagation and copies out of one admitted batch on its
+  // slot's stream (runs on the batch's own thread; the blocks are owned by
+  // the batch and returned in finish()).
   int launch(Batch& b) {
     const Key& k = b.key;
     const int d = k.dim, n = b.n;
     const int hits = k.has_ev ? k.ev.max_hits : 0;
-    // device layout: y0, y_end [d][n]; t_end [n]; hit_t [hits][n]; hit_y [hits][d][n]; 4 int arrays [n]
-    const size_t off_y0 = 0, off_ye = off_y0 + 8ull * d * n, off_te = off_ye + 8ull * d * n,
-                 off_ht = off_te + 8ull * n, off_hy = off_ht + 8ull * hits * n, off_i = off_hy + 8ull * hits * d * n;
-    const size_t total = off_i + 16ull * n + 256;
+    const Layout L(d, n, hits);
     cudaStream_t s = streams[b.slot];
-    cudaSetDevice(cfg.device);
-    if (cudaMallocAsync(&b.dev, total, s) != cudaSuccess) return HG_ERR_CUDA;
-    char* base = (char*)b.dev;
-    b.h_y0.assign((size_t)d * n, 0.0);
+    if (cudaSetDevice(cfg.device) != cudaSuccess) return HG_ERR_CUDA;
+    char* dev = dev_base + b.dev_off;
+    char* stg = stg_base + b.stg_off;
+    double* h_y0 = (double*)stg;
     int o = 0;
     for (auto& r : b.reqs) {
       for (int i = 0; i < r->n; ++i)
-        for (int c = 0; c < d; ++c) b.h_y0[(size_t)c * n + o + i] = r->y0[(size_t)i * d + c];
+        for (int c = 0; c < d; ++c) h_y0[(size_t)c * n + o + i] = r->y0[(size_t)i * d + c];
       o += r->n;
     }
-    if (cudaMemcpyAsync(base + off_y0, b.h_y0.data(), 8ull * d * n, cudaMemcpyHostToDevice, s) != cudaSuccess)
-      return HG_ERR_CUDA;
-    double* ye = (double*)(base + off_ye);
-    double* te = (double*)(base + off_te);
-    double* ht = hits ? (double*)(base + off_ht) : nullptr;
-    double* hy = hits ? (double*)(base + off_hy) : nullptr;
-    int* nh = (int*)(base + off_i);
+    if (cudaMemcpyAsync(dev, stg, 8ull * d * n, cudaMemcpyHostToDevice, s) != cudaSuccess) return HG_ERR_CUDA;
+    double* ye = (double*)(dev + L.off_ye);
+    double* te = (double*)(dev + L.off_te);
+    double* ht = hits ? (double*)(dev + L.off_ht) : nullptr;
+    double* hy = hits ? (double*)(dev + L.off_hy) : nullptr;
+    int* nh = (int*)(dev + L.off_i);
     int* na = nh + n;
     int* nr = na + n;
     int* st = nr + n;
+    void* ws = dev + L.io_bytes;
     if (hits && cudaMemsetAsync(ht, 0xFF, 8ull * hits * n * (1 + d), s) != cudaSuccess) return HG_ERR_CUDA;
-    int rc = HG_OK;
+    if (!hits && cudaMemsetAsync(nh, 0, 4ull * n, s) != cudaSuccess) return HG_ERR_CUDA;
+    int rc;
     if (d == 6 && n >= 4096) {
       // wide batches: host-scheduled segments (synchronous on this stream)
-      const long long wsb = hg_dop853_segmented_workspace_bytes(n, d, hits);
-      void* ws = nullptr;
-      if (cudaMallocAsync(&ws, (size_t)wsb, s) != cudaSuccess) return HG_ERR_CUDA;
-      rc = hg_propagate_dop853_scheduled(handles[b.slot], k.mu, d, n, (const double*)(base + off_y0), n, nullptr,
-                                         nullptr, k.t0, k.tmax, &k.o, k.has_ev ? &k.ev : nullptr, 0, 0, nullptr, ye,
-                                         te, ht, hy, nh, na, nr, st, ws, wsb, s);
-      cudaFreeAsync(ws, s);
+      rc = hg_propagate_dop853_scheduled(handles[b.slot], k.mu, d, n, (const double*)dev, n, nullptr, nullptr, k.t0,
+                                         k.tmax, &k.o, k.has_ev ? &k.ev : nullptr, 0, 0, nullptr, ye, te, ht, hy,
+                                         hits ? nh : nullptr, na, nr, st, ws, L.ws_bytes, s);
     } else {
-      rc = hg_propagate_dop853(handles[b.slot], k.mu, d, n, (const double*)(base + off_y0), n, nullptr, nullptr,
-                               k.t0, k.tmax, &k.o, k.has_ev ? &k.ev : nullptr, 0, 0, nullptr, ye, te, ht, hy, nh, na,
-                               nr, st, s);
+      // one segment long enough to finish every trajectory (same results as
+      // a single pass; the event records live in the batch's workspace)
+      const long long seg = std::min<long long>(k.o.max_steps + 1, INT_MAX);
+      rc = hg_propagate_dop853_segmented(handles[b.slot], k.mu, d, n, (const double*)dev, n, nullptr, nullptr, k.t0,
+                                         k.tmax, &k.o, k.has_ev ? &k.ev : nullptr, 0, 0, nullptr, ye, te, ht, hy,
+                                         hits ? nh : nullptr, na, nr, st, (int)seg, 1, 0, ws, L.ws_bytes, s);
     }
     if (rc != HG_OK) {
-      cudaFreeAsync(b.dev, s);
-      b.dev = nullptr;
       cudaStreamSynchronize(s);
       return rc;
     }
-    b.h_yend.resize((size_t)d * n);
-    b.h_tend.resize(n);
-    b.h_hitt.resize((size_t)hits * n);
-    b.h_hity.resize((size_t)hits * d * n);
-    b.h_nh.resize(n);
-    b.h_na.resize(n);
-    b.h_nr.resize(n);
-    b.h_st.resize(n);
-    if (cudaMemcpyAsync(b.h_yend.data(), ye, 8ull * d * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(b.h_tend.data(), te, 8ull * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(b.h_nh.data(), nh, 4ull * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(b.h_na.data(), na, 4ull * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(b.h_nr.data(), nr, 4ull * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(b.h_st.data(), st, 4ull * n, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    if (cudaMemcpyAsync(stg + L.off_ye, dev + L.off_ye, (size_t)L.out_bytes(), cudaMemcpyDeviceToHost, s) !=
+        cudaSuccess) {
+      cudaStreamSynchronize(s);
       return HG_ERR_CUDA;
-    if (hits && (cudaMemcpyAsync(b.h_hitt.data(), ht, 8ull * hits * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-                 cudaMemcpyAsync(b.h_hity.data(), hy, 8ull * hits * d * n, cudaMemcpyDeviceToHost, s) !=
-                     cudaSuccess))
-      return HG_ERR_CUDA;
-    cudaFreeAsync(b.dev, s);
-    b.dev = nullptr;
+    }
     return cudaStreamSynchronize(s) == cudaSuccess ? HG_OK : HG_ERR_CUDA;
   }
 
   // scatter a finished batch to its requests (called with the lock held)
   void finish(Batch& b) {
     const int d = b.key.dim, n = b.n, hits = b.key.has_ev ? b.key.ev.max_hits : 0;
+    const Layout L(d, n, hits);
+    const char* stg = stg_base + b.stg_off;
+    const double* h_yend = (const double*)(stg + L.off_ye);
+    const double* h_tend = (const double*)(stg + L.off_te);
+    const double* h_hitt = (const double*)(stg + L.off_ht);
+    const double* h_hity = (const double*)(stg + L.off_hy);
+    const int* h_nh = (const int*)(stg + L.off_i);
+    const int* h_na = h_nh + n;
+    const int* h_nr = h_na + n;
+    const int* h_st = h_nr + n;
     const auto now = Clock::now();
     int o = 0;
     for (auto& r : b.reqs) {
@@ -179,16 +244,16 @@ struct hg_server {
         r->hit_y.resize((size_t)m * hits * d);
         for (int i = 0; i < m; ++i) {
           const int g = o + i;
-          for (int c = 0; c < d; ++c) r->y_end[(size_t)i * d + c] = b.h_yend[(size_t)c * n + g];
-          r->t_end[i] = b.h_tend[g];
-          r->n_hits[i] = hits ? b.h_nh[g] : 0;
-          r->n_acc[i] = b.h_na[g];
-          r->n_rej[i] = b.h_nr[g];
-          r->status[i] = b.h_st[g];
+          for (int c = 0; c < d; ++c) r->y_end[(size_t)i * d + c] = h_yend[(size_t)c * n + g];
+          r->t_end[i] = h_tend[g];
+          r->n_hits[i] = hits ? h_nh[g] : 0;
+          r->n_acc[i] = h_na[g];
+          r->n_rej[i] = h_nr[g];
+          r->status[i] = h_st[g];
           for (int j = 0; j < hits; ++j) {
-            r->hit_t[(size_t)i * hits + j] = b.h_hitt[(size_t)j * n + g];
+            r->hit_t[(size_t)i * hits + j] = h_hitt[(size_t)j * n + g];
             for (int c = 0; c < d; ++c)
-              r->hit_y[((size_t)i * hits + j) * d + c] = b.h_hity[((size_t)j * d + c) * n + g];
+              r->hit_y[((size_t)i * hits + j) * d + c] = h_hity[((size_t)j * d + c) * n + g];
           }
         }
         r->state = 2;
@@ -200,10 +265,23 @@ struct hg_server {
       latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->submitted).count());
       o += m;
     }
-    in_use -= b.bytes;
+    dev_arena.release(b.dev_off, b.dev_len);
+    stg_arena.release(b.stg_off, b.stg_len);
     slot_busy[b.slot] = 0;
     ++batches;
   }
+
+  // A request that can never fit the arenas fails at once (lock held).
+  void reject(const std::shared_ptr<Request>& r) {
+    r->state = 3;
+    r->error = HG_ERR_ARGS;
+    r->finished = Clock::now();
+    latencies_ms.push_back(std::chrono::duration<double, std::milli>(r->finished - r->submitted).count());
+  }
+
+  long long dev_free_bytes() const { return free_total(dev_arena); }
+  long long stg_free_bytes() const { return free_total(stg_arena); }
+  static long long free_total(const Arena& a) { return a.free_bytes(); }
 
   void run() {
     std::unique_lock<std::mutex> lk(mu);
@@ -221,18 +299,25 @@ struct hg_server {
         }
       }
       if (stop && pending.empty() && running.empty()) return;
-      // admit: merge pending requests per problem, in arrival order
+      // admit: merge pending requests per problem, in arrival order, while
+      // the merged batches' blocks fit what the arenas have free
       std::vector<std::unique_ptr<Batch>> admit;
       if (!pending.empty()) {
         std::map<Key, Batch*> open;
         std::deque<std::shared_ptr<Request>> keep;
-        long long budget = cfg.hbm_budget_bytes - in_use;
+        long long dev_free = dev_free_bytes(), stg_free = stg_free_bytes();
         for (auto& r : pending) {
           const int hits = r->key.has_ev ? r->key.ev.max_hits : 0;
-          const long long bytes = batch_bytes(r->key.dim, r->n, hits);
+          const Layout alone(r->key.dim, r->n, hits);
+          if (alone.device_bytes() > dev_arena.size() || alone.io_bytes > stg_arena.size()) {
+            reject(r);
+            continue;
+          }
           auto it = open.find(r->key);
           Batch* b = it == open.end() ? nullptr : it->second;
-          const bool room = bytes <= budget || (in_use == 0 && admit.empty() && b == nullptr);
+          const Layout before(r->key.dim, b ? b->n : 0, hits), after(r->key.dim, (b ? b->n : 0) + r->n, hits);
+          const long long dd = b ? after.device_bytes() - before.device_bytes() : after.device_bytes();
+          const long long ds = b ? after.io_bytes - before.io_bytes : after.io_bytes;
           int free_slot = -1;
           if (!b) {
             for (size_t sidx = 0; sidx < slot_busy.size(); ++sidx)
@@ -245,7 +330,7 @@ struct hg_server {
                 }
               }
           }
-          if (room && (b || free_slot >= 0)) {
+          if (dd <= dev_free && ds <= stg_free && (b || free_slot >= 0)) {
             if (!b) {
               admit.emplace_back(new Batch());
               b = admit.back().get();
@@ -255,18 +340,45 @@ struct hg_server {
             }
             b->reqs.push_back(r);
             b->n += r->n;
-            b->bytes += bytes;
-            budget -= bytes;
-            r->state = 1;
+            dev_free -= dd;
+            stg_free -= ds;
           } else {
             keep.push_back(r);
           }
         }
+        // blocks for the admitted batches; a batch that does not fit the free
+        // blocks (fragmentation) goes back to waiting, in arrival order
+        std::vector<std::unique_ptr<Batch>> placed;
+        std::deque<std::shared_ptr<Request>> back;
+        for (auto& b : admit) {
+          const int hits = b->key.has_ev ? b->key.ev.max_hits : 0;
+          const Layout L(b->key.dim, b->n, hits);
+          b->dev_len = L.device_bytes();
+          b->stg_len = L.io_bytes;
+          b->dev_off = dev_arena.alloc(b->dev_len);
+          b->stg_off = b->dev_off >= 0 ? stg_arena.alloc(b->stg_len) : -1;
+          if (b->dev_off < 0 || b->stg_off < 0) {
+            if (b->dev_off >= 0) dev_arena.release(b->dev_off, b->dev_len);
+            for (auto& r : b->reqs) back.push_back(r);
+            continue;
+          }
+          for (auto& r : b->reqs) r->state = 1;
+          placed.push_back(std::move(b));
+        }
+        if (!back.empty()) {
+          // restore arrival order among the requests sent back and those kept
+          for (auto& r : keep) back.push_back(r);
+          std::stable_sort(back.begin(), back.end(),
+                           [](const std::shared_ptr<Request>& x, const std::shared_ptr<Request>& y) {
+                             return x->id < y->id;
+                           });
+          keep.swap(back);
+        }
         pending.swap(keep);
+        admit.swap(placed);
       }
       for (auto& b : admit) {
         slot_busy[b->slot] = 1;
-        in_use += b->bytes;
         Batch* bp = b.get();
         // each batch runs on its own thread (the scheduled driver waits on
         // its stream); completion wakes this loop
@@ -290,6 +402,7 @@ void hg_serve_config_default(hg_serve_config* c) {
   c->device = 0;
   c->hbm_budget_bytes = 8LL << 30;
   c->max_concurrent = 4;
+  c->staging_bytes = 1LL << 30;
 }
 
 int hg_serve_create(const hg_serve_config* cfg, hg_server** out) {
@@ -298,16 +411,31 @@ int hg_serve_create(const hg_serve_config* cfg, hg_server** out) {
   hg_serve_config c;
   hg_serve_config_default(&c);
   if (cfg) c = *cfg;
-  if (c.max_concurrent < 1 || c.max_concurrent > 64 || c.hbm_budget_bytes <= 0) return HG_ERR_ARGS;
+  if (c.max_concurrent < 1 || c.max_concurrent > 64 || c.hbm_budget_bytes <= 0 || c.staging_bytes <= 0)
+    return HG_ERR_ARGS;
   std::unique_ptr<hg_server> s(new hg_server());
   s->cfg = c;
   if (cudaSetDevice(c.device) != cudaSuccess) return HG_ERR_NO_DEVICE;
-  // a failure part way releases the streams and handles made so far (no worker runs yet)
+  // a failure part way releases what was made so far (no worker runs yet)
   auto release = [&s](int rc) {
     for (auto h : s->handles) hg_destroy(h);
     for (auto st : s->streams) cudaStreamDestroy(st);
+    if (s->dev_base) cudaFree(s->dev_base);
+    if (s->stg_base) cudaFreeHost(s->stg_base);
     return rc;
   };
+  if (cudaMalloc(&s->dev_base, (size_t)c.hbm_budget_bytes) != cudaSuccess) {
+    s->dev_base = nullptr;
+    cudaGetLastError();
+    return release(HG_ERR_CUDA);
+  }
+  if (cudaHostAlloc(&s->stg_base, (size_t)c.staging_bytes, cudaHostAllocDefault) != cudaSuccess) {
+    s->stg_base = nullptr;
+    cudaGetLastError();
+    return release(HG_ERR_CUDA);
+  }
+  s->dev_arena.reset(c.hbm_budget_bytes);
+  s->stg_arena.reset(c.staging_bytes);
   for (int i = 0; i < c.max_concurrent; ++i) {
     cudaStream_t st;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return release(HG_ERR_CUDA);
@@ -339,6 +467,8 @@ int hg_serve_destroy(hg_server* s) {
   if (s->worker.joinable()) s->worker.join();
   for (auto h : s->handles) hg_destroy(h);
   for (auto st : s->streams) cudaStreamDestroy(st);
+  if (s->dev_base) cudaFree(s->dev_base);
+  if (s->stg_base) cudaFreeHost(s->stg_base);
   delete s;
   return HG_OK;
 }

@@ -245,12 +245,14 @@ class NativeServer:
     that do not run this Python engine.  Requests with the same problem (mu,
     dimension, span, options, event) are merged; results equal direct calls."""
 
-    def __init__(self, device=0, hbm_budget_bytes=8 << 30, max_concurrent=4):
+    def __init__(self, device=0, hbm_budget_bytes=8 << 30, max_concurrent=4, staging_bytes=None):
         import ctypes as C
         from . import _lib
         self._C, self._lib = C, _lib
         self.L = _lib.load()
-        cfg = _lib.hg_serve_config(int(device), int(hbm_budget_bytes), int(max_concurrent))
+        if staging_bytes is None:
+            staging_bytes = min(int(hbm_budget_bytes), 1 << 30)
+        cfg = _lib.hg_serve_config(int(device), int(hbm_budget_bytes), int(max_concurrent), int(staging_bytes))
         self.ptr = C.c_void_p()
         rc = self.L.hg_serve_create(C.byref(cfg), C.byref(self.ptr))
         if rc != _lib.HG_OK:

@@ -11,8 +11,20 @@
  * row-major 6x6 STM Phi followed by the state (Phi[r][c] = y[6r + c],
  * state = y[36:42]).  Arithmetic is IEEE FP64 in the reference's operation
  * order (no contraction).  A handle is used by one host thread at a time;
- * separate handles may share a device.  No call allocates memory after
- * hg_create.
+ * separate handles may share a device.
+ *
+ * Allocation: hg_create allocates the handle's fixed scratch (refill
+ * counters, a pinned live-count word).  The record pool of deferred event
+ * refinement and the corrector's buffers are grow-only handle buffers: after
+ * hg_reserve(h, N, dim, max_hits) / hg_reserve_correct(h, orbits) no
+ * propagation or correction call on batches up to those sizes allocates
+ * device or pinned memory (HG_COUNTER_ALLOCATIONS counts every allocation
+ * made for a handle); without a reservation the first larger call grows the
+ * buffer once.  Segmented and scheduled DOP853 runs take a caller workspace;
+ * the connection searches take an optional caller workspace (NULL: a
+ * stream-ordered allocation per call); the no-alloc DOP853 entry point never
+ * allocates; the request server allocates its device and pinned arenas in
+ * hg_serve_create and nothing afterwards.
  */
 #ifndef HITENGPU_H
 #define HITENGPU_H
@@ -74,6 +86,13 @@ typedef struct {
 /* Replaces: nothing (lifecycle).  Creates a handle bound to cfg->device. */
 int hg_create(const hg_config* cfg, hg_handle** out);
 int hg_destroy(hg_handle* h);
+/* Sizes the handle's event-refinement pool so that single-pass DOP853 calls
+ * (hg_propagate_dop853 and the propagations inside hg_correct_halo) on up to
+ * max_N trajectories of dimension <= dim with up to max_hits crossings each
+ * allocate nothing.  Synchronous; the only call besides hg_create and
+ * hg_reserve_correct that allocates on purpose.
+ * Replaces: nothing (the reference allocates per call). */
+int hg_reserve(hg_handle* h, int max_N, int dim, int max_hits);
 /* Last error message recorded on this handle ("" if none). */
 const char* hg_last_error_string(hg_handle* h);
 /* Library version string. */
@@ -266,7 +285,9 @@ void hg_newton_opts_default(hg_newton_opts* o);
  * device [6][ld] initial states, overwritten by the corrected ones;
  * half_period, residual (final inf-norm), iterations, status (HG_OK,
  * HG_NEWTON_DIVERGED, HG_EVENT_NOT_FOUND, HG_LINE_SEARCH_FAILED): device [N].
- * Synchronous on `stream`; allocates its working buffers.  Host arithmetic
+ * Synchronous on `stream`.  Its device buffers belong to the handle: after
+ * hg_reserve_correct(h, M) calls with N <= M allocate nothing (otherwise the
+ * first larger call grows them once).  Host arithmetic
  * follows the reference's numpy expressions; an exactly singular Jacobian
  * (which the reference hands to lstsq) ends that orbit's line search.
  * Replaces: corrector/backends/newton.py:39-143 with
@@ -275,15 +296,24 @@ void hg_newton_opts_default(hg_newton_opts* o);
  * (orbit.correct() for halo orbits). */
 int hg_correct_halo(hg_handle* h, double mu, int N, double* x, long long ld, double* half_period, int* iterations,
                     double* residual, int* status, const hg_newton_opts* opts, void* stream);
+/* Sizes the handle's corrector buffers and event-refinement pool for
+ * hg_correct_halo on up to max_orbits orbits.  Synchronous.
+ * Replaces: nothing (the reference allocates per call). */
+int hg_reserve_correct(hg_handle* h, int max_orbits);
 
 /* Native request server (continuous batching of DOP853 propagation
  * requests).  A worker thread merges every pending request that shares a
  * problem (mu, dim, t0, tmax, options, event) into one batch, admits batches
- * while their device footprint fits hbm_budget_bytes, runs up to
- * max_concurrent batches at once on its own streams and handles (wide 6-dim
- * batches as host-scheduled segments) and keeps each request's results on
- * the host until fetched.  Results equal a direct hg_propagate_dop853 call
- * on the request alone.  Requests: y0 host row-major (N, dim); results host
+ * while their blocks fit the server's arenas, runs up to max_concurrent
+ * batches at once on its own streams and handles (wide 6-dim batches as
+ * host-scheduled segments) and keeps each request's results on the host
+ * until fetched.  hg_serve_create allocates a device arena of
+ * hbm_budget_bytes (each batch's inputs, outputs and workspace) and a pinned
+ * host arena of staging_bytes (each batch's inputs and outputs, so its copies
+ * are asynchronous); nothing is allocated afterwards, and a request too large
+ * for either arena alone fails (state 3, HG_ERR_ARGS).  Results equal a
+ * direct hg_propagate_dop853 call on the request alone.  Requests: y0 host
+ * row-major (N, dim); results host
  * row-major: y_end (N, dim), t_end (N), hit_t (N, max_hits), hit_y (N,
  * max_hits, dim), n_hits / n_accept / n_reject / status (N); null outputs
  * are skipped.  Poll states: 0 pending, 1 running, 2 done, 3 failed.
@@ -293,8 +323,9 @@ int hg_correct_halo(hg_handle* h, double mu, int N, double* x, long long ld, dou
 typedef struct hg_server hg_server;
 typedef struct hg_serve_config {
   int device;
-  long long hbm_budget_bytes;
-  int max_concurrent;
+  long long hbm_budget_bytes; /* device arena (default 8 GiB) */
+  int max_concurrent;         /* batches in flight (default 4) */
+  long long staging_bytes;    /* pinned host arena (default 1 GiB) */
 } hg_serve_config;
 void hg_serve_config_default(hg_serve_config* c);
 int hg_serve_create(const hg_serve_config* cfg, hg_server** out);
@@ -317,14 +348,21 @@ int hg_serve_stats(hg_server* s, double* p50_ms, double* p99_ms, long long* requ
  * (strict <, lowest index on ties; -1 when n < 2).
  * coord_max >= every |coordinate| involved: it sizes the FP32 pre-screen,
  * whose margin provably keeps the FP64 results exact.  Each call makes an
- * FP32 copy of the scanned set in stream-ordered scratch (cudaMallocAsync /
- * cudaFreeAsync on `stream`, 8 bytes per point); HG_ERR_CUDA if it fails.
+ * FP32 copy of the scanned set (the reference set of hg_radius_best, the
+ * set of hg_nearest_neighbor): into `workspace` (device, 16-byte aligned, at
+ * least hg_points_workspace_bytes(n) bytes; HG_ERR_ARGS if smaller) when it
+ * is given, so that the call allocates nothing, else into stream-ordered
+ * scratch (cudaMallocAsync / cudaFreeAsync on `stream`; HG_ERR_CUDA if it
+ * fails).
  * Replaces: connections/backends.py:31-99 (_pair_counts, _radpair2d: counts
  * and the pairs' per-query minimum used by _ConnectionsBackend.run :444-460)
  * and :174-235 (_nearest_neighbor_2d). */
+long long hg_points_workspace_bytes(int n);
 int hg_radius_best(int nq, const double* qx, const double* qy, int nr, const double* rx, const double* ry,
-                   double eps, double coord_max, int* count, int* best_idx, double* best_d2, void* stream);
-int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_max, int* out, void* stream);
+                   double eps, double coord_max, int* count, int* best_idx, double* best_d2,
+                   void* workspace, long long workspace_bytes, void* stream);
+int hg_nearest_neighbor(int n, const double* x, const double* y, double coord_max, int* out,
+                        void* workspace, long long workspace_bytes, void* stream);
 
 /* Segment refinement of n connection pairs (handle-free, asynchronous on
  * `stream`): pair k joins the unstable-side points pu[I[k]], pu[IU[k]] and the
@@ -382,8 +420,11 @@ int hg_get_tuning(hg_handle* h, int key, int* value);
 /* Counters of a handle.  HG_COUNTER_KERNEL_LAUNCHES: kernels launched
  * through the handle since hg_create (every propagation kernel, segment,
  * refinement and set-up kernel; memsets and copies are not kernels).
+ * HG_COUNTER_ALLOCATIONS: device and pinned-host allocations made for the
+ * handle since (and including) hg_create.
  * Replaces: nothing (instrumentation only). */
 #define HG_COUNTER_KERNEL_LAUNCHES 1
+#define HG_COUNTER_ALLOCATIONS 2
 int hg_get_counter(hg_handle* h, int key, long long* value);
 
 /* Host helper: out[i] = pow(x[i], e) through the C library's pow, i < n

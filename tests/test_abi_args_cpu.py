@@ -22,22 +22,27 @@ def test_connection_search_args(L):
     x, i = _buf(), _buf(t=C.c_int)
     ok, bad = _lib.HG_OK, _lib.HG_ERR_ARGS
     # negative sizes, NaN or negative eps / coord_max
-    assert L.hg_radius_best(-1, x, x, 1, x, x, 0.1, 1.0, i, i, x, None) == bad
-    assert L.hg_radius_best(1, x, x, -1, x, x, 0.1, 1.0, i, i, x, None) == bad
-    assert L.hg_radius_best(1, x, x, 1, x, x, -0.1, 1.0, i, i, x, None) == bad
-    assert L.hg_radius_best(1, x, x, 1, x, x, float("nan"), 1.0, i, i, x, None) == bad
-    assert L.hg_radius_best(1, x, x, 1, x, x, 0.1, -1.0, i, i, x, None) == bad
+    assert L.hg_radius_best(-1, x, x, 1, x, x, 0.1, 1.0, i, i, x, None, 0, None) == bad
+    assert L.hg_radius_best(1, x, x, -1, x, x, 0.1, 1.0, i, i, x, None, 0, None) == bad
+    assert L.hg_radius_best(1, x, x, 1, x, x, -0.1, 1.0, i, i, x, None, 0, None) == bad
+    assert L.hg_radius_best(1, x, x, 1, x, x, float("nan"), 1.0, i, i, x, None, 0, None) == bad
+    assert L.hg_radius_best(1, x, x, 1, x, x, 0.1, -1.0, i, i, x, None, 0, None) == bad
     # missing query or output buffers; reference buffers only when nr > 0
-    assert L.hg_radius_best(1, None, x, 1, x, x, 0.1, 1.0, i, i, x, None) == bad
-    assert L.hg_radius_best(1, x, x, 1, x, x, 0.1, 1.0, None, i, x, None) == bad
-    assert L.hg_radius_best(1, x, x, 1, None, x, 0.1, 1.0, i, i, x, None) == bad
+    assert L.hg_radius_best(1, None, x, 1, x, x, 0.1, 1.0, i, i, x, None, 0, None) == bad
+    assert L.hg_radius_best(1, x, x, 1, x, x, 0.1, 1.0, None, i, x, None, 0, None) == bad
+    assert L.hg_radius_best(1, x, x, 1, None, x, 0.1, 1.0, i, i, x, None, 0, None) == bad
     # an empty query set is done before anything touches the device
-    assert L.hg_radius_best(0, None, None, 5, None, None, 0.1, 1.0, None, None, None, None) == ok
-    assert L.hg_nearest_neighbor(-1, x, x, 1.0, i, None) == bad
-    assert L.hg_nearest_neighbor(3, x, x, -1.0, i, None) == bad
-    assert L.hg_nearest_neighbor(3, None, x, 1.0, i, None) == bad
-    assert L.hg_nearest_neighbor(3, x, x, 1.0, None, None) == bad
-    assert L.hg_nearest_neighbor(0, None, None, 1.0, None, None) == ok
+    assert L.hg_radius_best(0, None, None, 5, None, None, 0.1, 1.0, None, None, None, None, 0, None) == ok
+    assert L.hg_nearest_neighbor(-1, x, x, 1.0, i, None, 0, None) == bad
+    assert L.hg_nearest_neighbor(3, x, x, -1.0, i, None, 0, None) == bad
+    assert L.hg_nearest_neighbor(3, None, x, 1.0, i, None, 0, None) == bad
+    assert L.hg_nearest_neighbor(3, x, x, 1.0, None, None, 0, None) == bad
+    assert L.hg_nearest_neighbor(0, None, None, 1.0, None, None, 0, None) == ok
+    # a caller workspace smaller than hg_points_workspace_bytes(n) is refused up front
+    w = _buf(64, C.c_double)
+    assert L.hg_points_workspace_bytes(3) == 256 and L.hg_points_workspace_bytes(-1) == -1
+    assert L.hg_nearest_neighbor(3, x, x, 1.0, i, w, 255, None) == bad
+    assert L.hg_radius_best(1, x, x, 40, x, x, 0.1, 1.0, i, i, x, w, 256, None) == bad
     b = _buf(t=C.c_ubyte)
     assert L.hg_connection_refine(-1, i, i, i, i, b, 1, x, x, 1, x, x, x, x, x, None) == bad
     assert L.hg_connection_refine(1, i, i, i, i, b, -1, x, x, 1, x, x, x, x, x, None) == bad
@@ -100,10 +105,10 @@ def test_native_server_host_checks(L):
     import torch
     c = _lib.hg_serve_config()
     L.hg_serve_config_default(C.byref(c))
-    assert (c.device, c.hbm_budget_bytes, c.max_concurrent) == (0, 8 << 30, 4)
+    assert (c.device, c.hbm_budget_bytes, c.max_concurrent, c.staging_bytes) == (0, 8 << 30, 4, 1 << 30)
     out = C.c_void_p(123)
     assert L.hg_serve_create(C.byref(c), None) == _lib.HG_ERR_ARGS
-    for field, bad in (("max_concurrent", 0), ("max_concurrent", 65), ("hbm_budget_bytes", 0)):
+    for field, bad in (("max_concurrent", 0), ("max_concurrent", 65), ("hbm_budget_bytes", 0), ("staging_bytes", 0)):
         d = _lib.hg_serve_config()
         L.hg_serve_config_default(C.byref(d))
         setattr(d, field, bad)

@@ -69,3 +69,27 @@ def test_native_server_cancels_queued_request(gpu):
         assert not srv.cancel(big)
     finally:
         srv.close()
+
+
+def test_native_server_arena_limits(gpu):
+    """A request larger than the device arena fails on its own (state 3)
+    while the others run; requests that together exceed the arena wait for
+    blocks to free and still give the bits of direct calls."""
+    from hiten_gb300.serving import NativeServer
+    ev = gpu.EventSpec(index=1, offset=0.0, direction=-1, max_hits=8)
+    srv = NativeServer(hbm_budget_bytes=24 << 20, max_concurrent=2, staging_bytes=8 << 20)
+    try:
+        huge = srv.submit(W.section_states(40000, seed=11), MU, 0.0, 5.0, rtol=1e-11, atol=1e-11, event=ev)
+        small = [srv.submit(W.section_states(3000, seed=12 + k), MU, 0.0, 5.0, rtol=1e-11, atol=1e-11, event=ev)
+                 for k in range(4)]
+        for rid in small:
+            srv.wait(rid)
+        assert srv.poll(huge) == 3
+        got = [srv.fetch(rid) for rid in small]
+    finally:
+        srv.close()
+    for k, g in enumerate(got):
+        d = _direct(gpu, W.section_states(3000, seed=12 + k), 0.0, 5.0,
+                    dict(rtol=1e-11, atol=1e-11, event=ev, scheduled=False))
+        for f in ("y_end", "t_end", "n_accept", "status", "n_hits"):
+            assert np.array_equal(g[f], d[f]), f
