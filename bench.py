@@ -440,6 +440,21 @@ def sec_correct(steps, dev, peak, cpu=True):
     corrector.correct_halo_native(g[:64], mu)
     torch.cuda.synchronize()
     reps = max(2, steps // 4)
+    # the device-resident form: every orbit's Newton iterations and line
+    # searches inside one CUDA graph (built on the first call, then replayed)
+    from hiten_gb300 import _lib
+    L = _lib.load()
+    ws = torch.empty(int(L.hg_correct_halo_graph_workspace_bytes(len(g))) + 256, dtype=torch.uint8, device=dev)
+    gr = corrector.correct_halo_graph(g, mu, workspace=ws)
+    torch.cuda.synchronize()
+    tg = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gr = corrector.correct_halo_graph(g, mu, workspace=ws)
+        torch.cuda.synchronize()
+        tg.append(time.perf_counter() - t0)
+    sg = statistics.median(tg)
     tn = []
     for _ in range(reps):
         torch.cuda.synchronize()
@@ -456,8 +471,9 @@ def sec_correct(steps, dev, peak, cpu=True):
     torch.cuda.synchronize()
     sp = time.perf_counter() - t0
     flops = FLOPS_PER_ATTEMPT_D6 * be.attempts[6] + FLOPS_PER_ATTEMPT_D42 * be.attempts[42]
-    ok = nat.status == 0
-    dx = corrector.newton_step_norms(nat.x0[ok], mu, device=dev)
+    ok = gr.status == 0
+    dx = corrector.newton_step_norms(gr.x0[ok], mu, device=dev)
+    both = ok & (nat.status == 0)
     n_plain = 8
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -466,12 +482,20 @@ def sec_correct(steps, dev, peak, cpu=True):
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
     out = {"workload": "halo correction, 2048 guesses (L1/L2, Az 0.01-0.4)", "metric": "orbits corrected/s",
-           "value": len(g) / sn, "unit": "orbits/s", "ms": sn * 1e3,
-           "config": {"orbits": len(g), "driver": "native C-ABI hg_correct_halo", "zenith": "seeded 50/50"},
-           "timing": "host wall clock around the synchronous call (device work and host Newton/Armijo "
-                     "bookkeeping), median",
-           "converged": int(ok.sum()), "iterations_hist": np.bincount(nat.iterations).tolist(),
-           "convergence": {"residual_inf_max": float(np.max(nat.residual_norm[ok])),
+           "value": len(g) / sg, "unit": "orbits/s", "ms": sg * 1e3,
+           "config": {"orbits": len(g), "driver": "hg_correct_halo_graph (one CUDA graph per correction)",
+                      "zenith": "seeded 50/50"},
+           "timing": "host wall clock around the call and a device synchronize (the graph replays; inputs copied "
+                     "in and results out inside), median",
+           "graph": {"host_launch_calls_per_correction": int(gr.launches),
+                     "same_status_as_host_driver": int(np.sum(gr.status == nat.status)),
+                     "max_state_diff_vs_host_driver": float(np.max(np.abs(gr.x0[both] - nat.x0[both]))),
+                     "max_period_diff_vs_host_driver": float(np.max(np.abs(gr.period[both] - nat.period[both]))),
+                     "iterations_diff_max": int(np.max(np.abs(gr.iterations - nat.iterations)))},
+           "native_host_driver": {"ms": sn * 1e3, "orbits_per_s": len(g) / sn,
+                                  "converged": int((nat.status == 0).sum())},
+           "converged": int(ok.sum()), "iterations_hist": np.bincount(gr.iterations).tolist(),
+           "convergence": {"residual_inf_max": float(np.max(gr.residual_norm[ok])),
                            "dx_inf_max": float(np.nanmax(dx)), "dx_inf_median": float(np.nanmedian(dx)),
                            "dx_below_1e-12": int(np.sum(dx < 1e-12)),
                            "criterion": "stop when ||r||_inf < 1e-12 (the reference's test); ||dx||_inf is the "

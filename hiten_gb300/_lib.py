@@ -34,7 +34,8 @@ EXPORTED = ("hg_create", "hg_destroy", "hg_last_error_string", "hg_version", "hg
             "hg_newton_opts_default", "hg_correct_halo", "hg_serve_config_default", "hg_serve_create",
             "hg_serve_destroy", "hg_serve_submit", "hg_serve_poll", "hg_serve_wait", "hg_serve_fetch",
             "hg_serve_cancel", "hg_serve_stats", "hg_selftest_bounded_wait", "hg_host_pow", "hg_reserve",
-            "hg_reserve_correct", "hg_points_workspace_bytes")
+            "hg_reserve_correct", "hg_points_workspace_bytes", "hg_correct_halo_graph_workspace_bytes",
+            "hg_correct_halo_graph")
 HG_COUNTER_KERNEL_LAUNCHES = 1
 HG_COUNTER_ALLOCATIONS = 2
 HG_RUNNING = -1
@@ -173,6 +174,11 @@ def load(build_if_missing=True):
         L.hg_reserve.restype = C.c_int
         L.hg_reserve_correct.argtypes = [_P, C.c_int]
         L.hg_reserve_correct.restype = C.c_int
+        L.hg_correct_halo_graph_workspace_bytes.argtypes = [C.c_int]
+        L.hg_correct_halo_graph_workspace_bytes.restype = C.c_longlong
+        L.hg_correct_halo_graph.argtypes = [_P, C.c_double, C.c_int, _P, C.c_longlong, _P, _P, _P, _P,
+                                            C.POINTER(hg_newton_opts), _P, C.c_longlong, _P]
+        L.hg_correct_halo_graph.restype = C.c_int
         L.hg_selftest_bounded_wait.argtypes = [_P, C.c_int, _P, _P]
         L.hg_selftest_bounded_wait.restype = C.c_int
         L.hg_host_pow.argtypes = [C.c_longlong, _P, C.c_double, _P]

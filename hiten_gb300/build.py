@@ -19,9 +19,9 @@ LIB = os.path.join(HERE, "libhitengpu.so")
 BUILD_DIR = os.path.join(HERE, "_build")
 SOURCES = [os.path.join(CSRC, "hg_api.cu"), os.path.join(CSRC, "hg_noalloc.cu"), os.path.join(CSRC, "hg_section.cu"),
            os.path.join(CSRC, "hg_connect.cu"), os.path.join(CSRC, "hg_correct.cu"),
-           os.path.join(CSRC, "hg_serve.cu")]
+           os.path.join(CSRC, "hg_correct_graph.cu"), os.path.join(CSRC, "hg_serve.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("hg_kernels.cuh", "hg_pair.cuh", "hg_crmath.cuh", "hg_crmath_tables.h",
-                                                  "hg_tableaux.h")] + [os.path.join(REPO, "include", "hitengpu.h")]
+                                                  "hg_tableaux.h", "hg_internal.h")] + [os.path.join(REPO, "include", "hitengpu.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

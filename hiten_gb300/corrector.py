@@ -315,6 +315,49 @@ def newton_step_norms(x0, mu, options=None, backend=None, device=None):
     return out
 
 
+def correct_halo_graph(guesses, mu, options=None, device=None, workspace=None):
+    """correct_halo run on the device as one CUDA graph
+    (``hg_correct_halo_graph``): every orbit's Newton iterations and Armijo
+    line searches as nested conditional loops, no host round trip inside the
+    correction.  ``workspace``: an optional uint8 device tensor of at least
+    hg_correct_halo_graph_workspace_bytes(N) bytes (reused across calls so
+    the cached graph stays valid; one is allocated when omitted).  Returns a
+    HaloCorrectionResult."""
+    import ctypes as C
+
+    import torch
+
+    from . import _lib
+    o = options or HaloCorrectionOptions()
+    dev = P._device(device)
+    g = np.atleast_2d(np.asarray(guesses, dtype=np.float64))
+    N = g.shape[0]
+    L = _lib.load()
+    need = int(L.hg_correct_halo_graph_workspace_bytes(max(N, 1)))
+    if workspace is None or workspace.numel() < need + 256:
+        workspace = torch.empty(need + 256, dtype=torch.uint8, device=dev)
+    off = (-workspace.data_ptr()) % 256
+    x = torch.as_tensor(g, device=dev).t().contiguous()
+    half = torch.empty(max(N, 1), dtype=torch.float64, device=dev)
+    resid = torch.empty(max(N, 1), dtype=torch.float64, device=dev)
+    iters = torch.empty(max(N, 1), dtype=torch.int32, device=dev)
+    status = torch.empty(max(N, 1), dtype=torch.int32, device=dev)
+    no = _lib.hg_newton_opts(o.tol, o.max_attempts, np.inf if o.max_delta is None else o.max_delta,
+                             o.alpha_reduction, o.min_alpha, o.armijo_c, o.cond_threshold, o.event_rtol,
+                             o.event_atol, o.stm_rtol, o.stm_atol, o.steps)
+    H = _lib.handle(dev.index or 0)
+    with torch.cuda.device(dev):
+        H.check(L.hg_correct_halo_graph(H.ptr, float(mu), N, P._ptr(x), max(N, 1), P._ptr(half), P._ptr(iters),
+                                        P._ptr(resid), P._ptr(status), C.byref(no),
+                                        C.c_void_p(workspace.data_ptr() + off), workspace.numel() - off,
+                                        C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
+    st = status[:N].cpu().numpy().astype(np.int32)
+    hp = half[:N].cpu().numpy()
+    return HaloCorrectionResult(x0=x[:, :N].t().cpu().numpy(), half_period=hp, period=2.0 * hp,
+                                iterations=iters[:N].cpu().numpy().astype(np.int64),
+                                residual_norm=resid[:N].cpu().numpy(), status=st, launches=3)
+
+
 def correct_halo_native(guesses, mu, options=None, device=None):
     """correct_halo through the library's native driver (``hg_correct_halo``):
     the same batched Newton/Armijo loop on the host side of the C ABI, for

@@ -33,6 +33,8 @@ struct hg_handle {
   long long scratch_bytes = 0;
   char* corr = nullptr;       // grow-only: device buffers of hg_correct_halo
   long long corr_bytes = 0;
+  void* corr_graph = nullptr;            // the device corrector's instantiated graph and its key
+  void (*corr_graph_free)(void*) = nullptr;
   long long launches = 0;   // kernels launched through this handle
   long long allocs = 0;     // device and pinned-host allocations made for this handle
   char err[512] = {0};
@@ -165,6 +167,15 @@ int launch_fixed_pair(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
   return check_launch(h, "fixed_rk_pair_kernel");
 }
 
+// Three-warp fixed-step launch: one block of 96 threads per five trajectories.
+template <int ORDER>
+int launch_fixed_trio(hg_handle* h, const hg::FixedParams& p, cudaStream_t s) {
+  const int grid = (p.N + hg::kPairTraj - 1) / hg::kPairTraj;
+  if (grid < 1) return HG_OK;
+  hg::fixed_rk_trio_kernel<ORDER><<<grid, 96, 0, s>>>(p);
+  return check_launch(h, "fixed_rk_trio_kernel");
+}
+
 int fixed_common(hg_handle* h, double mu, int order, int dim, int N, const double* y0, long long ld_in,
                  const double* t_vals, int n_nodes, int out_every, double* y_out, long long ld_out, int fwd,
                  int flip_lo, int flip_hi, int* status, hg::FixedParams& p) {
@@ -198,6 +209,11 @@ int fixed_dispatch(hg_handle* h, int order, int dim, const hg::FixedParams& p, c
     return launch_fixed<8, 1>(h, p, s);
   }
   const int g42 = p.ev_index < 0 ? lanes_d42(h, p.N, true, kPairLatFixed) : 7;
+  if (g42 == 18) {
+    if (order == 4) return launch_fixed_trio<4>(h, p, s);
+    if (order == 6) return launch_fixed_trio<6>(h, p, s);
+    return launch_fixed_trio<8>(h, p, s);
+  }
   if (g42 == 12) {
     if (order == 4) return launch_fixed_pair<4>(h, p, s);
     if (order == 6) return launch_fixed_pair<6>(h, p, s);
@@ -536,6 +552,7 @@ int hg_destroy(hg_handle* h) {
   if (h->host_count) cudaFreeHost(h->host_count);
   if (h->scratch) cudaFree(h->scratch);
   if (h->corr) cudaFree(h->corr);
+  if (h->corr_graph && h->corr_graph_free) h->corr_graph_free(h->corr_graph);
   delete h;
   return HG_OK;
 }
@@ -911,5 +928,21 @@ int correct_buffers(hg_handle* h, long long bytes, void** out) {
 int reserve_refine(hg_handle* h, int N, int dim, int max_hits) { return hg_reserve(h, N, dim, max_hits); }
 
 int fail_msg(hg_handle* h, int code, const char* msg) { return fail(h, code, "%s", msg); }
+
+void** graph_slot(hg_handle* h, void (*free_fn)(void*)) {
+  h->corr_graph_free = free_fn;
+  return &h->corr_graph;
+}
+
+void count_launches(hg_handle* h, long long n) { h->launches += n; }
+
+int device_of(const hg_handle* h) { return h->device; }
+
+int tuning(const hg_handle* h, int key) {
+  if (key == HG_TUNE_DOP853_LANES_D6) return h->lanes_d6;
+  if (key == HG_TUNE_LANES_D42) return h->lanes_d42;
+  if (key == HG_TUNE_BLOCK_THREADS) return h->block;
+  return 0;
+}
 
 }  // namespace hg_internal

@@ -382,6 +382,72 @@ __global__ void __launch_bounds__(128) fixed_rk_pair_kernel(FixedParams p) {
   }
 }
 
+// Three-warp fixed-step RK (42-dim, no event): blocks of 96 threads, warp 0
+// the state warp of five trajectories, warps 1 and 2 their STM as half
+// columns (PairStmHalf), as dop853_trio_kernel lays them out.  The STM
+// warp's stage work is halved and a batch of N trajectories issues 3N / 5
+// warps instead of 2N / 5, so a batch of about a thousand fills every SM
+// sub-partition's FP64 pipe.  The Hessian ring's "empty" barriers take both
+// STM warps' arrivals.
+template <int ORDER>
+__global__ void __launch_bounds__(96) fixed_rk_trio_kernel(FixedParams p) {
+  __shared__ PairLink link;
+  __shared__ int fin_half[kPairTraj][2];
+  const int w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x < (int)kPairSlots) {
+    mbar_init(&link.full[threadIdx.x], 32);
+    mbar_init(&link.empty[threadIdx.x], 64);
+    if (threadIdx.x == 0) link.broken = 0;
+  }
+  if (threadIdx.x < 2 * kPairTraj) fin_half[threadIdx.x >> 1][threadIdx.x & 1] = 1;
+  __syncthreads();
+  const PairLane pl(lane);
+  const int group = blockIdx.x;
+  const bool active = group * kPairTraj < p.N;  // uniform over the block
+  const int hg = 5 * (w - 1) + pl.t;            // STM warps: half-group 0..9
+  const int tg = w == 0 ? pl.t : hg / 2;
+  const int traj = group * kPairTraj + tg;
+  const bool valid = active && traj < p.N;
+  const int tc = valid ? traj : (active ? p.N - 1 : 0);
+  bool finite = true, broken = false;
+  if (active) {
+    if (w == 0) {
+      PairState L;
+      L.role = pl.role;
+      L.base = pl.base;
+      L.t = pl.t;
+      L.gmask = pl.gmask;
+      L.link = &link;
+      L.seq = 0;
+      L.broken = false;
+      finite = pair_fixed_run<ORDER>(L, p, tc, valid && pl.role < 6);
+      broken = L.broken;
+      finite = __all_sync(pl.gmask, finite);
+    } else {
+      PairStmHalf L;
+      L.t = tg;
+      L.half = hg & 1;
+      L.role = pl.role;
+      L.base = pl.base;
+      L.gmask = pl.gmask;
+      L.link = &link;
+      L.seq = 0;
+      L.broken = false;
+      finite = pair_fixed_run<ORDER>(L, p, tc, valid && pl.role < 6);
+      broken = L.broken;
+      finite = __all_sync(pl.gmask, finite);
+      if (pl.role == 0) fin_half[tg][hg & 1] = finite ? 1 : 0;
+      if (broken && lane == 0) link.broken = 1;
+    }
+  }
+  __syncthreads();
+  if (w == 0 && valid && pl.role == 0 && p.status) {
+    const bool all_fin = finite && fin_half[pl.t][0] != 0 && fin_half[pl.t][1] != 0;
+    p.status[traj] = (broken || link.broken) ? HG_SYNC_TIMEOUT : (all_fin ? HG_OK : HG_NONFINITE);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // DOP853 on the paired warps (42-dim, single pass, no event; rk.py:2375-2549)
 // ---------------------------------------------------------------------------

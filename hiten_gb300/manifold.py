@@ -2,15 +2,19 @@
 
 Follows algorithms/types/services/manifold.py: the STM grid of the periodic
 orbit (_compute_stm with steps=2000 and the manifold's direction, :215-245),
-the monodromy eigenvector (host numpy eig), seeds
-x0W = x(t_k) + (d / |(dir * Phi(t_k) v)[0:3]|) * dir * Phi(t_k) v at the grid
-time nearest to fraction * T (:470-573), then DOP853 propagation of all
+the NN-th real stable or unstable eigenvector of the monodromy as the
+manifold service chooses it (eigen-decomposition of the discrete system
+with delta = 1e-6, pivot-normalised complex eigenvectors, :347-367 and
+algorithms/linalg/backend.py:196-260), seeds
+x0W = x(t_k) + (d / |(dir * Phi(t_k) v)[0:3]|) * Re(dir * Phi(t_k) v) at the
+grid time nearest to fraction * T (:470-573), then DOP853 propagation of all
 seeds at once with the flip of components 0:6 for backward time (:396-409).
 """
 import numpy as np
 import torch
 
 from . import propagate as P
+from . import stability
 from .workloads import identity_stm_state
 
 
@@ -24,36 +28,42 @@ def stm_grid(x0, period, mu, steps=2000, forward=1, rtol=1e-12, atol=1e-12, devi
     return times, PHI
 
 
-def stable_eigvec(phi_T, stable=True):
-    """Real eigenvector of the monodromy for the smallest (stable) or largest
-    (unstable) real eigenvalue."""
-    w, V = np.linalg.eig(phi_T)
-    real = np.abs(w.imag) < 1e-10
-    idx = np.nonzero(real)[0]
-    mags = np.abs(w.real[idx])
-    k = idx[np.argmin(mags)] if stable else idx[np.argmax(mags)]
-    v = V[:, k].real
-    return v / np.linalg.norm(v)
+def stable_eigvec(phi_T, stable=True, NN=1, delta=1e-6):
+    """The NN-th real stable (or unstable) eigenvector of the monodromy, as
+    the manifold service picks it: complex128, pivot-normalised (first entry
+    of modulus >= 1e-14 equal to 1, real vectors with a positive pivot),
+    among the eigenvalues with |lambda| < 1 - delta (> 1 + delta) that
+    np.isreal accepts, in numpy eig's order (services/manifold.py:347-367)."""
+    sn, un, _, Ws, Wu, _ = stability.eigenvalue_decomposition(np.asarray(phi_T), delta)
+    _, vecs = stability.real_eigenvectors(Ws, sn) if stable else stability.real_eigenvectors(Wu, un)
+    col = NN - 1
+    if col < 0 or vecs.shape[1] <= col:
+        kind = "stable" if stable else "unstable"
+        raise ValueError(f"Requested {kind} eigenvector {NN} not available. "
+                         f"Only {vecs.shape[1]} real {kind} eigenvectors found.")
+    return vecs[:, col]
 
 
 def seeds(times, PHI, period, fractions, displacements, eigvec, direction=1):
-    """Seeds for every (fraction, displacement) pair (fraction-major)."""
+    """Seeds for every (fraction, displacement) pair (fraction-major), in the
+    operation order of _compute_manifold_section (services/manifold.py:470-537)."""
     tt = np.abs(times)
     xx = PHI[:, 36:42]
     out = np.empty((len(fractions) * len(displacements), 6))
     n = 0
     for f in fractions:
         k = int(np.argmin(np.abs(f * period - tt)))
-        phi = PHI[k, :36].reshape(6, 6)
+        phi = PHI[k, :36].reshape((6, 6))
         man = direction * (phi @ eigvec)
         mag = np.linalg.norm(man[0:3])
         if mag < 1e-14:
             mag = 1.0
-        for d in displacements:
-            x = xx[k] + (d / mag) * man
-            if abs(x[2]) < 1e-15:
+        for disp in displacements:
+            d = disp / mag
+            x = (xx[k, :].copy() + d * man.real).flatten()
+            if abs(x[2]) < 1.0e-15:
                 x[2] = 0.0
-            if abs(x[5]) < 1e-15:
+            if abs(x[5]) < 1.0e-15:
                 x[5] = 0.0
             out[n] = x
             n += 1
@@ -99,7 +109,7 @@ def compute(x0, period, mu, stable=True, direction=1, step=0.02, integration_fra
         raise NotImplementedError("manifold propagation on the GPU path is DOP853")
     forward = -1 if stable else 1
     times, PHI = stm_grid(x0, period, mu, steps=2000, forward=forward, device=device)
-    eigvec = stable_eigvec(PHI[-1, :36].reshape(6, 6), stable=stable)
+    eigvec = stable_eigvec(PHI[-1, :36].reshape(6, 6), stable=stable, NN=NN)
     fractions = np.arange(0.0, 1.0, step)
     disps = np.atleast_1d(displacement if displacements is None else displacements)
     seeds_arr = seeds(times, PHI, period, fractions, disps, eigvec, direction=direction)

@@ -301,6 +301,27 @@ int hg_correct_halo(hg_handle* h, double mu, int N, double* x, long long ld, dou
  * Replaces: nothing (the reference allocates per call). */
 int hg_reserve_correct(hg_handle* h, int max_orbits);
 
+/* hg_correct_halo run entirely on the device as one CUDA graph: the Newton
+ * iterations of all N orbits and their Armijo line searches are nested
+ * conditional WHILE nodes, the propagation legs run in list mode (the live
+ * count read from device memory), and the Newton algebra and line-search
+ * decisions are device kernels.  Asynchronous on `stream` (one graph launch
+ * plus a load and a store kernel; nothing is read back).  Same arguments and
+ * outputs as hg_correct_halo plus a caller workspace of at least
+ * hg_correct_halo_graph_workspace_bytes(N) bytes (256-byte aligned), which
+ * holds all iteration state; the call allocates nothing.  The graph is built
+ * on the first call and cached on the handle (rebuilt when N, mu, the
+ * options, the workspace or the lane tuning change).  Arithmetic differs from
+ * hg_correct_halo in one place: the quadratic term's powers are correctly
+ * rounded where the host driver calls the C library's pow (results agree to
+ * the last bits of the Jacobian; iteration counts can differ by one where a
+ * residual lands at the tolerance).  N <= 2^22, max_attempts <= 1000.
+ * Replaces: as hg_correct_halo (execution on the device). */
+long long hg_correct_halo_graph_workspace_bytes(int N);
+int hg_correct_halo_graph(hg_handle* h, double mu, int N, double* x, long long ld, double* half_period,
+                          int* iterations, double* residual, int* status, const hg_newton_opts* opts,
+                          void* workspace, long long workspace_bytes, void* stream);
+
 /* Native request server (continuous batching of DOP853 propagation
  * requests).  A worker thread merges every pending request that shares a
  * problem (mu, dim, t0, tmax, options, event) into one batch, admits batches
@@ -393,8 +414,8 @@ int hg_connection_refine(int n, const int* I, const int* IU, const int* J, const
  * without an event: a state warp with the Hessian and an STM warp per five
  * trajectories, ~0.6x the per-step latency of 7 for RK8; blocks of one pair,
  * or of two pairs with HG_TUNE_BLOCK_THREADS 128; other calls then use 7),
- * 18 (three warps, single-pass DOP853 without an event: the STM of five
- * trajectories on two warps of half columns; fixed RK and other calls then
+ * 18 (three warps, fixed RK and single-pass DOP853 without an event: the
+ * STM of five trajectories on two warps of half columns; other calls then
  * use 7), 0 = automatic (the default).
  * HG_TUNE_SM_CAPACITY: the layout cost models' FP64 capacity of an SM, in
  * tenths of a warp's demand (default 30: three warps run at full speed).

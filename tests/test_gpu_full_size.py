@@ -75,6 +75,30 @@ def test_manifold_16384_full(gpu, dev_oracle):
     _vs_oracle(sched, idx, ref)
 
 
+def test_unstable_manifold_16384_full(gpu, dev_oracle):
+    """The other leg of the manifold's t = +-8: the unstable manifold of the
+    same halo (forward STM grid, the largest real eigenvalue's eigenvector),
+    16384 seeds propagated forward to t = +8 with the terminal x = 1 - mu
+    crossing; single pass and scheduled plans, permutation invariance, and a
+    seeded 2048-seed sample against the oracle."""
+    from hiten_gb300 import manifold as M
+    times, PHI = M.stm_grid(W.HALO_L1_AZ02_X0, W.HALO_L1_AZ02_T, MU, steps=2000, forward=1)
+    v = M.stable_eigvec(PHI[-1, :36].reshape(6, 6), stable=False)
+    phases, disp = W.manifold_grid(512, 32, seed=0)
+    s = M.seeds(times, PHI, W.HALO_L1_AZ02_T, phases, disp, v, direction=1)
+    assert s.shape == (16384, 6)
+    sched = M.propagate_to_plane(s, MU, tf=8.0, forward=1, scheduled=True)
+    single = M.propagate_to_plane(s, MU, tf=8.0, forward=1, scheduled=False)
+    _same(sched, single)
+    perm = np.random.default_rng(6).permutation(len(s))
+    _same(sched, M.propagate_to_plane(s[perm], MU, tf=8.0, forward=1, scheduled=True), perm)
+    na = _np(sched.n_accept)
+    assert na.min() < na.max()  # uneven lengths
+    idx = np.sort(np.random.default_rng(7).choice(len(s), 2048, replace=False))
+    ref = dev_oracle.dop853_event_batch(s[idx], 0.0, 8.0, MU, 0, 1 - MU, 0, 1, max_step=1e4, fwd=1, flip=(0, 6))
+    _vs_oracle(sched, idx, ref)
+
+
 def test_section_65536_full(gpu, dev_oracle):
     """65536 section states, DOP853 1e-11 to t = 20, up to 8 crossings of y = 0 (direction -1)."""
     y0 = W.section_states(65536, seed=0)

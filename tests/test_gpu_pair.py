@@ -24,13 +24,14 @@ def _np(t):
     return t.detach().cpu().numpy()
 
 
+@pytest.mark.parametrize("lanes", [12, 18])
 @pytest.mark.parametrize("order", [4, 6, 8])
 @pytest.mark.parametrize("n", [1, 7, 10, 23])
 @pytest.mark.parametrize("fwd,flip", [(1, None), (-1, (36, 42)), (-1, (0, 42)), (-1, (30, 40))])
-def test_pair_fixed_matches_oracle(gpu, dev_oracle, order, n, fwd, flip):
+def test_pair_fixed_matches_oracle(gpu, dev_oracle, lanes, order, n, fwd, flip):
     y0 = W.stm_fixed_batch(64, seed=3)[:n]
     t = np.linspace(0.0, 0.8, 121)
-    with gpu.tuning(lanes_d42=12):
+    with gpu.tuning(lanes_d42=lanes):
         out, st = gpu.propagate_fixed(y0, t, MU, order=order, out_every=7, fwd=fwd, flip=flip, return_status=True)
     ref, rst = dev_oracle.fixed_rk_batch(order, y0, t, MU, out_every=7, fwd=fwd, flip=flip)
     assert rst == 0
@@ -45,11 +46,12 @@ def test_pair_many_blocks_equals_single_warp_layouts(gpu, dev_oracle):
     y0 = W.stm_fixed_batch(2003, seed=5)
     t = np.linspace(0.0, 0.5, 51)
     outs = {}
-    for lanes in (12, 7, 14):
+    for lanes in (12, 7, 14, 18):
         with gpu.tuning(lanes_d42=lanes):
             outs[lanes] = _np(gpu.propagate_fixed(y0, t, MU, order=8, out_every=5))
     assert np.array_equal(outs[12], outs[7])
     assert np.array_equal(outs[12], outs[14])
+    assert np.array_equal(outs[12], outs[18])
     idx = np.array([0, 4, 5, 999, 2000, 2002])
     ref, rst = dev_oracle.fixed_rk_batch(8, y0[idx], t, MU, out_every=5)
     assert rst == 0
@@ -63,16 +65,17 @@ def test_pair_nonfinite_status_per_trajectory(gpu):
     y0[6, 36:] = [-MU, 0.0, 0.0, 0.0, 0.0, 0.0]
     t = np.linspace(0.0, 0.2, 21)
     res = {}
-    for lanes in (12, 7):
+    for lanes in (12, 7, 18):
         with gpu.tuning(lanes_d42=lanes):
             out, st = gpu.propagate_fixed(y0, t, MU, order=8, out_every=4, return_status=True)
         res[lanes] = (_np(out), _np(st))
     st = res[12][1]
     assert st[6] == _lib.HG_NONFINITE
     assert np.all(np.delete(st, 6) == _lib.HG_OK)
-    assert np.array_equal(res[12][1], res[7][1])
     ok = np.delete(np.arange(12), 6)
-    assert np.array_equal(res[12][0][:, ok], res[7][0][:, ok])
+    for lanes in (7, 18):
+        assert np.array_equal(res[12][1], res[lanes][1])
+        assert np.array_equal(res[12][0][:, ok], res[lanes][0][:, ok])
 
 
 # ------------------------------------------------------------------ DOP853 (42-dim, paired warps)
