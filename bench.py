@@ -445,15 +445,20 @@ def sec_correct(steps, dev, peak, cpu=True):
     from hiten_gb300 import _lib
     L = _lib.load()
     ws = torch.empty(int(L.hg_correct_halo_graph_workspace_bytes(len(g))) + 256, dtype=torch.uint8, device=dev)
-    gr = corrector.correct_halo_graph(g, mu, workspace=ws)
-    torch.cuda.synchronize()
+    from hiten_gb300 import autotune
+    from hiten_gb300 import propagate as P
+    shape, shape_ms = autotune.tune_correct("correct_2048", lambda: corrector.correct_halo_graph(g, mu, workspace=ws),
+                                            device=dev)
     tg = []
-    for _ in range(reps):
+    with P.tuning(device=dev, lanes_d6=shape[0], lanes_d42=shape[1]):
+        gr = corrector.correct_halo_graph(g, mu, workspace=ws)  # (re)builds the graph for the chosen layout
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        gr = corrector.correct_halo_graph(g, mu, workspace=ws)
-        torch.cuda.synchronize()
-        tg.append(time.perf_counter() - t0)
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            gr = corrector.correct_halo_graph(g, mu, workspace=ws)
+            torch.cuda.synchronize()
+            tg.append(time.perf_counter() - t0)
     sg = statistics.median(tg)
     tn = []
     for _ in range(reps):
@@ -488,6 +493,7 @@ def sec_correct(steps, dev, peak, cpu=True):
            "timing": "host wall clock around the call and a device synchronize (the graph replays; inputs copied "
                      "in and results out inside), median",
            "graph": {"host_launch_calls_per_correction": int(gr.launches),
+                     "layout": {"event_lanes": shape[0], "stm_lanes": shape[1], "autotune_ms": shape_ms},
                      "same_status_as_host_driver": int(np.sum(gr.status == nat.status)),
                      "max_state_diff_vs_host_driver": float(np.max(np.abs(gr.x0[both] - nat.x0[both]))),
                      "max_period_diff_vs_host_driver": float(np.max(np.abs(gr.period[both] - nat.period[both]))),

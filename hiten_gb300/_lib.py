@@ -75,7 +75,7 @@ class hg_newton_opts(C.Structure):
 
 class hg_serve_config(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_longlong), ("max_concurrent", C.c_int),
-                ("staging_bytes", C.c_longlong)]
+                ("staging_bytes", C.c_longlong), ("pool_slots", C.c_int), ("seg_steps", C.c_int)]
 
 
 class hg_config(C.Structure):

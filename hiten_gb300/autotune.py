@@ -109,3 +109,31 @@ def tune(key, fn, shapes=DEFAULT_SHAPES, reps=2, device=None, cache_file=None):
         with open(cache_file, "w") as f:
             json.dump({k: list(v) for k, v in _cache.items()}, f)
     return best, timings
+
+
+# Lane layouts of the device-resident halo correction (hg_correct_halo_graph):
+# lanes per 6-dim event-leg trajectory and per 42-dim STM-leg trajectory.
+CORRECT_SHAPES = ((6, 14), (6, 7), (2, 14), (1, 14))
+_correct_cache = {}
+
+
+def tune_correct(key, run, shapes=CORRECT_SHAPES, reps=2, device=None):
+    """Pick the lane layouts of the device corrector's legs by measurement.
+
+    `run()` must run one correction through ``corrector.correct_halo_graph``
+    (each shape rebuilds the cached graph once, in the warm-up call).  Every
+    shape gives the same bits; returns the winning (lanes_d6, lanes_d42) --
+    not applied to the handle, since those knobs also steer other calls: run
+    the correction under ``propagate.tuning(lanes_d6=..., lanes_d42=...)`` --
+    with all timings (ms)."""
+    if key in _correct_cache:
+        return _correct_cache[key], {}
+    timings = {}
+    for g6, g42 in shapes:
+        with P.tuning(device=device, lanes_d6=g6, lanes_d42=g42):
+            run()  # warm: builds and caches the graph for this layout
+            torch.cuda.synchronize()
+            timings[(g6, g42)] = _time(run, reps)
+    best = min(timings, key=timings.get)
+    _correct_cache[key] = best
+    return best, {f"event{g6}_stm{g42}": ms for (g6, g42), ms in timings.items()}

@@ -895,7 +895,14 @@ int hg_correct_halo_graph(hg_handle* h, double mu, int N, double* x, long long l
     }
     c = new (std::nothrow) GraphCache();
     if (!c) return hg_internal::fail_msg(h, HG_ERR_CUDA, "out of host memory");
-    cudaError_t e = build_graph(w, mu, o, g6, g42, sms, spec_traj, s, &c->graph, &c->kernels);
+    // capture on a private stream: the caller's may be the legacy default
+    // stream, which cannot be captured; the graph is launched on the caller's
+    cudaStream_t cs = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+      e = build_graph(w, mu, o, g6, g42, sms, spec_traj, cs, &c->graph, &c->kernels);
+      cudaStreamDestroy(cs);
+    }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&c->exec, c->graph, 0);
     if (e != cudaSuccess) {
       free_cache(c);

@@ -1,19 +1,31 @@
-// Native request server for DOP853 propagation requests (continuous
-// batching).  Requests are host arrays; a worker thread merges every pending
-// request that shares a problem (mu, dim, span, options, event) into one
-// batch, admits batches while their device footprint fits the device arena,
-// runs them concurrently on its own streams and handles (host-scheduled
-// segments for wide 6-dim batches, one segment that finishes every
-// trajectory otherwise), and parks each request's results on the host until
-// it is fetched.  Results are those of a direct hg_propagate_dop853 call on
-// the request alone: trajectories never interact.
+// Native request server for DOP853 propagation requests: continuous batching
+// at the level of trajectory slots.
+//
+// Every problem (mu, dim, span, options, event) that has work gets a pool of
+// C trajectory slots resident on the device: the states, step sizes,
+// controller memory, counters and crossings of every live trajectory stay in
+// the pool between segments.  A pool's thread loops:
+//   1. admission: trajectories of waiting requests of its problem take free
+//      slots (a request can enter over several rounds; its inputs are copied
+//      through pinned staging and scattered into the slots by a kernel);
+//   2. one segment: every live slot advances by up to seg_steps attempted
+//      steps (the library's DOP853 kernel in list mode; its lane layout chosen
+//      from the live count, as the scheduled driver does), then the saved
+//      crossings are refined;
+//   3. collection: a kernel gathers the slots that finished into one staging
+//      block; one copy brings them back; their requests receive the rows and
+//      the slots are free for the next admission.
+// So a request arriving while others run is admitted at the next segment
+// boundary as slots free up, and its work overlaps theirs on the device.
+// Trajectories never interact and a paused trajectory resumes with every
+// bit, so each request's results equal a direct hg_propagate_dop853 call on
+// it alone.
 //
 // Memory: hg_serve_create allocates a device arena of hbm_budget_bytes and a
-// pinned host staging arena of staging_bytes; every batch takes one block of
-// each (its inputs, outputs and segment workspace on the device; its inputs
-// and outputs in pinned memory, so its copies run asynchronously on its
-// stream) and returns them when it finishes, on success or failure.  Nothing
-// is allocated after creation.
+// pinned host arena of staging_bytes; a pool takes one block of each when it
+// opens (its slot count C = pool_slots, halved until the free arenas hold it)
+// and returns them when its problem has no work left.  Nothing is allocated
+// after creation.
 #include <cuda_runtime.h>
 #include <limits.h>
 #include <string.h>
@@ -29,6 +41,7 @@
 #include <thread>
 #include <vector>
 
+#include "hg_kernels.cuh"
 #include "hitengpu.h"
 
 namespace {
@@ -41,15 +54,18 @@ struct Key {
   hg_dop853_opts o;
   int has_ev;
   hg_event ev;
-  bool operator<(const Key& b) const { return memcmp(this, &b, sizeof(Key)) < 0; }
 };
+
+bool same_key(const Key& a, const Key& b) { return memcmp(&a, &b, sizeof(Key)) == 0; }
 
 struct Request {
   long long id;
   Key key;
   int n;
   std::vector<double> y0;  // row-major (n, dim)
-  // results
+  int admitted = 0;        // trajectories given a slot so far
+  int done = 0;            // trajectories finished
+  // results (row-major)
   std::vector<double> y_end, t_end, hit_t, hit_y;
   std::vector<int> n_hits, n_acc, n_rej, status;
   int state = 0;  // 0 pending, 1 running, 2 done, 3 failed
@@ -61,12 +77,9 @@ struct Request {
 class Arena {
  public:
   void reset(long long size) {
-    size_ = size;
     free_.clear();
     if (size > 0) free_[0] = size;
   }
-  long long size() const { return size_; }
-  // offset of a block of `bytes` (256-byte aligned), or -1
   long long alloc(long long bytes) {
     bytes = up(bytes);
     for (auto it = free_.begin(); it != free_.end(); ++it) {
@@ -95,46 +108,186 @@ class Arena {
       }
     }
   }
-  static long long up(long long x) { return (x + 255) & ~255LL; }
-  long long free_bytes() const {
-    long long t = 0;
-    for (const auto& f : free_) t += f.second;
-    return t;
+  long long largest() const {
+    long long m = 0;
+    for (const auto& f : free_) m = std::max(m, f.second);
+    return m;
   }
+  static long long up(long long x) { return (x + 255) & ~255LL; }
 
  private:
-  long long size_ = 0;
   std::map<long long, long long> free_;  // offset -> length, disjoint, not adjacent
 };
 
-// Layout of a batch of n trajectories: the inputs and outputs (the same
-// layout on the device and in pinned staging) and, on the device only, the
-// segment workspace.  y0 [d][n]; outputs y_end [d][n], t_end [n],
-// hit_t [hits][n], hit_y [hits][d][n], then four int arrays [n].
-struct Layout {
-  long long off_ye, off_te, off_ht, off_hy, off_i, io_bytes, ws_bytes;
-  Layout(int d, int n, int hits) {
-    const long long nn = n;
-    off_ye = Arena::up(8 * d * nn);
-    off_te = off_ye + 8 * d * nn;
-    off_ht = off_te + 8 * nn;
-    off_hy = off_ht + 8 * hits * nn;
-    off_i = off_hy + 8 * (long long)hits * d * nn;
-    io_bytes = Arena::up(off_i + 16 * nn);
-    ws_bytes = Arena::up(hg_dop853_segmented_workspace_bytes(n, d, hits));
-  }
-  long long device_bytes() const { return io_bytes + ws_bytes; }
-  long long out_bytes() const { return io_bytes - off_ye; }
+// Doubles and ints of one finished trajectory's result row.
+struct RowShape {
+  int dim, hits;
+  int nd() const { return dim + 1 + hits + hits * dim; }  // y_end, t_end, hit_t, hit_y
+  static constexpr int ni = 4;                            // n_accept, n_reject, n_hits, status
 };
 
-struct Batch {
+// A pool's device and staging layout for C slots.
+struct PoolLayout {
+  long long dev_bytes = 0, stg_bytes = 0;
+  // device offsets
+  long long y0, y_end, t_end, hit_t, hit_y, wh, wep, wpp, wq, na, nr, nh, st, list0, list1, cnt, fin, out_d, out_i,
+      stage_y0, stage_slots, refine;
+  // staging offsets (pinned)
+  long long s_y0, s_slots, s_cnt, s_fin, s_out_d, s_out_i;
+  PoolLayout(int C, int dim, int hits) {
+    const RowShape rs{dim, hits};
+    const long long c = C;
+    auto D = [&](long long& o, long long bytes) {
+      o = dev_bytes;
+      dev_bytes += Arena::up(bytes);
+    };
+    D(y0, 8 * dim * c);
+    D(y_end, 8 * dim * c);
+    D(t_end, 8 * c);
+    D(hit_t, 8 * hits * c + 8);
+    D(hit_y, 8 * hits * dim * c + 8);
+    D(wh, 8 * c);
+    D(wep, 8 * c);
+    D(wpp, 8 * c);
+    D(wq, 4 * c);
+    D(na, 4 * c);
+    D(nr, 4 * c);
+    D(nh, 4 * c);
+    D(st, 4 * c);
+    D(list0, 4 * c);
+    D(list1, 4 * c);
+    D(cnt, 64);
+    D(fin, 4 * c);
+    D(out_d, 8LL * rs.nd() * c);
+    D(out_i, 4LL * RowShape::ni * c);
+    D(stage_y0, 8 * dim * c);
+    D(stage_slots, 4 * c);
+    const long long recs = c * std::max(hits, 1);
+    D(refine, hits > 0 ? 256 + 2 * Arena::up(recs * 4) + Arena::up((15LL * dim + 3) * recs * 8) : 256);
+    auto S = [&](long long& o, long long bytes) {
+      o = stg_bytes;
+      stg_bytes += Arena::up(bytes);
+    };
+    S(s_y0, 8 * dim * c);
+    S(s_slots, 4 * c);
+    S(s_cnt, 64);
+    S(s_fin, 4 * c);
+    S(s_out_d, 8LL * rs.nd() * c);
+    S(s_out_i, 4LL * RowShape::ni * c);
+  }
+};
+
+// New trajectories into their slots: inputs, "not started" status, the tail
+// of the live list; the live count becomes live + n.
+__global__ void admit_kernel(int n, int C, int dim, const double* stage, const int* slots, double* y0, int* status,
+                             int* list, int* count, int live) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int s = slots[j];
+    for (int c = 0; c < dim; ++c) y0[(long long)c * C + s] = stage[(long long)c * n + j];
+    status[s] = -2;
+    list[live + j] = s;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = live + n;
+}
+
+// Slots of the last segment's list that finished: their result rows,
+// gathered (fin[k] = slot of row k; *n_fin rows).
+__global__ void collect_kernel(int C, int dim, int hits, const int* list, const int* n_in, const double* y_end,
+                               const double* t_end, const double* hit_t, const double* hit_y, const int* na,
+                               const int* nr, const int* nh, const int* st, int* fin, int* n_fin, double* out_d,
+                               int* out_i) {
+  const int n = *n_in;
+  const int nd = dim + 1 + hits + hits * dim;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int s = list[j];
+    if (st[s] == HG_RUNNING) continue;
+    const int k = atomicAdd(n_fin, 1);
+    fin[k] = s;
+    double* r = out_d + (long long)k * nd;
+    for (int c = 0; c < dim; ++c) r[c] = y_end[(long long)c * C + s];
+    r[dim] = t_end[s];
+    const int h = hits ? nh[s] : 0;
+    for (int q = 0; q < hits; ++q) {
+      r[dim + 1 + q] = q < h ? hit_t[(long long)q * C + s] : 0.0;
+      for (int c = 0; c < dim; ++c)
+        r[dim + 1 + hits + q * dim + c] = q < h ? hit_y[((long long)q * dim + c) * C + s] : 0.0;
+    }
+    int* ri = out_i + (long long)k * RowShape::ni;
+    ri[0] = na[s];
+    ri[1] = nr[s];
+    ri[2] = h;
+    ri[3] = st[s];
+  }
+}
+
+template <class K>
+int resident_blocks(K kern, int block, int sms) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return per_sm * sms;
+}
+
+// One segment over the live list (its first `live` entries) in layout G.
+template <int G>
+cudaError_t segment(hg::DopParams p, int live, int sms, cudaStream_t s) {
+  const int tpb = hg::Layout<G>::TPW;
+  const int need = (live + tpb - 1) / tpb;
+  const int cap = resident_blocks(hg::dop853_kernel<G, false>, 32, sms);
+  const int grid = need < cap ? need : cap;
+  if (grid < 1) return cudaSuccess;
+  p.stride = grid * tpb;
+  hg::dop853_kernel<G, false><<<grid, 32, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+// The crossings the segment saved (records [0, *refine_count)).
+template <int G>
+cudaError_t refine(hg::DopParams p, int sms, cudaStream_t s) {
+  const int tpb = hg::Layout<G>::TPW;
+  const long long need = (p.rec_ld + tpb - 1) / tpb;
+  const int cap = resident_blocks(hg::refine_kernel<G>, 32, sms);
+  const int grid = need < cap ? (int)need : cap;
+  if (grid < 1) return cudaSuccess;
+  p.stride = grid * tpb;
+  hg::refine_kernel<G><<<grid, 32, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+// Lanes per trajectory for a segment of n live trajectories: the least
+// lat(G) x max(1, warps / capacity), the host-scheduled driver's rule.
+int lanes_for(int dim, int n, int sms) {
+  const double cap = 3.0 * sms;
+  if (dim == 6) {
+    const int gs[3] = {1, 2, 6}, tpw[3] = {32, 16, 5};
+    const double lat[3] = {1.0, 0.622, 0.400};
+    int best = 0;
+    double bc = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      const double warps = (double)((n + tpw[i] - 1) / tpw[i]);
+      const double c = lat[i] * std::max(1.0, warps / cap);
+      if (i == 0 || c < bc) {
+        best = i;
+        bc = c;
+      }
+    }
+    return gs[best];
+  }
+  const double w7 = (double)((n + 3) / 4), w14 = (double)((n + 1) / 2);
+  const double c7 = std::max(1.0, w7 / cap), c14 = 0.65 * std::max(1.0, w14 / cap);
+  return c14 < c7 ? 14 : 7;
+}
+
+struct Pool {
   Key key;
-  std::vector<std::shared_ptr<Request>> reqs;
-  int n = 0;
-  int slot = -1;
-  long long dev_off = -1, dev_len = 0, stg_off = -1, stg_len = 0;  // arena blocks
-  std::atomic<int> finished{0};
+  int dim = 6, hits = 0, C = 0, slot = -1;
+  long long dev_off = -1, dev_len = 0, stg_off = -1, stg_len = 0;
+  std::vector<int> free_slots;
+  std::vector<std::pair<std::shared_ptr<Request>, int>> owner;  // per slot: request, trajectory index
   std::thread runner;
+  std::atomic<int> finished{0};
   int rc = HG_OK;
 };
 
@@ -144,253 +297,329 @@ struct hg_server {
   hg_serve_config cfg;
   std::mutex mu;
   std::condition_variable cv;
-  std::deque<std::shared_ptr<Request>> pending;
+  std::deque<std::shared_ptr<Request>> pending;  // requests with trajectories not yet admitted
   std::map<long long, std::shared_ptr<Request>> all;
-  std::vector<std::unique_ptr<Batch>> running;
+  std::vector<std::unique_ptr<Pool>> pools;
   std::vector<cudaStream_t> streams;
-  std::vector<hg_handle*> handles;
   std::vector<char> slot_busy;
   long long next_id = 1;
-  char* dev_base = nullptr;  // device arena (hbm_budget_bytes)
-  char* stg_base = nullptr;  // pinned staging arena (staging_bytes)
+  char* dev_base = nullptr;
+  char* stg_base = nullptr;
   Arena dev_arena, stg_arena;
   bool stop = false;
   std::thread worker;
   std::vector<double> latencies_ms;
-  long long batches = 0;
+  long long segments = 0;
+  int sms = 1;
 
-  // Copies in, propagation and copies out of one admitted batch on its
-  // slot's stream (runs on the batch's own thread; the blocks are owned by
-  // the batch and returned in finish()).
-  int launch(Batch& b) {
-    const Key& k = b.key;
-    const int d = k.dim, n = b.n;
-    const int hits = k.has_ev ? k.ev.max_hits : 0;
-    const Layout L(d, n, hits);
-    cudaStream_t s = streams[b.slot];
-    if (cudaSetDevice(cfg.device) != cudaSuccess) return HG_ERR_CUDA;
-    char* dev = dev_base + b.dev_off;
-    char* stg = stg_base + b.stg_off;
-    double* h_y0 = (double*)stg;
-    int o = 0;
-    for (auto& r : b.reqs) {
-      for (int i = 0; i < r->n; ++i)
-        for (int c = 0; c < d; ++c) h_y0[(size_t)c * n + o + i] = r->y0[(size_t)i * d + c];
-      o += r->n;
+  // Admission for one pool (lock held): trajectories of waiting requests of
+  // its problem, in arrival order, take free slots.
+  void take_admissions(Pool& P, std::vector<int>& slots, std::vector<std::pair<std::shared_ptr<Request>, int>>& who) {
+    for (auto it = pending.begin(); it != pending.end() && !P.free_slots.empty();) {
+      auto r = *it;
+      if (!same_key(r->key, P.key)) {
+        ++it;
+        continue;
+      }
+      while (r->admitted < r->n && !P.free_slots.empty()) {
+        const int s = P.free_slots.back();
+        P.free_slots.pop_back();
+        slots.push_back(s);
+        who.emplace_back(r, r->admitted);
+        P.owner[s] = {r, r->admitted};
+        ++r->admitted;
+      }
+      r->state = 1;
+      if (r->admitted == r->n)
+        it = pending.erase(it);
+      else
+        ++it;
     }
-    if (cudaMemcpyAsync(dev, stg, 8ull * d * n, cudaMemcpyHostToDevice, s) != cudaSuccess) return HG_ERR_CUDA;
-    double* ye = (double*)(dev + L.off_ye);
-    double* te = (double*)(dev + L.off_te);
-    double* ht = hits ? (double*)(dev + L.off_ht) : nullptr;
-    double* hy = hits ? (double*)(dev + L.off_hy) : nullptr;
-    int* nh = (int*)(dev + L.off_i);
-    int* na = nh + n;
-    int* nr = na + n;
-    int* st = nr + n;
-    void* ws = dev + L.io_bytes;
-    if (hits && cudaMemsetAsync(ht, 0xFF, 8ull * hits * n * (1 + d), s) != cudaSuccess) return HG_ERR_CUDA;
-    if (!hits && cudaMemsetAsync(nh, 0, 4ull * n, s) != cudaSuccess) return HG_ERR_CUDA;
-    int rc;
-    if (d == 6 && n >= 4096) {
-      // wide batches: host-scheduled segments (synchronous on this stream)
-      rc = hg_propagate_dop853_scheduled(handles[b.slot], k.mu, d, n, (const double*)dev, n, nullptr, nullptr, k.t0,
-                                         k.tmax, &k.o, k.has_ev ? &k.ev : nullptr, 0, 0, nullptr, ye, te, ht, hy,
-                                         hits ? nh : nullptr, na, nr, st, ws, L.ws_bytes, s);
-    } else {
-      // one segment long enough to finish every trajectory (same results as
-      // a single pass; the event records live in the batch's workspace)
-      const long long seg = std::min<long long>(k.o.max_steps + 1, INT_MAX);
-      rc = hg_propagate_dop853_segmented(handles[b.slot], k.mu, d, n, (const double*)dev, n, nullptr, nullptr, k.t0,
-                                         k.tmax, &k.o, k.has_ev ? &k.ev : nullptr, 0, 0, nullptr, ye, te, ht, hy,
-                                         hits ? nh : nullptr, na, nr, st, (int)seg, 1, 0, ws, L.ws_bytes, s);
-    }
-    if (rc != HG_OK) {
-      cudaStreamSynchronize(s);
-      return rc;
-    }
-    if (cudaMemcpyAsync(stg + L.off_ye, dev + L.off_ye, (size_t)L.out_bytes(), cudaMemcpyDeviceToHost, s) !=
-        cudaSuccess) {
-      cudaStreamSynchronize(s);
-      return HG_ERR_CUDA;
-    }
-    return cudaStreamSynchronize(s) == cudaSuccess ? HG_OK : HG_ERR_CUDA;
   }
 
-  // scatter a finished batch to its requests (called with the lock held)
-  void finish(Batch& b) {
-    const int d = b.key.dim, n = b.n, hits = b.key.has_ev ? b.key.ev.max_hits : 0;
-    const Layout L(d, n, hits);
-    const char* stg = stg_base + b.stg_off;
-    const double* h_yend = (const double*)(stg + L.off_ye);
-    const double* h_tend = (const double*)(stg + L.off_te);
-    const double* h_hitt = (const double*)(stg + L.off_ht);
-    const double* h_hity = (const double*)(stg + L.off_hy);
-    const int* h_nh = (const int*)(stg + L.off_i);
-    const int* h_na = h_nh + n;
-    const int* h_nr = h_na + n;
-    const int* h_st = h_nr + n;
-    const auto now = Clock::now();
-    int o = 0;
-    for (auto& r : b.reqs) {
-      const int m = r->n;
-      if (b.rc == HG_OK) {
-        r->y_end.resize((size_t)m * d);
-        r->t_end.resize(m);
-        r->n_hits.resize(m);
-        r->n_acc.resize(m);
-        r->n_rej.resize(m);
-        r->status.resize(m);
-        r->hit_t.resize((size_t)m * hits);
-        r->hit_y.resize((size_t)m * hits * d);
-        for (int i = 0; i < m; ++i) {
-          const int g = o + i;
-          for (int c = 0; c < d; ++c) r->y_end[(size_t)i * d + c] = h_yend[(size_t)c * n + g];
-          r->t_end[i] = h_tend[g];
-          r->n_hits[i] = hits ? h_nh[g] : 0;
-          r->n_acc[i] = h_na[g];
-          r->n_rej[i] = h_nr[g];
-          r->status[i] = h_st[g];
-          for (int j = 0; j < hits; ++j) {
-            r->hit_t[(size_t)i * hits + j] = h_hitt[(size_t)j * n + g];
-            for (int c = 0; c < d; ++c)
-              r->hit_y[((size_t)i * hits + j) * d + c] = h_hity[((size_t)j * d + c) * n + g];
+  // The pool's loop (its own thread): admit, advance one segment, collect;
+  // returns when its problem has no trajectory live or waiting.
+  int run_pool(Pool& P) {
+    const Key& k = P.key;
+    const int d = P.dim, H = P.hits, C = P.C;
+    const RowShape rs{d, H};
+    const PoolLayout L(C, d, H);
+    cudaStream_t s = streams[P.slot];
+    if (cudaSetDevice(cfg.device) != cudaSuccess) return HG_ERR_CUDA;
+    char* dv = dev_base + P.dev_off;
+    char* sg = stg_base + P.stg_off;
+    double* y0 = (double*)(dv + L.y0);
+    int* status = (int*)(dv + L.st);
+    int* lists[2] = {(int*)(dv + L.list0), (int*)(dv + L.list1)};
+    int* cnt = (int*)(dv + L.cnt);  // [0], [1] counts of the two live lists, [2] finished rows
+    int* s_cnt = (int*)(sg + L.s_cnt);
+    hg::DopParams p;
+    memset(&p, 0, sizeof(p));
+    p.N = C;
+    p.mu = k.mu;
+    p.dir.neg_lo = k.o.fwd == -1 ? k.o.flip_lo : 0;
+    p.dir.neg_hi = k.o.fwd == -1 ? k.o.flip_hi : 0;
+    p.y0 = y0;
+    p.ld = C;
+    p.t0 = k.t0;
+    p.tmax = k.tmax;
+    p.rtol = k.o.rtol;
+    p.atol = k.o.atol;
+    p.max_step = k.o.max_step;
+    p.min_step = k.o.min_step;
+    p.max_steps = k.o.max_steps;
+    p.ev_index = -1;
+    if (k.has_ev) {
+      p.ev_index = k.ev.index;
+      p.ev_offset = k.ev.offset;
+      p.ev_dir = k.ev.direction;
+      p.max_hits = k.ev.max_hits;
+      p.xtol = k.ev.xtol;
+      p.gtol = k.ev.gtol;
+      const long long recs = (long long)C * H;
+      char* ra = dv + L.refine;
+      p.refine_count = (int*)ra;
+      p.refine_list = (int*)(ra + 256);
+      p.refine_hit = (int*)(ra + 256 + Arena::up(recs * 4));
+      p.rec = (double*)(ra + 256 + 2 * Arena::up(recs * 4));
+      p.rec_ld = recs;
+      p.hit_t = (double*)(dv + L.hit_t);
+      p.hit_y = (double*)(dv + L.hit_y);
+      p.n_hits = (int*)(dv + L.nh);
+    }
+    p.y_end = (double*)(dv + L.y_end);
+    p.t_end = (double*)(dv + L.t_end);
+    p.n_accept = (int*)(dv + L.na);
+    p.n_reject = (int*)(dv + L.nr);
+    p.status = status;
+    p.seg = 1;
+    p.seg_steps = cfg.seg_steps;
+    p.ws_h = (double*)(dv + L.wh);
+    p.ws_err_prev = (double*)(dv + L.wep);
+    p.ws_prev_pow = (double*)(dv + L.wpp);
+    p.ws_q = (int*)(dv + L.wq);
+    int live = 0, a = 0;
+    std::vector<int> slots;
+    std::vector<std::pair<std::shared_ptr<Request>, int>> who;
+    for (;;) {
+      slots.clear();
+      who.clear();
+      {
+        std::lock_guard<std::mutex> g(mu);
+        take_admissions(P, slots, who);
+        if (live == 0 && slots.empty()) return HG_OK;  // no work left for this problem
+      }
+      const int n_new = (int)slots.size();
+      if (n_new > 0) {
+        double* stg_y0 = (double*)(sg + L.s_y0);
+        int* stg_slots = (int*)(sg + L.s_slots);
+        for (int j = 0; j < n_new; ++j) {
+          const auto& w = who[j];
+          for (int c = 0; c < d; ++c) stg_y0[(long long)c * n_new + j] = w.first->y0[(size_t)w.second * d + c];
+          stg_slots[j] = slots[j];
+        }
+        if (cudaMemcpyAsync(dv + L.stage_y0, stg_y0, 8ull * d * n_new, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(dv + L.stage_slots, stg_slots, 4ull * n_new, cudaMemcpyHostToDevice, s) != cudaSuccess)
+          return HG_ERR_CUDA;
+        const int blocks = std::min((n_new + 255) / 256, 1024);
+        admit_kernel<<<blocks, 256, 0, s>>>(n_new, C, d, (const double*)(dv + L.stage_y0),
+                                            (const int*)(dv + L.stage_slots), y0, status, lists[a], cnt + a, live);
+        if (cudaGetLastError() != cudaSuccess) return HG_ERR_CUDA;
+        live += n_new;
+      }
+      // one segment over the live list, then the crossings it saved
+      const int b = a ^ 1;
+      if (cudaMemsetAsync(cnt + b, 0, sizeof(int), s) != cudaSuccess ||
+          cudaMemsetAsync(cnt + 2, 0, sizeof(int), s) != cudaSuccess)
+        return HG_ERR_CUDA;
+      if (k.has_ev && cudaMemsetAsync(p.refine_count, 0, sizeof(int), s) != cudaSuccess) return HG_ERR_CUDA;
+      p.active_in = lists[a];
+      p.n_in = cnt + a;
+      p.active_out = lists[b];
+      p.n_out = cnt + b;
+      const int g = lanes_for(d, live, sms);
+      cudaError_t e;
+      if (d == 6)
+        e = g == 6 ? segment<6>(p, live, sms, s) : (g == 2 ? segment<2>(p, live, sms, s) : segment<1>(p, live, sms, s));
+      else
+        e = g == 14 ? segment<14>(p, live, sms, s) : segment<7>(p, live, sms, s);
+      if (e == cudaSuccess && k.has_ev) e = d == 6 ? refine<1>(p, sms, s) : refine<7>(p, sms, s);
+      if (e != cudaSuccess) return HG_ERR_CUDA;
+      // finished slots of this segment's list: rows gathered and brought back
+      {
+        const int blocks = std::min((live + 255) / 256, 1024);
+        collect_kernel<<<blocks, 256, 0, s>>>(C, d, H, lists[a], cnt + a, p.y_end, p.t_end, p.hit_t, p.hit_y,
+                                              p.n_accept, p.n_reject, (const int*)(dv + L.nh), status,
+                                              (int*)(dv + L.fin), cnt + 2, (double*)(dv + L.out_d),
+                                              (int*)(dv + L.out_i));
+        if (cudaGetLastError() != cudaSuccess) return HG_ERR_CUDA;
+      }
+      if (cudaMemcpyAsync(s_cnt, cnt, 16, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess)
+        return HG_ERR_CUDA;
+      const int n_fin = s_cnt[2];
+      const int next_live = s_cnt[b];
+      if (n_fin > 0) {
+        if (cudaMemcpyAsync(sg + L.s_fin, dv + L.fin, 4ull * n_fin, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(sg + L.s_out_d, dv + L.out_d, 8ull * rs.nd() * n_fin, cudaMemcpyDeviceToHost, s) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(sg + L.s_out_i, dv + L.out_i, 4ull * RowShape::ni * n_fin, cudaMemcpyDeviceToHost, s) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+          return HG_ERR_CUDA;
+      }
+      {
+        std::lock_guard<std::mutex> g(mu);
+        ++segments;
+        const int* fin = (const int*)(sg + L.s_fin);
+        const double* od = (const double*)(sg + L.s_out_d);
+        const int* oi = (const int*)(sg + L.s_out_i);
+        const auto now = Clock::now();
+        for (int q = 0; q < n_fin; ++q) {
+          const int sl = fin[q];
+          auto own = P.owner[sl];
+          P.owner[sl].first.reset();
+          P.free_slots.push_back(sl);
+          Request& r = *own.first;
+          const int i = own.second;
+          const double* row = od + (long long)q * rs.nd();
+          for (int c = 0; c < d; ++c) r.y_end[(size_t)i * d + c] = row[c];
+          r.t_end[i] = row[d];
+          for (int j = 0; j < H; ++j) {
+            r.hit_t[(size_t)i * H + j] = row[d + 1 + j];
+            for (int c = 0; c < d; ++c) r.hit_y[((size_t)i * H + j) * d + c] = row[d + 1 + H + j * d + c];
+          }
+          const int* ri = oi + (long long)q * RowShape::ni;
+          r.n_acc[i] = ri[0];
+          r.n_rej[i] = ri[1];
+          r.n_hits[i] = ri[2];
+          r.status[i] = ri[3];
+          if (++r.done == r.n) {
+            r.state = 2;
+            r.finished = now;
+            latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r.submitted).count());
           }
         }
-        r->state = 2;
-      } else {
-        r->state = 3;
-        r->error = b.rc;
       }
-      r->finished = now;
-      latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->submitted).count());
-      o += m;
+      if (n_fin > 0) cv.notify_all();
+      live = next_live;
+      a = b;
     }
-    dev_arena.release(b.dev_off, b.dev_len);
-    stg_arena.release(b.stg_off, b.stg_len);
-    slot_busy[b.slot] = 0;
-    ++batches;
   }
 
-  // A request that can never fit the arenas fails at once (lock held).
-  void reject(const std::shared_ptr<Request>& r) {
-    r->state = 3;
-    r->error = HG_ERR_ARGS;
-    r->finished = Clock::now();
-    latencies_ms.push_back(std::chrono::duration<double, std::milli>(r->finished - r->submitted).count());
+  // A pool that failed (lock held): the requests it holds, and those of its
+  // problem still waiting, fail.
+  void fail_pool(Pool& P, int rc) {
+    const auto now = Clock::now();
+    for (auto& o : P.owner) {
+      if (!o.first) continue;
+      Request& r = *o.first;
+      if (r.state < 2) {
+        r.state = 3;
+        r.error = rc;
+        r.finished = now;
+      }
+      o.first.reset();
+    }
+    for (auto& r : pending)
+      if (same_key(r->key, P.key) && r->state < 2) {
+        r->state = 3;
+        r->error = rc;
+        r->finished = now;
+      }
+    pending.erase(std::remove_if(pending.begin(), pending.end(),
+                                 [](const std::shared_ptr<Request>& r) { return r->state == 3; }),
+                  pending.end());
   }
-
-  long long dev_free_bytes() const { return free_total(dev_arena); }
-  long long stg_free_bytes() const { return free_total(stg_arena); }
-  static long long free_total(const Arena& a) { return a.free_bytes(); }
 
   void run() {
     std::unique_lock<std::mutex> lk(mu);
     while (true) {
-      // completed batches
-      for (size_t q = 0; q < running.size();) {
-        Batch& b = *running[q];
-        if (b.finished.load()) {
-          if (b.runner.joinable()) b.runner.join();
-          finish(b);
-          running.erase(running.begin() + q);
+      // retired pools return their arena blocks and stream
+      for (size_t q = 0; q < pools.size();) {
+        Pool& P = *pools[q];
+        if (P.finished.load()) {
+          if (P.runner.joinable()) {
+            lk.unlock();
+            P.runner.join();
+            lk.lock();
+          }
+          if (P.rc != HG_OK) fail_pool(P, P.rc);
+          dev_arena.release(P.dev_off, P.dev_len);
+          stg_arena.release(P.stg_off, P.stg_len);
+          slot_busy[P.slot] = 0;
+          pools.erase(pools.begin() + q);
           cv.notify_all();
         } else {
           ++q;
         }
       }
-      if (stop && pending.empty() && running.empty()) return;
-      // admit: merge pending requests per problem, in arrival order, while
-      // the merged batches' blocks fit what the arenas have free
-      std::vector<std::unique_ptr<Batch>> admit;
-      if (!pending.empty()) {
-        std::map<Key, Batch*> open;
-        std::deque<std::shared_ptr<Request>> keep;
-        long long dev_free = dev_free_bytes(), stg_free = stg_free_bytes();
-        for (auto& r : pending) {
-          const int hits = r->key.has_ev ? r->key.ev.max_hits : 0;
-          const Layout alone(r->key.dim, r->n, hits);
-          if (alone.device_bytes() > dev_arena.size() || alone.io_bytes > stg_arena.size()) {
-            reject(r);
-            continue;
+      if (stop && pending.empty() && pools.empty()) return;
+      // open a pool for the oldest waiting problem that has none
+      bool opened = false;
+      for (auto& r : pending) {
+        bool has_pool = false;
+        for (auto& P : pools) has_pool |= same_key(P->key, r->key);
+        if (has_pool) continue;
+        int free_slot = -1;
+        for (size_t i = 0; i < slot_busy.size(); ++i)
+          if (!slot_busy[i]) {
+            free_slot = (int)i;
+            break;
           }
-          auto it = open.find(r->key);
-          Batch* b = it == open.end() ? nullptr : it->second;
-          const Layout before(r->key.dim, b ? b->n : 0, hits), after(r->key.dim, (b ? b->n : 0) + r->n, hits);
-          const long long dd = b ? after.device_bytes() - before.device_bytes() : after.device_bytes();
-          const long long ds = b ? after.io_bytes - before.io_bytes : after.io_bytes;
-          int free_slot = -1;
-          if (!b) {
-            for (size_t sidx = 0; sidx < slot_busy.size(); ++sidx)
-              if (!slot_busy[sidx]) {
-                bool taken = false;
-                for (auto& a : admit) taken |= a->slot == (int)sidx;
-                if (!taken) {
-                  free_slot = (int)sidx;
-                  break;
-                }
-              }
-          }
-          if (dd <= dev_free && ds <= stg_free && (b || free_slot >= 0)) {
-            if (!b) {
-              admit.emplace_back(new Batch());
-              b = admit.back().get();
-              b->key = r->key;
-              b->slot = free_slot;
-              open[r->key] = b;
-            }
-            b->reqs.push_back(r);
-            b->n += r->n;
-            dev_free -= dd;
-            stg_free -= ds;
-          } else {
-            keep.push_back(r);
-          }
+        if (free_slot < 0) break;
+        const int d = r->key.dim, H = r->key.has_ev ? r->key.ev.max_hits : 0;
+        // slots: pool_slots, halved until the free arenas hold the pool
+        int C = cfg.pool_slots;
+        while (C >= 32) {
+          const PoolLayout L(C, d, H);
+          if (L.dev_bytes <= dev_arena.largest() && L.stg_bytes <= stg_arena.largest()) break;
+          C /= 2;
         }
-        // blocks for the admitted batches; a batch that does not fit the free
-        // blocks (fragmentation) goes back to waiting, in arrival order
-        std::vector<std::unique_ptr<Batch>> placed;
-        std::deque<std::shared_ptr<Request>> back;
-        for (auto& b : admit) {
-          const int hits = b->key.has_ev ? b->key.ev.max_hits : 0;
-          const Layout L(b->key.dim, b->n, hits);
-          b->dev_len = L.device_bytes();
-          b->stg_len = L.io_bytes;
-          b->dev_off = dev_arena.alloc(b->dev_len);
-          b->stg_off = b->dev_off >= 0 ? stg_arena.alloc(b->stg_len) : -1;
-          if (b->dev_off < 0 || b->stg_off < 0) {
-            if (b->dev_off >= 0) dev_arena.release(b->dev_off, b->dev_len);
-            for (auto& r : b->reqs) back.push_back(r);
-            continue;
+        if (C < 32) {
+          if (pools.empty()) {
+            // not even 32 slots fit an idle server: the request cannot run
+            auto gone = r;
+            gone->state = 3;
+            gone->error = HG_ERR_ARGS;
+            gone->finished = Clock::now();
+            pending.erase(std::find(pending.begin(), pending.end(), gone));
+            cv.notify_all();
+            opened = true;  // rescan
           }
-          for (auto& r : b->reqs) r->state = 1;
-          placed.push_back(std::move(b));
+          break;
         }
-        if (!back.empty()) {
-          // restore arrival order among the requests sent back and those kept
-          for (auto& r : keep) back.push_back(r);
-          std::stable_sort(back.begin(), back.end(),
-                           [](const std::shared_ptr<Request>& x, const std::shared_ptr<Request>& y) {
-                             return x->id < y->id;
-                           });
-          keep.swap(back);
+        const PoolLayout L(C, d, H);
+        std::unique_ptr<Pool> P(new Pool());
+        P->key = r->key;
+        P->dim = d;
+        P->hits = H;
+        P->C = C;
+        P->slot = free_slot;
+        P->dev_len = L.dev_bytes;
+        P->stg_len = L.stg_bytes;
+        P->dev_off = dev_arena.alloc(L.dev_bytes);
+        P->stg_off = P->dev_off >= 0 ? stg_arena.alloc(L.stg_bytes) : -1;
+        if (P->dev_off < 0 || P->stg_off < 0) {
+          if (P->dev_off >= 0) dev_arena.release(P->dev_off, P->dev_len);
+          break;
         }
-        pending.swap(keep);
-        admit.swap(placed);
-      }
-      for (auto& b : admit) {
-        slot_busy[b->slot] = 1;
-        Batch* bp = b.get();
-        // each batch runs on its own thread (the scheduled driver waits on
-        // its stream); completion wakes this loop
-        bp->runner = std::thread([this, bp] {
+        P->free_slots.resize(C);
+        for (int i = 0; i < C; ++i) P->free_slots[i] = C - 1 - i;  // slot 0 taken first
+        P->owner.resize(C);
+        slot_busy[free_slot] = 1;
+        Pool* pp = P.get();
+        pools.push_back(std::move(P));
+        pp->runner = std::thread([this, pp] {
           cudaSetDevice(cfg.device);
-          bp->rc = launch(*bp);
-          bp->finished.store(1);
+          pp->rc = run_pool(*pp);
+          pp->finished.store(1);
           cv.notify_all();
         });
-        running.push_back(std::move(b));
+        opened = true;
+        break;  // one at a time: rescan with the new pool in place
       }
-      if (admit.empty()) cv.wait_for(lk, std::chrono::microseconds(500));
+      if (!opened) cv.wait_for(lk, std::chrono::microseconds(500));
     }
   }
 };
@@ -403,6 +632,8 @@ void hg_serve_config_default(hg_serve_config* c) {
   c->hbm_budget_bytes = 8LL << 30;
   c->max_concurrent = 4;
   c->staging_bytes = 1LL << 30;
+  c->pool_slots = 16384;
+  c->seg_steps = 32;
 }
 
 int hg_serve_create(const hg_serve_config* cfg, hg_server** out) {
@@ -411,19 +642,21 @@ int hg_serve_create(const hg_serve_config* cfg, hg_server** out) {
   hg_serve_config c;
   hg_serve_config_default(&c);
   if (cfg) c = *cfg;
-  if (c.max_concurrent < 1 || c.max_concurrent > 64 || c.hbm_budget_bytes <= 0 || c.staging_bytes <= 0)
+  if (c.max_concurrent < 1 || c.max_concurrent > 64 || c.hbm_budget_bytes <= 0 || c.staging_bytes <= 0 ||
+      c.pool_slots < 32 || c.pool_slots > (1 << 24) || c.seg_steps < 1 || c.seg_steps > (1 << 20))
     return HG_ERR_ARGS;
   std::unique_ptr<hg_server> s(new hg_server());
   s->cfg = c;
   if (cudaSetDevice(c.device) != cudaSuccess) return HG_ERR_NO_DEVICE;
   // a failure part way releases what was made so far (no worker runs yet)
   auto release = [&s](int rc) {
-    for (auto h : s->handles) hg_destroy(h);
     for (auto st : s->streams) cudaStreamDestroy(st);
     if (s->dev_base) cudaFree(s->dev_base);
     if (s->stg_base) cudaFreeHost(s->stg_base);
     return rc;
   };
+  if (cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess || s->sms < 1)
+    return release(HG_ERR_NO_DEVICE);
   if (cudaMalloc(&s->dev_base, (size_t)c.hbm_budget_bytes) != cudaSuccess) {
     s->dev_base = nullptr;
     cudaGetLastError();
@@ -440,11 +673,6 @@ int hg_serve_create(const hg_serve_config* cfg, hg_server** out) {
     cudaStream_t st;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return release(HG_ERR_CUDA);
     s->streams.push_back(st);
-    hg_handle* h = nullptr;
-    hg_config hc{c.device};
-    const int rc = hg_create(&hc, &h);
-    if (rc != HG_OK) return release(rc);
-    s->handles.push_back(h);
   }
   s->slot_busy.assign(c.max_concurrent, 0);
   hg_server* raw = s.release();
@@ -465,7 +693,6 @@ int hg_serve_destroy(hg_server* s) {
   }
   s->cv.notify_all();
   if (s->worker.joinable()) s->worker.join();
-  for (auto h : s->handles) hg_destroy(h);
   for (auto st : s->streams) cudaStreamDestroy(st);
   if (s->dev_base) cudaFree(s->dev_base);
   if (s->stg_base) cudaFreeHost(s->stg_base);
@@ -476,7 +703,11 @@ int hg_serve_destroy(hg_server* s) {
 int hg_serve_submit(hg_server* s, double mu, int dim, int N, const double* y0, double t0, double tmax,
                     const hg_dop853_opts* opts, const hg_event* ev, long long* request_id) {
   if (!s || !request_id || !opts || (dim != 6 && dim != 42) || N < 1 || !y0) return HG_ERR_ARGS;
-  if (ev && ev->index >= 0 && (ev->index >= dim || ev->max_hits < 1)) return HG_ERR_ARGS;
+  if (ev && ev->index >= 0 && (ev->index >= dim || ev->max_hits < 1 || ev->direction < -1 || ev->direction > 1))
+    return HG_ERR_ARGS;
+  if (opts->flip_lo < 0 || opts->flip_hi > dim || opts->flip_lo > opts->flip_hi || !(opts->rtol >= 0.0) ||
+      !(opts->atol >= 0.0) || !(opts->min_step > 0.0) || !(opts->max_step > 0.0) || opts->max_steps < 1)
+    return HG_ERR_ARGS;
   auto r = std::make_shared<Request>();
   memset(&r->key, 0, sizeof(Key));
   r->key.mu = mu;
@@ -502,8 +733,17 @@ int hg_serve_submit(hg_server* s, double mu, int dim, int N, const double* y0, d
     r->key.ev.xtol = ev->xtol;
     r->key.ev.gtol = ev->gtol;
   }
+  const int H = r->key.has_ev ? r->key.ev.max_hits : 0;
   r->n = N;
   r->y0.assign(y0, y0 + (size_t)N * dim);
+  r->y_end.assign((size_t)N * dim, 0.0);
+  r->t_end.assign(N, 0.0);
+  r->hit_t.assign((size_t)N * H, 0.0);
+  r->hit_y.assign((size_t)N * H * dim, 0.0);
+  r->n_hits.assign(N, 0);
+  r->n_acc.assign(N, 0);
+  r->n_rej.assign(N, 0);
+  r->status.assign(N, 0);
   r->submitted = Clock::now();
   {
     std::lock_guard<std::mutex> g(s->mu);
@@ -581,7 +821,7 @@ int hg_serve_stats(hg_server* s, double* p50_ms, double* p99_ms, long long* requ
   {
     std::lock_guard<std::mutex> g(s->mu);
     v = s->latencies_ms;
-    if (batches) *batches = s->batches;
+    if (batches) *batches = s->segments;
   }
   if (requests) *requests = (long long)v.size();
   auto pct = [&](double q) {

@@ -241,18 +241,21 @@ def poisson_requests(rate_hz, duration_s, mu, seed=0, manifold_seeds=None, size_
 
 class NativeServer:
     """The library's native request server (``hg_serve_*``): continuous
-    batching of DOP853 propagation requests behind the C ABI, for callers
-    that do not run this Python engine.  Requests with the same problem (mu,
-    dimension, span, options, event) are merged; results equal direct calls."""
+    batching of DOP853 propagation requests behind the C ABI at the level of
+    trajectory slots -- every problem (mu, dimension, span, options, event)
+    gets a pool of device-resident slots that waiting requests enter as slots
+    free up, segment by segment; results equal direct calls."""
 
-    def __init__(self, device=0, hbm_budget_bytes=8 << 30, max_concurrent=4, staging_bytes=None):
+    def __init__(self, device=0, hbm_budget_bytes=8 << 30, max_concurrent=4, staging_bytes=None, pool_slots=16384,
+                 seg_steps=32):
         import ctypes as C
         from . import _lib
         self._C, self._lib = C, _lib
         self.L = _lib.load()
         if staging_bytes is None:
             staging_bytes = min(int(hbm_budget_bytes), 1 << 30)
-        cfg = _lib.hg_serve_config(int(device), int(hbm_budget_bytes), int(max_concurrent), int(staging_bytes))
+        cfg = _lib.hg_serve_config(int(device), int(hbm_budget_bytes), int(max_concurrent), int(staging_bytes),
+                                   int(pool_slots), int(seg_steps))
         self.ptr = C.c_void_p()
         rc = self.L.hg_serve_create(C.byref(cfg), C.byref(self.ptr))
         if rc != _lib.HG_OK:

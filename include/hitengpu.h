@@ -322,31 +322,37 @@ int hg_correct_halo_graph(hg_handle* h, double mu, int N, double* x, long long l
                           int* iterations, double* residual, int* status, const hg_newton_opts* opts,
                           void* workspace, long long workspace_bytes, void* stream);
 
-/* Native request server (continuous batching of DOP853 propagation
- * requests).  A worker thread merges every pending request that shares a
- * problem (mu, dim, t0, tmax, options, event) into one batch, admits batches
- * while their blocks fit the server's arenas, runs up to max_concurrent
- * batches at once on its own streams and handles (wide 6-dim batches as
- * host-scheduled segments) and keeps each request's results on the host
- * until fetched.  hg_serve_create allocates a device arena of
- * hbm_budget_bytes (each batch's inputs, outputs and workspace) and a pinned
- * host arena of staging_bytes (each batch's inputs and outputs, so its copies
- * are asynchronous); nothing is allocated afterwards, and a request too large
- * for either arena alone fails (state 3, HG_ERR_ARGS).  Results equal a
- * direct hg_propagate_dop853 call on the request alone.  Requests: y0 host
- * row-major (N, dim); results host
- * row-major: y_end (N, dim), t_end (N), hit_t (N, max_hits), hit_y (N,
- * max_hits, dim), n_hits / n_accept / n_reject / status (N); null outputs
- * are skipped.  Poll states: 0 pending, 1 running, 2 done, 3 failed.
- * Latency = submit to completion; hg_serve_stats reports its p50 / p99.
+/* Native request server: continuous batching of DOP853 propagation requests
+ * at the level of trajectory slots.  Every problem (mu, dim, t0, tmax,
+ * options, event) with work gets a pool of device-resident trajectory slots
+ * (pool_slots, halved until the server's free arenas hold the pool) on its own
+ * stream; at most max_concurrent pools run at once.  A pool's thread admits
+ * the waiting requests' trajectories into free slots (a request may enter
+ * over several rounds), advances every live slot by seg_steps attempted
+ * steps, refines the crossings saved, and returns the trajectories that
+ * finished to their requests, freeing their slots: a request arriving while
+ * others run enters at the next segment boundary, as slots free up.
+ * hg_serve_create allocates a device arena of hbm_budget_bytes and a pinned
+ * host arena of staging_bytes that the pools are carved from; nothing is
+ * allocated afterwards, and a request whose problem cannot get even a
+ * 32-slot pool on an idle server fails (state 3, HG_ERR_ARGS).  Results equal
+ * a direct hg_propagate_dop853 call on the request alone.  Requests: y0 host
+ * row-major (N, dim); results host row-major: y_end (N, dim), t_end (N),
+ * hit_t (N, max_hits), hit_y (N, max_hits, dim), n_hits / n_accept /
+ * n_reject / status (N); null outputs are skipped.  Poll states: 0 pending,
+ * 1 running (some trajectories admitted), 2 done, 3 failed.  Latency =
+ * submit to completion; hg_serve_stats reports its p50 / p99 and the number
+ * of segments run.
  * Replaces: nothing in the reference (its solves are synchronous calls);
  * the serving pattern of this library's Python engine behind the C ABI. */
 typedef struct hg_server hg_server;
 typedef struct hg_serve_config {
   int device;
   long long hbm_budget_bytes; /* device arena (default 8 GiB) */
-  int max_concurrent;         /* batches in flight (default 4) */
+  int max_concurrent;         /* pools (problems) in flight (default 4) */
   long long staging_bytes;    /* pinned host arena (default 1 GiB) */
+  int pool_slots;             /* trajectory slots of a pool (default 16384, >= 32) */
+  int seg_steps;              /* attempted steps per segment (default 32) */
 } hg_serve_config;
 void hg_serve_config_default(hg_serve_config* c);
 int hg_serve_create(const hg_serve_config* cfg, hg_server** out);
