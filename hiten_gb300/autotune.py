@@ -113,7 +113,7 @@ def tune(key, fn, shapes=DEFAULT_SHAPES, reps=2, device=None, cache_file=None):
 
 # Lane layouts of the device-resident halo correction (hg_correct_halo_graph):
 # lanes per 6-dim event-leg trajectory and per 42-dim STM-leg trajectory.
-CORRECT_SHAPES = ((6, 14), (6, 7), (2, 14), (1, 14))
+CORRECT_SHAPES = ((6, 12), (6, 18), (6, 14), (2, 12), (1, 12))
 _correct_cache = {}
 
 

@@ -34,6 +34,7 @@
 
 #include "hg_internal.h"
 #include "hg_kernels.cuh"
+#include "hg_pair.cuh"
 #include "hitengpu.h"
 
 namespace {
@@ -680,12 +681,22 @@ void stm_leg(const Ws& w, double mu, const hg_newton_opts& o, int sms, cudaStrea
   p.ws_err_prev = w.wep;
   p.ws_prev_pow = w.wpp;
   p.ws_q = w.wq;
-  const int tpb = hg::Layout<G>::TPW;
-  const int need = (w.cap + tpb - 1) / tpb;
-  const int cap_blocks = resident_blocks(hg::dop853_kernel<G, true>, 32, sms);
-  const int grid = need < cap_blocks ? need : cap_blocks;
-  p.stride = grid * tpb;
-  hg::dop853_kernel<G, true><<<grid, 32, 0, s>>>(p);
+  if constexpr (G == 12 || G == 18) {
+    // the paired (12) and three-warp (18) layouts: five trajectories per
+    // block, the live count read from n_in (their list is the identity)
+    const int grid = (w.cap + hg::kPairTraj - 1) / hg::kPairTraj;
+    if constexpr (G == 18)
+      hg::dop853_trio_kernel<<<grid, 96, 0, s>>>(p);
+    else
+      hg::dop853_pair_kernel<<<grid, 64, 0, s>>>(p);
+  } else {
+    const int tpb = hg::Layout<G>::TPW;
+    const int need = (w.cap + tpb - 1) / tpb;
+    const int cap_blocks = resident_blocks(hg::dop853_kernel<G, true>, 32, sms);
+    const int grid = need < cap_blocks ? need : cap_blocks;
+    p.stride = grid * tpb;
+    hg::dop853_kernel<G, true><<<grid, 32, 0, s>>>(p);
+  }
   *launches += 1;
 }
 
@@ -697,7 +708,13 @@ int lanes_d6(int n, int sms, int tuned) {
   return 1;
 }
 
-int lanes_d42(int tuned) { return tuned == 7 ? 7 : 14; }
+// STM leg layout: the handle's tuning, else the three-warp layout while its
+// warps fit about three per SM (3 N / 5 <= 3 x SMs) and the paired warps above
+// (the host driver's rule for event-free 42-dim legs).
+int lanes_d42(int tuned, int n, int sms) {
+  if (tuned == 7 || tuned == 14 || tuned == 12 || tuned == 18) return tuned;
+  return 3LL * ((n + hg::kPairTraj - 1) / hg::kPairTraj) <= 3LL * sms ? 18 : 12;
+}
 
 void event_leg_any(int g, const Ws& w, double mu, const hg_newton_opts& o, int sms, cudaStream_t s, int* n) {
   if (g == 6)
@@ -808,8 +825,12 @@ cudaError_t build_graph(const Ws& w, double mu, const hg_newton_opts& o, int g6,
   gc_converge<<<1, kBlockCtl, 0, s>>>(w, o.tol);
   if (g42 == 7)
     stm_leg<7>(w, mu, o, sms, s, &nk);
-  else
+  else if (g42 == 14)
     stm_leg<14>(w, mu, o, sms, s, &nk);
+  else if (g42 == 18)
+    stm_leg<18>(w, mu, o, sms, s, &nk);
+  else
+    stm_leg<12>(w, mu, o, sms, s, &nk);
   gc_newton<<<blocks, 256, 0, s>>>(w, mu, o.cond_threshold, o.max_delta, inner);
   nk += 2;
   cudaGraph_t body_g = body;
@@ -883,7 +904,7 @@ int hg_correct_halo_graph(hg_handle* h, double mu, int N, double* x, long long l
   layout(N, (char*)workspace, &w);
   const int spec_traj = N < 20 * sms ? N : 20 * sms;
   const int g6 = lanes_d6(N, sms, hg_internal::tuning(h, HG_TUNE_DOP853_LANES_D6));
-  const int g42 = lanes_d42(hg_internal::tuning(h, HG_TUNE_LANES_D42));
+  const int g42 = lanes_d42(hg_internal::tuning(h, HG_TUNE_LANES_D42), N, sms);
   void** slot = hg_internal::graph_slot(h, free_cache);
   GraphCache* c = (GraphCache*)*slot;
   const bool hit = c && c->ws == workspace && c->N == N && c->mu == mu && same_opts(c->o, o) && c->g6 == g6 &&

@@ -87,7 +87,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 // 1 arrives at a second barrier and warp 0's wait on it must succeed.
 // out[0] = 1 if the first wait ran out, out[1] = 1 if the second completed,
 // out[2] = elapsed nanoseconds of the first wait.
-__global__ void bounded_wait_selftest_kernel(int* out, unsigned long long limit_ns) {
+static __global__ void bounded_wait_selftest_kernel(int* out, unsigned long long limit_ns) {
   __shared__ unsigned long long bars[2];
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 32);
@@ -655,7 +655,7 @@ __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, Pa
 }
 
 // Blocks of one or two pairs, laid out as fixed_rk_pair_kernel's.
-__global__ void __launch_bounds__(128) dop853_pair_kernel(DopParams p) {
+static __global__ void __launch_bounds__(128) dop853_pair_kernel(DopParams p) {
   __shared__ PairLink links[2];
   __shared__ PairGather gathers[2];
   __shared__ double coef_tab[dop_nnz()];
@@ -678,10 +678,13 @@ __global__ void __launch_bounds__(128) dop853_pair_kernel(DopParams p) {
   __syncthreads();
   const PairLane pl(lane);
   const int group = blockIdx.x * npairs + pair;
-  const bool active = group * kPairTraj < p.N;  // uniform over the pair's two warps
+  // list mode (n_in given): the trajectories 0 .. *n_in - 1 of a launch sized
+  // for p.N run; the others' blocks return at once
+  const int N = p.n_in ? *p.n_in : p.N;
+  const bool active = group * kPairTraj < N;  // uniform over the pair's two warps
   const int traj = group * kPairTraj + pl.t;
-  const bool valid = active && traj < p.N;
-  const int tc = valid ? traj : (active ? p.N - 1 : 0);
+  const bool valid = active && traj < N;
+  const int tc = valid ? traj : (active ? N - 1 : 0);
   bool broken = false;
   if (active) {
     if (!stm) {
@@ -718,7 +721,7 @@ __global__ void __launch_bounds__(128) dop853_pair_kernel(DopParams p) {
 // batches too small to fill the GPU, where one warp's step sets the time.
 // The Hessian ring's "empty" barriers take both STM warps' arrivals, the
 // norm gather all three warps'.
-__global__ void __launch_bounds__(96) dop853_trio_kernel(DopParams p) {
+static __global__ void __launch_bounds__(96) dop853_trio_kernel(DopParams p) {
   __shared__ PairLink link;
   __shared__ PairGather gather;
   __shared__ double coef_tab[dop_nnz()];
@@ -734,13 +737,15 @@ __global__ void __launch_bounds__(96) dop853_trio_kernel(DopParams p) {
   __syncthreads();
   const PairLane pl(lane);
   const int group = blockIdx.x;
-  const bool active = group * kPairTraj < p.N;  // uniform over the block
+  // list mode (n_in given): the trajectories 0 .. *n_in - 1 run
+  const int N = p.n_in ? *p.n_in : p.N;
+  const bool active = group * kPairTraj < N;  // uniform over the block
   // trajectory of this lane within the group
   const int hg = 5 * (w - 1) + pl.t;                 // STM warps: half-group 0..9
   const int tg = w == 0 ? pl.t : hg / 2;
   const int traj = group * kPairTraj + tg;
-  const bool valid = active && traj < p.N;
-  const int tc = valid ? traj : (active ? p.N - 1 : 0);
+  const bool valid = active && traj < N;
+  const int tc = valid ? traj : (active ? N - 1 : 0);
   bool broken = false;
   if (active) {
     if (w == 0) {
