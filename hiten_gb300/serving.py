@@ -76,6 +76,31 @@ def _solve(kind, x, mu, device, batched=True):
     raise ValueError(kind)
 
 
+# The propagation problem of each propagating request kind: (t span, keyword
+# arguments of propagate_dop853 / NativeServer.submit), as _solve runs it.
+def _problem(kind, mu):
+    if kind == "manifold":
+        return 8.0, dict(rtol=1e-12, atol=1e-12, max_step=1e4, fwd=-1, flip=(0, 6),
+                         event=P.EventSpec(index=0, offset=1.0 - mu, direction=0, max_hits=1))
+    return 20.0, dict(rtol=1e-11, atol=1e-11, max_step=1e4, event=P.EventSpec(index=1, offset=0.0, direction=-1,
+                                                                                max_hits=8))
+
+
+def _native_result(kind, f):
+    """A request's rows from the native server in _solve's form (crossing
+    entries past each trajectory's count are NaN, as the direct call leaves them)."""
+    ht, hy = f["hit_t"].copy(), f["hit_y"].copy()
+    unused = np.arange(ht.shape[1])[None, :] >= f["n_hits"][:, None]
+    ht[unused] = np.nan
+    hy[unused] = np.nan
+    out = {"y_end": f["y_end"], "n_hits": f["n_hits"], "hit_t": ht, "hit_y": hy, "n_accept": f["n_accept"],
+           "status": f["status"]}
+    if kind == "manifold":
+        out = {"y_end": f["y_end"], "t_end": f["t_end"], "n_hits": f["n_hits"], "hit_t": ht, "hit_y": hy,
+               "n_accept": f["n_accept"], "status": f["status"]}
+    return out
+
+
 def _split(kind, res, sizes):
     out, off = [], 0
     for n in sizes:
@@ -121,9 +146,17 @@ class ServingStats:
 
 
 class ServingEngine:
-    """Continuous batching with HBM-footprint admission (see module docstring)."""
+    """Continuous batching with HBM-footprint admission (see module docstring).
 
-    def __init__(self, mu, device=None, hbm_budget_bytes=8 << 30, max_concurrent=6, tick_s=0.002):
+    ``slots=True``: manifold and synodic requests go to the library's native
+    server (``NativeServer``), where each kind runs in a pool of
+    device-resident trajectory slots that arriving requests enter at every
+    segment boundary as slots free up (lane-level admission; the budget is
+    the server's device arena); correction requests keep the per-tick merged
+    batches."""
+
+    def __init__(self, mu, device=None, hbm_budget_bytes=8 << 30, max_concurrent=6, tick_s=0.002, slots=False,
+                 pool_slots=16384, seg_steps=32):
         self.mu = float(mu)
         self.device = P._device(device)
         self.budget = int(hbm_budget_bytes)
@@ -134,6 +167,10 @@ class ServingEngine:
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_concurrent)]
         self.free_streams = list(range(max_concurrent))
         self.lock = threading.Lock()
+        self.native = None
+        if slots:
+            self.native = NativeServer(device=self.device.index or 0, hbm_budget_bytes=self.budget,
+                                       max_concurrent=2, pool_slots=pool_slots, seg_steps=seg_steps)
 
     def _run_batch(self, kind, reqs, sidx):
         x = np.concatenate([r.payload for r in reqs])
@@ -151,13 +188,25 @@ class ServingEngine:
         t0 = time.perf_counter() if t0 is None else t0
         waiting = []
         futures = set()
+        in_server = {}  # native request id -> request
         nxt = 0
         stats = ServingStats()
-        while nxt < len(requests) or waiting or futures:
+        while nxt < len(requests) or waiting or futures or in_server:
             now = time.perf_counter() - t0
             while nxt < len(requests) and requests[nxt].arrival <= now:
-                waiting.append(requests[nxt])
+                r = requests[nxt]
                 nxt += 1
+                if self.native is not None and r.kind != "correct":
+                    tf, kw = _problem(r.kind, self.mu)
+                    r.admitted = time.perf_counter()
+                    in_server[self.native.submit(r.payload, self.mu, 0.0, tf, **kw)] = r
+                else:
+                    waiting.append(r)
+            # requests the native server finished
+            for rid in [q for q in in_server if self.native.poll(q) >= 2]:
+                r = in_server.pop(rid)
+                r.result = _native_result(r.kind, self.native.fetch(rid))
+                r.done = time.perf_counter()
             # collect finished batches
             done = {f for f in futures if f.done()}
             for f in done:
@@ -174,7 +223,7 @@ class ServingEngine:
                     sidx = self.free_streams.pop()
                     futures.add(self.pool.submit(self._run_batch, kind, reqs, sidx))
             if not done:
-                time.sleep(self.tick_s)
+                time.sleep(self.tick_s if not in_server else min(self.tick_s, 0.0005))
         stats.wall_s = time.perf_counter() - t0
         for r in requests:
             stats.n += 1
@@ -185,6 +234,9 @@ class ServingEngine:
 
     def close(self):
         self.pool.shutdown(wait=True)
+        if self.native is not None:
+            self.native.close()
+            self.native = None
 
 
 def run_sequential(requests, mu, device=None, t0=None):

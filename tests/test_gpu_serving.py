@@ -31,6 +31,24 @@ def test_served_results_equal_alone(gpu, budget):
         assert r.done >= r.admitted
 
 
+def test_slot_level_served_results_equal_alone(gpu):
+    """Lane-level continuous batching (manifold and synodic requests in the
+    native server's slot pools, entering as slots free up): every result is
+    bit-identical to the request solved alone."""
+    from hiten_gb300 import serving
+    mu = W.MU_EM
+    reqs = serving.poisson_requests(200.0, 0.25, mu, seed=7, size_scale=0.05)
+    assert len({r.kind for r in reqs}) == 3
+    eng = serving.ServingEngine(mu, max_concurrent=4, slots=True, pool_slots=4096)
+    stats = eng.serve(reqs)
+    eng.close()
+    assert stats.n == len(reqs)
+    for r in reqs:
+        alone = serving._solve(r.kind, r.payload, mu, None)
+        _same(r.result, alone)
+        assert r.done >= r.admitted
+
+
 def test_sequential_plain_form(gpu):
     from hiten_gb300 import serving
     mu = W.MU_EM
