@@ -12,9 +12,12 @@
 //      steps (the library's DOP853 kernel in list mode; its lane layout chosen
 //      from the live count, as the scheduled driver does), then the saved
 //      crossings are refined;
-//   3. collection: a kernel gathers the slots that finished into one staging
-//      block; one copy brings them back; their requests receive the rows and
-//      the slots are free for the next admission.
+//   3. collection: a kernel gathers the result rows of the slots that
+//      finished straight into pinned host staging (mapped into the device's
+//      address space; two halves used in turn), the live and finished counts
+//      follow in one 16-byte copy, and the thread synchronizes once per
+//      segment.  The finished slots are free for the next admission at once;
+//      their rows are copied into the requests while the next segment runs.
 // So a request arriving while others run is admitted at the next segment
 // boundary as slots free up, and its work overlaps theirs on the device.
 // Trajectories never interact and a paused trajectory resumes with every
@@ -130,10 +133,12 @@ struct RowShape {
 struct PoolLayout {
   long long dev_bytes = 0, stg_bytes = 0;
   // device offsets
-  long long y0, y_end, t_end, hit_t, hit_y, wh, wep, wpp, wq, na, nr, nh, st, list0, list1, cnt, fin, out_d, out_i,
-      stage_y0, stage_slots, refine;
-  // staging offsets (pinned)
-  long long s_y0, s_slots, s_cnt, s_fin, s_out_d, s_out_i;
+  long long y0, y_end, t_end, hit_t, hit_y, wh, wep, wpp, wq, na, nr, nh, st, list0, list1, cnt, stage_y0,
+      stage_slots, refine;
+  // staging offsets (pinned): admission inputs, then two halves of counts and
+  // finished rows (a segment's collection writes one while the rows of the
+  // segment before are delivered from the other)
+  long long s_y0, s_slots, s_cnt[2], s_fin[2], s_out_d[2], s_out_i[2];
   PoolLayout(int C, int dim, int hits) {
     const RowShape rs{dim, hits};
     const long long c = C;
@@ -157,9 +162,6 @@ struct PoolLayout {
     D(list0, 4 * c);
     D(list1, 4 * c);
     D(cnt, 64);
-    D(fin, 4 * c);
-    D(out_d, 8LL * rs.nd() * c);
-    D(out_i, 4LL * RowShape::ni * c);
     D(stage_y0, 8 * dim * c);
     D(stage_slots, 4 * c);
     const long long recs = c * std::max(hits, 1);
@@ -170,10 +172,12 @@ struct PoolLayout {
     };
     S(s_y0, 8 * dim * c);
     S(s_slots, 4 * c);
-    S(s_cnt, 64);
-    S(s_fin, 4 * c);
-    S(s_out_d, 8LL * rs.nd() * c);
-    S(s_out_i, 4LL * RowShape::ni * c);
+    for (int h = 0; h < 2; ++h) {
+      S(s_cnt[h], 64);
+      S(s_fin[h], 4 * c);
+      S(s_out_d[h], 8LL * rs.nd() * c);
+      S(s_out_i[h], 4LL * RowShape::ni * c);
+    }
   }
 };
 
@@ -191,7 +195,8 @@ __global__ void admit_kernel(int n, int C, int dim, const double* stage, const i
 }
 
 // Slots of the last segment's list that finished: their result rows,
-// gathered (fin[k] = slot of row k; *n_fin rows).
+// gathered (fin[k] = slot of row k; *n_fin rows).  fin, out_d and out_i are
+// the device addresses of pinned host staging.
 __global__ void collect_kernel(int C, int dim, int hits, const int* list, const int* n_in, const double* y_end,
                                const double* t_end, const double* hit_t, const double* hit_y, const int* na,
                                const int* nr, const int* nh, const int* st, int* fin, int* n_fin, double* out_d,
@@ -286,6 +291,9 @@ struct Pool {
   long long dev_off = -1, dev_len = 0, stg_off = -1, stg_len = 0;
   std::vector<int> free_slots;
   std::vector<std::pair<std::shared_ptr<Request>, int>> owner;  // per slot: request, trajectory index
+  // rows gathered from finished slots (slots already free), not yet copied
+  // into their requests: request, trajectory index, in row order
+  std::vector<std::pair<std::shared_ptr<Request>, int>> held;
   std::thread runner;
   std::atomic<int> finished{0};
   int rc = HG_OK;
@@ -305,6 +313,7 @@ struct hg_server {
   long long next_id = 1;
   char* dev_base = nullptr;
   char* stg_base = nullptr;
+  char* stg_dev = nullptr;  // the staging arena's device address (mapped pinned memory)
   Arena dev_arena, stg_arena;
   bool stop = false;
   std::thread worker;
@@ -348,11 +357,11 @@ struct hg_server {
     if (cudaSetDevice(cfg.device) != cudaSuccess) return HG_ERR_CUDA;
     char* dv = dev_base + P.dev_off;
     char* sg = stg_base + P.stg_off;
+    char* sd = stg_dev + P.stg_off;  // the same staging block, as the device addresses it
     double* y0 = (double*)(dv + L.y0);
     int* status = (int*)(dv + L.st);
     int* lists[2] = {(int*)(dv + L.list0), (int*)(dv + L.list1)};
     int* cnt = (int*)(dv + L.cnt);  // [0], [1] counts of the two live lists, [2] finished rows
-    int* s_cnt = (int*)(sg + L.s_cnt);
     hg::DopParams p;
     memset(&p, 0, sizeof(p));
     p.N = C;
@@ -398,7 +407,7 @@ struct hg_server {
     p.ws_err_prev = (double*)(dv + L.wep);
     p.ws_prev_pow = (double*)(dv + L.wpp);
     p.ws_q = (int*)(dv + L.wq);
-    int live = 0, a = 0;
+    int live = 0, a = 0, h = 0;
     std::vector<int> slots;
     std::vector<std::pair<std::shared_ptr<Request>, int>> who;
     for (;;) {
@@ -407,9 +416,10 @@ struct hg_server {
       {
         std::lock_guard<std::mutex> g(mu);
         take_admissions(P, slots, who);
-        if (live == 0 && slots.empty()) return HG_OK;  // no work left for this problem
       }
       const int n_new = (int)slots.size();
+      const bool run_seg = live + n_new > 0;
+      const int b = a ^ 1;
       if (n_new > 0) {
         double* stg_y0 = (double*)(sg + L.s_y0);
         int* stg_slots = (int*)(sg + L.s_slots);
@@ -427,92 +437,105 @@ struct hg_server {
         if (cudaGetLastError() != cudaSuccess) return HG_ERR_CUDA;
         live += n_new;
       }
-      // one segment over the live list, then the crossings it saved
-      const int b = a ^ 1;
-      if (cudaMemsetAsync(cnt + b, 0, sizeof(int), s) != cudaSuccess ||
-          cudaMemsetAsync(cnt + 2, 0, sizeof(int), s) != cudaSuccess)
-        return HG_ERR_CUDA;
-      if (k.has_ev && cudaMemsetAsync(p.refine_count, 0, sizeof(int), s) != cudaSuccess) return HG_ERR_CUDA;
-      p.active_in = lists[a];
-      p.n_in = cnt + a;
-      p.active_out = lists[b];
-      p.n_out = cnt + b;
-      const int g = lanes_for(d, live, sms);
-      cudaError_t e;
-      if (d == 6)
-        e = g == 6 ? segment<6>(p, live, sms, s) : (g == 2 ? segment<2>(p, live, sms, s) : segment<1>(p, live, sms, s));
-      else
-        e = g == 14 ? segment<14>(p, live, sms, s) : segment<7>(p, live, sms, s);
-      if (e == cudaSuccess && k.has_ev) e = d == 6 ? refine<1>(p, sms, s) : refine<7>(p, sms, s);
-      if (e != cudaSuccess) return HG_ERR_CUDA;
-      // finished slots of this segment's list: rows gathered and brought back
-      {
+      if (run_seg) {
+        // one segment over the live list, then the crossings it saved
+        if (cudaMemsetAsync(cnt + b, 0, sizeof(int), s) != cudaSuccess ||
+            cudaMemsetAsync(cnt + 2, 0, sizeof(int), s) != cudaSuccess)
+          return HG_ERR_CUDA;
+        if (k.has_ev && cudaMemsetAsync(p.refine_count, 0, sizeof(int), s) != cudaSuccess) return HG_ERR_CUDA;
+        p.active_in = lists[a];
+        p.n_in = cnt + a;
+        p.active_out = lists[b];
+        p.n_out = cnt + b;
+        const int g = lanes_for(d, live, sms);
+        cudaError_t e;
+        if (d == 6)
+          e = g == 6 ? segment<6>(p, live, sms, s)
+                     : (g == 2 ? segment<2>(p, live, sms, s) : segment<1>(p, live, sms, s));
+        else
+          e = g == 14 ? segment<14>(p, live, sms, s) : segment<7>(p, live, sms, s);
+        if (e == cudaSuccess && k.has_ev) e = d == 6 ? refine<1>(p, sms, s) : refine<7>(p, sms, s);
+        if (e != cudaSuccess) return HG_ERR_CUDA;
+        // finished slots of this segment's list: rows gathered into staging half h
         const int blocks = std::min((live + 255) / 256, 1024);
         collect_kernel<<<blocks, 256, 0, s>>>(C, d, H, lists[a], cnt + a, p.y_end, p.t_end, p.hit_t, p.hit_y,
                                               p.n_accept, p.n_reject, (const int*)(dv + L.nh), status,
-                                              (int*)(dv + L.fin), cnt + 2, (double*)(dv + L.out_d),
-                                              (int*)(dv + L.out_i));
-        if (cudaGetLastError() != cudaSuccess) return HG_ERR_CUDA;
-      }
-      if (cudaMemcpyAsync(s_cnt, cnt, 16, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-          cudaStreamSynchronize(s) != cudaSuccess)
-        return HG_ERR_CUDA;
-      const int n_fin = s_cnt[2];
-      const int next_live = s_cnt[b];
-      if (n_fin > 0) {
-        if (cudaMemcpyAsync(sg + L.s_fin, dv + L.fin, 4ull * n_fin, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-            cudaMemcpyAsync(sg + L.s_out_d, dv + L.out_d, 8ull * rs.nd() * n_fin, cudaMemcpyDeviceToHost, s) !=
-                cudaSuccess ||
-            cudaMemcpyAsync(sg + L.s_out_i, dv + L.out_i, 4ull * RowShape::ni * n_fin, cudaMemcpyDeviceToHost, s) !=
-                cudaSuccess ||
-            cudaStreamSynchronize(s) != cudaSuccess)
+                                              (int*)(sd + L.s_fin[h]), cnt + 2, (double*)(sd + L.s_out_d[h]),
+                                              (int*)(sd + L.s_out_i[h]));
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(sg + L.s_cnt[h], cnt, 16, cudaMemcpyDeviceToHost, s) != cudaSuccess)
           return HG_ERR_CUDA;
       }
+      // the rows of the segment before (staging half h ^ 1) go to their
+      // requests while this one runs
+      deliver(P, rs, (const double*)(sg + L.s_out_d[h ^ 1]), (const int*)(sg + L.s_out_i[h ^ 1]));
+      if (!run_seg) return HG_OK;  // no trajectory live or waiting for this problem
+      if (cudaStreamSynchronize(s) != cudaSuccess) return HG_ERR_CUDA;
+      const int* sc = (const int*)(sg + L.s_cnt[h]);
+      const int n_fin = sc[2];
+      const int next_live = sc[b];
       {
         std::lock_guard<std::mutex> g(mu);
         ++segments;
-        const int* fin = (const int*)(sg + L.s_fin);
-        const double* od = (const double*)(sg + L.s_out_d);
-        const int* oi = (const int*)(sg + L.s_out_i);
-        const auto now = Clock::now();
+        const int* fin = (const int*)(sg + L.s_fin[h]);
         for (int q = 0; q < n_fin; ++q) {
           const int sl = fin[q];
-          auto own = P.owner[sl];
-          P.owner[sl].first.reset();
+          P.held.push_back(std::move(P.owner[sl]));
+          P.owner[sl] = {};
           P.free_slots.push_back(sl);
-          Request& r = *own.first;
-          const int i = own.second;
-          const double* row = od + (long long)q * rs.nd();
-          for (int c = 0; c < d; ++c) r.y_end[(size_t)i * d + c] = row[c];
-          r.t_end[i] = row[d];
-          for (int j = 0; j < H; ++j) {
-            r.hit_t[(size_t)i * H + j] = row[d + 1 + j];
-            for (int c = 0; c < d; ++c) r.hit_y[((size_t)i * H + j) * d + c] = row[d + 1 + H + j * d + c];
-          }
-          const int* ri = oi + (long long)q * RowShape::ni;
-          r.n_acc[i] = ri[0];
-          r.n_rej[i] = ri[1];
-          r.n_hits[i] = ri[2];
-          r.status[i] = ri[3];
-          if (++r.done == r.n) {
-            r.state = 2;
-            r.finished = now;
-            latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r.submitted).count());
-          }
         }
       }
-      if (n_fin > 0) cv.notify_all();
       live = next_live;
       a = b;
+      h ^= 1;
     }
+  }
+
+  // Copies the held rows (in row order, from the staging half `od` / `oi`)
+  // into their requests, then marks the requests they complete.  Only the
+  // pool's thread writes a request's result arrays, and fetch reads them
+  // only after the state turns 2 under the lock.
+  void deliver(Pool& P, const RowShape& rs, const double* od, const int* oi) {
+    if (P.held.empty()) return;
+    const int d = rs.dim, H = rs.hits;
+    for (size_t q = 0; q < P.held.size(); ++q) {
+      Request& r = *P.held[q].first;
+      const int i = P.held[q].second;
+      const double* row = od + (long long)q * rs.nd();
+      for (int c = 0; c < d; ++c) r.y_end[(size_t)i * d + c] = row[c];
+      r.t_end[i] = row[d];
+      for (int j = 0; j < H; ++j) {
+        r.hit_t[(size_t)i * H + j] = row[d + 1 + j];
+        for (int c = 0; c < d; ++c) r.hit_y[((size_t)i * H + j) * d + c] = row[d + 1 + H + j * d + c];
+      }
+      const int* ri = oi + (long long)q * RowShape::ni;
+      r.n_acc[i] = ri[0];
+      r.n_rej[i] = ri[1];
+      r.n_hits[i] = ri[2];
+      r.status[i] = ri[3];
+    }
+    {
+      std::lock_guard<std::mutex> g(mu);
+      const auto now = Clock::now();
+      for (auto& hq : P.held) {
+        Request& r = *hq.first;
+        if (++r.done == r.n) {
+          r.state = 2;
+          r.finished = now;
+          latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r.submitted).count());
+        }
+      }
+      P.held.clear();
+    }
+    cv.notify_all();
   }
 
   // A pool that failed (lock held): the requests it holds, and those of its
   // problem still waiting, fail.
   void fail_pool(Pool& P, int rc) {
     const auto now = Clock::now();
-    for (auto& o : P.owner) {
-      if (!o.first) continue;
+    auto fail = [&](std::pair<std::shared_ptr<Request>, int>& o) {
+      if (!o.first) return;
       Request& r = *o.first;
       if (r.state < 2) {
         r.state = 3;
@@ -520,7 +543,10 @@ struct hg_server {
         r.finished = now;
       }
       o.first.reset();
-    }
+    };
+    for (auto& o : P.owner) fail(o);
+    for (auto& o : P.held) fail(o);
+    P.held.clear();
     for (auto& r : pending)
       if (same_key(r->key, P.key) && r->state < 2) {
         r->state = 3;
@@ -632,8 +658,8 @@ void hg_serve_config_default(hg_serve_config* c) {
   c->hbm_budget_bytes = 8LL << 30;
   c->max_concurrent = 4;
   c->staging_bytes = 1LL << 30;
-  c->pool_slots = 16384;
-  c->seg_steps = 32;
+  c->pool_slots = 32768;
+  c->seg_steps = 16;
 }
 
 int hg_serve_create(const hg_serve_config* cfg, hg_server** out) {
@@ -662,8 +688,13 @@ int hg_serve_create(const hg_serve_config* cfg, hg_server** out) {
     cudaGetLastError();
     return release(HG_ERR_CUDA);
   }
-  if (cudaHostAlloc(&s->stg_base, (size_t)c.staging_bytes, cudaHostAllocDefault) != cudaSuccess) {
+  if (cudaHostAlloc(&s->stg_base, (size_t)c.staging_bytes, cudaHostAllocMapped) != cudaSuccess) {
     s->stg_base = nullptr;
+    cudaGetLastError();
+    return release(HG_ERR_CUDA);
+  }
+  // the collection kernel writes finished rows straight into the staging
+  if (cudaHostGetDevicePointer((void**)&s->stg_dev, s->stg_base, 0) != cudaSuccess) {
     cudaGetLastError();
     return release(HG_ERR_CUDA);
   }

@@ -156,7 +156,7 @@ class ServingEngine:
     batches."""
 
     def __init__(self, mu, device=None, hbm_budget_bytes=8 << 30, max_concurrent=6, tick_s=0.002, slots=False,
-                 pool_slots=16384, seg_steps=32):
+                 pool_slots=32768, seg_steps=16):
         self.mu = float(mu)
         self.device = P._device(device)
         self.budget = int(hbm_budget_bytes)
@@ -298,8 +298,8 @@ class NativeServer:
     gets a pool of device-resident slots that waiting requests enter as slots
     free up, segment by segment; results equal direct calls."""
 
-    def __init__(self, device=0, hbm_budget_bytes=8 << 30, max_concurrent=4, staging_bytes=None, pool_slots=16384,
-                 seg_steps=32):
+    def __init__(self, device=0, hbm_budget_bytes=8 << 30, max_concurrent=4, staging_bytes=None, pool_slots=32768,
+                 seg_steps=16):
         import ctypes as C
         from . import _lib
         self._C, self._lib = C, _lib

@@ -331,9 +331,12 @@ int hg_correct_halo_graph(hg_handle* h, double mu, int N, double* x, long long l
  * over several rounds), advances every live slot by seg_steps attempted
  * steps, refines the crossings saved, and returns the trajectories that
  * finished to their requests, freeing their slots: a request arriving while
- * others run enters at the next segment boundary, as slots free up.
- * hg_serve_create allocates a device arena of hbm_budget_bytes and a pinned
- * host arena of staging_bytes that the pools are carved from; nothing is
+ * others run enters at the next segment boundary, as slots free up.  One
+ * host synchronization per segment: finished rows are gathered straight into
+ * the pinned staging (mapped into the device's address space) and copied into
+ * their requests while the next segment runs.
+ * hg_serve_create allocates a device arena of hbm_budget_bytes and a pinned,
+ * mapped host arena of staging_bytes that the pools are carved from; nothing is
  * allocated afterwards, and a request whose problem cannot get even a
  * 32-slot pool on an idle server fails (state 3, HG_ERR_ARGS).  Results equal
  * a direct hg_propagate_dop853 call on the request alone.  Requests: y0 host
@@ -351,8 +354,8 @@ typedef struct hg_serve_config {
   long long hbm_budget_bytes; /* device arena (default 8 GiB) */
   int max_concurrent;         /* pools (problems) in flight (default 4) */
   long long staging_bytes;    /* pinned host arena (default 1 GiB) */
-  int pool_slots;             /* trajectory slots of a pool (default 16384, >= 32) */
-  int seg_steps;              /* attempted steps per segment (default 32) */
+  int pool_slots;             /* trajectory slots of a pool (default 32768, >= 32) */
+  int seg_steps;              /* attempted steps per segment (default 16) */
 } hg_serve_config;
 void hg_serve_config_default(hg_serve_config* c);
 int hg_serve_create(const hg_serve_config* cfg, hg_server** out);

@@ -106,7 +106,7 @@ def test_native_server_host_checks(L):
     c = _lib.hg_serve_config()
     L.hg_serve_config_default(C.byref(c))
     assert (c.device, c.hbm_budget_bytes, c.max_concurrent, c.staging_bytes, c.pool_slots, c.seg_steps) == \
-        (0, 8 << 30, 4, 1 << 30, 16384, 32)
+        (0, 8 << 30, 4, 1 << 30, 32768, 16)
     out = C.c_void_p(123)
     assert L.hg_serve_create(C.byref(c), None) == _lib.HG_ERR_ARGS
     for field, bad in (("max_concurrent", 0), ("max_concurrent", 65), ("hbm_budget_bytes", 0), ("staging_bytes", 0),
