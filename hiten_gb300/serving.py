@@ -12,10 +12,17 @@ Requests arrive at any time.  Every scheduler tick the engine:
 3. collects finished batches, splits the results back per request, releases
    their memory and stamps the completion time.
 
+With ``slots=True`` the propagating kinds (manifold, synodic) go instead to
+the library's native request server (``NativeServer`` over ``hg_serve_*``):
+each problem runs in a pool of device-resident trajectory slots, and the
+trajectories of a request that arrives while others run enter the pool at
+the next segment boundary as slots free up (lane-level admission; one host
+synchronisation per segment).  Corrections keep the merged batches.
+
 Trajectories are independent lanes in every kernel, so a request's result
 does not depend on what it was batched with (checked bit for bit by
-tests/test_gpu_serving.py).  `run_sequential` is the plain form: one request
-at a time, each with its own kernel calls, on one stream.
+tests/test_gpu_serving.py in both forms).  `run_sequential` is the plain
+form: one request at a time, each with its own kernel calls, on one stream.
 
 Request kinds (types/services: manifold.py:293-442, orbits.py:114-151;
 poincare/synodic): 'manifold' (seeds, DOP853 1e-12 backward to t = -8 or the
