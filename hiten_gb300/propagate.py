@@ -237,6 +237,92 @@ def propagate_dop853(y0, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min
     return res
 
 
+class Dop853Batch:
+    """One DOP853 call shape prepared once, for repeated batches: N states of
+    dimension `dim` with the same span, options and event.  The SoA input,
+    the outputs and the scheduled driver's workspace are allocated here; each
+    `run(y0)` copies the new states in (one transpose copy), resets the hit
+    arrays to NaN (one fill: they share one buffer), and calls the library --
+    the host work of `propagate_dop853` (argument handling, allocations, size
+    queries, result views) is done once.  Results are the same bits as
+    `propagate_dop853` with the same arguments; `run` returns one
+    Dop853Result whose tensors are views of the batch's buffers, valid until
+    the next `run`.  Scalar t0 / tmax; no dense samples."""
+
+    def __init__(self, n, dim, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min_step=None,
+                 max_steps=100_000, fwd=1, flip=None, event=None, scheduled=None, device=None):
+        if np.ndim(t0) != 0 or np.ndim(tmax) != 0:
+            raise ValueError("a prepared batch takes scalar t0 and tmax")
+        self.dev = _device(device)
+        if self.dev.index is None:
+            self.dev = torch.device("cuda", torch.cuda.current_device())
+        self.n, self.dim = int(n), int(dim)
+        if self.n < 1:
+            raise ValueError("a prepared batch needs at least one state")
+        self.scheduled = ((self.dim == 6 and self.n >= SCHEDULE_MIN) if scheduled is None else bool(scheduled))
+        n, d, ld, dev = self.n, self.dim, self.n, self.dev
+        f64 = dict(dtype=torch.float64, device=dev)
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.Y0 = torch.empty((d, ld), **f64)
+        self.y_end = torch.empty((d, ld), **f64)
+        self.t_end = torch.empty(ld, **f64)
+        self.n_acc = torch.empty(ld, **i32)
+        self.n_rej = torch.empty(ld, **i32)
+        self.status = torch.empty(ld, **i32)
+        lo, hi = _flip(d, fwd, flip)
+        self.opts = _lib.hg_dop853_opts(float(rtol), float(atol), float(max_step),
+                                        float(10.0 * EPS if min_step is None else min_step), int(max_steps),
+                                        int(fwd), lo, hi)
+        self.evp = None
+        self.hits = None
+        mh = 0
+        if event is not None:
+            mh = int(event.max_hits)
+            self.evp = _lib.hg_event(int(event.index), float(event.offset), int(event.direction), mh,
+                                     float(event.xtol), float(event.gtol))
+            self.hits = torch.empty(mh * ld * (1 + d), **f64)  # hit_t then hit_y, one fill per run
+            hit_t = self.hits[:mh * ld].view(mh, ld)
+            hit_y = self.hits[mh * ld:].view(mh, d, ld)
+            self.n_hits = torch.empty(ld, **i32)
+        self.H = _lib.handle(dev.index or 0)
+        self.ws_bytes = int(self.H.lib.hg_dop853_segmented_workspace_bytes(n, d, mh)) if self.scheduled else 0
+        self.ws = torch.empty(max(self.ws_bytes, 1), dtype=torch.uint8, device=dev) if self.scheduled else None
+        self.args = (self.H.ptr, float(mu), d, n, _ptr(self.Y0), ld, None, None, float(t0), float(tmax),
+                     C.byref(self.opts), C.byref(self.evp) if self.evp is not None else None, 0, 0, None,
+                     _ptr(self.y_end), _ptr(self.t_end), _ptr(hit_t) if mh else None,
+                     _ptr(hit_y) if mh else None, _ptr(self.n_hits) if mh else None, _ptr(self.n_acc),
+                     _ptr(self.n_rej), _ptr(self.status))
+        self.result = Dop853Result(y_end=self.y_end.t(), t_end=self.t_end, n_accept=self.n_acc,
+                                   n_reject=self.n_rej, status=self.status)
+        if mh:
+            self.result.hit_t = hit_t.t()
+            self.result.hit_y = hit_y.permute(2, 0, 1)
+            self.result.n_hits = self.n_hits
+
+    def run(self, y0):
+        """Propagate the (N, dim) states `y0` (a CUDA tensor on the batch's
+        device, or anything torch.as_tensor takes)."""
+        y = torch.as_tensor(y0, dtype=torch.float64)
+        if tuple(y.shape) != (self.n, self.dim):
+            raise ValueError(f"prepared for shape ({self.n}, {self.dim}), got {tuple(y.shape)}")
+        self.Y0.copy_(y.t())
+        if self.hits is not None:
+            self.hits.fill_(float("nan"))
+        if torch.cuda.current_device() != self.dev.index:
+            with torch.cuda.device(self.dev):
+                self._call()
+        else:
+            self._call()
+        return self.result
+
+    def _call(self):
+        st = _stream(self.dev)
+        if self.scheduled:
+            self.H.check(self.H.lib.hg_propagate_dop853_scheduled(*self.args, _ptr(self.ws), self.ws_bytes, st))
+        else:
+            self.H.check(self.H.lib.hg_propagate_dop853(*self.args, st))
+
+
 def fp64_peak_tflops(device=None):
     """Measured FP64 FMA throughput of the device (TFLOP/s)."""
     dev = _device(device)
