@@ -17,9 +17,10 @@ Metric: accepted trajectory-steps per second (attempted steps reported
 beside it).  `value`: throughput with the seeds resident in HBM, each step
 one run of the call prepared once (propagate.Dop853Batch: static input,
 output and workspace buffers; checked bit-identical to propagate_dop853);
-`e2e`: the same through the reference-shaped public API
-(hiten_gb300.manifold.propagate_to_plane, a full per-call setup) from pinned
-host seeds, H2D and D2H copies inside the timed region.  `gpu_launches`:
+`e2e`: the same prepared call from pinned host seeds, H2D and D2H copies
+inside the timed region (wall clock); `e2e.dropin` the same through the
+reference-shaped public API (hiten_gb300.manifold.propagate_to_plane, a full
+per-call setup).  `gpu_launches`:
 kernels launched in the timed region, read from the library's counter.
 
 `secondary`: the other BASELINE configs measured in the same run after the
@@ -828,27 +829,35 @@ def main():
     host_seeds = torch.as_tensor(seeds).pin_memory()
     h2d = host_seeds.numel() * 8
 
-    def e2e_step():
-        r = M.propagate_to_plane(host_seeds, mu, tf=TF, forward=-1, device=dev, scheduled=sched)
+    def fetch(r):
         y_end = r.y_end.cpu()
         hit_y = r.hit_y.cpu()
         hit_t = r.hit_t.cpu()
         n_acc = r.n_accept.cpu()
         return int(n_acc.sum()), (y_end.numel() + hit_y.numel() + hit_t.numel()) * 8 + n_acc.numel() * 4
 
-    for _ in range(max(args.warmup, 3)):  # untimed, like the device-resident steps
-        e2e_step()
-    e2e_acc = 0
-    d2h = 0
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    for i in range(args.steps):
-        n, d2h = e2e_step()
-        e2e_acc += n
-    torch.cuda.synchronize(dev)
-    e2e_value, e2e_s = whole_job_rate(e2e_acc, time.perf_counter() - t0, device=dev)
+    def e2e_step():  # the prepared call (the timed steps' API) from pinned host memory
+        return fetch(batch.run(host_seeds))
+
+    def e2e_dropin_step():  # the reference-shaped per-call API
+        return fetch(M.propagate_to_plane(host_seeds, mu, tf=TF, forward=-1, device=dev, scheduled=sched))
+
+    def e2e_rate(step):
+        for _ in range(max(args.warmup, 3)):  # untimed, like the device-resident steps
+            step()
+        acc_, d2h_ = 0, 0
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            n, d2h_ = step()
+            acc_ += n
+        torch.cuda.synchronize(dev)
+        return whole_job_rate(acc_, time.perf_counter() - t0, device=dev)[0], d2h_
+
+    e2e_value, d2h = e2e_rate(e2e_step)
+    e2e_dropin_value, _ = e2e_rate(e2e_dropin_step)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -920,7 +929,10 @@ def main():
                             "flops_per_attempted_step": FLOPS_PER_ATTEMPT_D6,
                             "dominant_launch": dom_info, "step_achieved": step_achieved,
                             "fp64_pipe": pipe},
-               "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+               "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "api": "propagate.Dop853Batch.run from pinned host seeds (the timed steps' prepared call)",
+                       "dropin": {"value": e2e_dropin_value, "unit": UNIT,
+                                  "api": "manifold.propagate_to_plane from pinned host seeds (per-call setup)"}},
                "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
                "plan": {"chosen": autotune.plan_name(plan), "autotune_ms": plan_ms},
                "plain_gpu": {"value": plain_value, "unit": UNIT,

@@ -264,6 +264,7 @@ class Dop853Batch:
         f64 = dict(dtype=torch.float64, device=dev)
         i32 = dict(dtype=torch.int32, device=dev)
         self.Y0 = torch.empty((d, ld), **f64)
+        self.stage = None  # (N, dim) device copy of host inputs, made on the first host run
         self.y_end = torch.empty((d, ld), **f64)
         self.t_end = torch.empty(ld, **f64)
         self.n_acc = torch.empty(ld, **i32)
@@ -305,6 +306,12 @@ class Dop853Batch:
         y = torch.as_tensor(y0, dtype=torch.float64)
         if tuple(y.shape) != (self.n, self.dim):
             raise ValueError(f"prepared for shape ({self.n}, {self.dim}), got {tuple(y.shape)}")
+        if y.device != self.dev:
+            # host states: one contiguous copy (asynchronous from pinned memory), then the transpose on the device
+            if self.stage is None:
+                self.stage = torch.empty((self.n, self.dim), dtype=torch.float64, device=self.dev)
+            self.stage.copy_(y, non_blocking=bool(y.is_pinned()))
+            y = self.stage
         self.Y0.copy_(y.t())
         if self.hits is not None:
             self.hits.fill_(float("nan"))

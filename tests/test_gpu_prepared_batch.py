@@ -29,3 +29,15 @@ def test_prepared_batch_checks_the_shape(gpu):
     b = gpu.Dop853Batch(10, 6, 0.0, 1.0, MU)
     with pytest.raises(ValueError):
         b.run(np.zeros((11, 6)))
+
+
+def test_prepared_batch_from_pinned_host_states(gpu):
+    """Host input (pinned): the same bits as the device-resident input."""
+    ev = gpu.EventSpec(index=0, offset=1.0 - MU, direction=0, max_hits=1)
+    b = gpu.Dop853Batch(500, 6, 0.0, 3.0, MU, fwd=-1, flip=(0, 6), event=ev)
+    y = W.section_states(500, seed=4)
+    dev = b.run(torch.as_tensor(y, device="cuda"))
+    d = {f: getattr(dev, f).clone() for f in ("y_end", "t_end", "n_accept", "n_hits")}
+    host = b.run(torch.as_tensor(y).pin_memory())
+    for f, v in d.items():
+        assert torch.equal(getattr(host, f), v), f
