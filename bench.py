@@ -119,25 +119,38 @@ def make_seeds(device):
 
 
 class ClockSampler:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region.
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    The sampler is started before the warm-up steps (nvidia-smi's own start-up queries the driver
+    heavily, which delays the host calls of a synchronous driver if it falls inside the timed region);
+    `begin()` / `end()` mark the timed region on the host clock and `summary()` keeps the samples
+    taken inside it (the nearest one on either side as well, so that a short region has samples)."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    INTERVAL_MS = 50
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
+        self.t_begin = self.t_end = None
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
-                                         stderr=subprocess.DEVNULL)
+                                          "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
         return self
+
+    def begin(self):
+        self.t_begin = time.time()
+
+    def end(self):
+        self.t_end = time.time()
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -147,24 +160,41 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
+    @staticmethod
+    def _stamp(text):
+        import datetime
+        for fmt in ("%Y/%m/%d %H:%M:%S.%f", "%Y/%m/%d %H:%M:%S"):
+            try:
+                return datetime.datetime.strptime(text, fmt).timestamp()
+            except ValueError:
+                pass
+        return None
+
     def summary(self):
         self.f.flush()
         self.f.seek(0)
-        sm, mx, reasons = [], [], set()
+        rows = []
         for line in self.f.read().splitlines():
             p = [x.strip() for x in line.split(",")]
-            if len(p) < 9:
+            if len(p) < 10:
                 continue
             try:
-                sm.append(float(p[1]))
-                mx.append(float(p[2]))
+                rows.append((self._stamp(p[0]), float(p[2]), float(p[3]), p[6:10]))
             except ValueError:
                 continue
-            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
-                               p[5:9]):
+        os.unlink(self.f.name)
+        if rows and self.t_begin is not None and self.t_end is not None and all(r[0] is not None for r in rows):
+            inside = [r for r in rows if self.t_begin <= r[0] <= self.t_end]
+            before = [r for r in rows if r[0] < self.t_begin][-1:]
+            after = [r for r in rows if r[0] > self.t_end][:1]
+            rows = before + inside + after
+        sm = [r[1] for r in rows]
+        mx = [r[2] for r in rows]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), r[3]):
                 if v.lower().startswith("active"):
                     reasons.add(name)
-        os.unlink(self.f.name)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
@@ -768,6 +798,9 @@ def main():
     def one_step():
         return batch.run(seeds_dev)
 
+    # the clock sampler starts here, ahead of the warm-up steps, so that its start-up is over before
+    # the timed region; it is stopped after the timed steps
+    clk = ClockSampler(local).__enter__()
     for _ in range(max(args.warmup, 3)):
         one_step()
     torch.cuda.synchronize(dev)
@@ -799,7 +832,8 @@ def main():
         dist.barrier()
     torch.cuda.synchronize(dev)
     launches0 = H.kernel_launches()
-    with ClockSampler(local) as clk:
+    try:
+        clk.begin()
         results = []
         for i in range(args.steps):
             flush.fill_(float(i))
@@ -808,6 +842,9 @@ def main():
             evs[i][1].record(stream)
             results.append(r)
         torch.cuda.synchronize(dev)
+        clk.end()
+    finally:
+        clk.__exit__(None, None, None)
     launches = H.kernel_launches() - launches0
     if world > 1:
         dist.barrier()
@@ -918,6 +955,7 @@ def main():
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(world),
+               "step_ms": {"min": min(times_ms), "median": statistics.median(times_ms), "max": max(times_ms)},
                "attempted_steps_per_s": att_rate,
                "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                             "frac": achieved / peak if peak else None, "traffic": traffic,
