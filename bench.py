@@ -34,6 +34,7 @@ oracle in numba-lowering mode, one trajectory per task, all host threads),
 on a bounded sample of the same seeds.
 """
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -129,7 +130,7 @@ class ClockSampler:
     FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
-    INTERVAL_MS = 50
+    INTERVAL_MS = 200
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
@@ -832,6 +833,8 @@ def main():
         dist.barrier()
     torch.cuda.synchronize(dev)
     launches0 = H.kernel_launches()
+    gc.collect()
+    gc.disable()  # no collector pause inside the host-synchronised steps
     try:
         clk.begin()
         results = []
@@ -844,6 +847,7 @@ def main():
         torch.cuda.synchronize(dev)
         clk.end()
     finally:
+        gc.enable()
         clk.__exit__(None, None, None)
     launches = H.kernel_launches() - launches0
     if world > 1:
@@ -886,12 +890,18 @@ def main():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            n, d2h_ = step()
-            acc_ += n
-        torch.cuda.synchronize(dev)
-        return whole_job_rate(acc_, time.perf_counter() - t0, device=dev)[0], d2h_
+        gc.collect()
+        gc.disable()
+        try:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                n, d2h_ = step()
+                acc_ += n
+            torch.cuda.synchronize(dev)
+            dt = time.perf_counter() - t0
+        finally:
+            gc.enable()
+        return whole_job_rate(acc_, dt, device=dev)[0], d2h_
 
     e2e_value, d2h = e2e_rate(e2e_step)
     e2e_dropin_value, _ = e2e_rate(e2e_dropin_step)

@@ -106,9 +106,12 @@ HG_HD void hg_fast_two_sum(double a, double b, double& s, double& e) {
 // within one ulp of a/b, the remainder r = a - b*q0 is exact with an fma,
 // and RN(q0 + r*rb) = RN(a/b).  Valid for finite, normal operands whose
 // quotient and remainder neither overflow nor underflow -- the CR3BP values
-// on this path (distances 1e-3..1e3) stay far from those limits.  One
-// reciprocal serves every quotient with the same denominator: 3 FP64
-// operations per quotient instead of a full division.
+// on this path (distances 1e-3..1e3) stay far from those limits.  A zero
+// numerator (z = 0 in a planar problem) gives a zero quotient whose sign can
+// differ from IEEE division's (+0 for -0 / b); keeping that sign costs 2-6 %
+// of the propagation kernels' time, so it is not kept.  One reciprocal
+// serves every quotient with the same denominator: 3 FP64 operations per
+// quotient instead of a full division.
 HG_HD double hg_div_rn(double a, double b, double rb) {
   const double q0 = a * rb;
   const double r = fma(-b, q0, a);
