@@ -1247,6 +1247,71 @@ struct DopGroupCoef {
   }
 };
 
+// Row I of the step's coefficients (I < 12: the stage row a_Ij; I = 12: the
+// solution weights b_j), its count of nonzero entries and the column of the
+// k-th of them.
+template <int I>
+__host__ __device__ constexpr double dop_row_coef(int j) {
+  return I < DopTab::S ? DopTab::a(I, j) : DopTab::b(j);
+}
+template <int I>
+__host__ __device__ constexpr int dop_row_nnz() {
+  int n = 0;
+  for (int j = 0; j < (I < DopTab::S ? I : DopTab::S); ++j) n += dop_row_coef<I>(j) != 0.0;
+  return n;
+}
+template <int I>
+__host__ __device__ constexpr int dop_row_col(int k) {
+  for (int j = 0; j < (I < DopTab::S ? I : DopTab::S); ++j)
+    if (dop_row_coef<I>(j) != 0.0 && k-- == 0) return j;
+  return -1;
+}
+
+// Lane pairs (G = 2, one step size per pair): the products h * a_ij, h * b_j
+// formed row by row at the start of each stage, two per FP64 multiply --
+// lane `role` of the pair forms the (2m + role)-th nonzero entry of the row
+// -- and exchanged by shuffle: the same products as DopInlineCoef in about
+// half the multiplies.  `c` holds the current row's products by column.
+struct DopPairCoef {
+  double h;
+  int role;
+  int base;
+  unsigned gmask;
+  mutable double c[DopTab::S];
+  __device__ __forceinline__ void set_step(double hh) { h = hh; }
+  template <int I>
+  __device__ __forceinline__ void row() const {
+    constexpr int n = dop_row_nnz<I>();
+    static_for<(n + 1) / 2>([&](auto mc) {
+      constexpr int m = decltype(mc)::value;
+      constexpr int ja = dop_row_col<I>(2 * m);
+      constexpr int jb = 2 * m + 1 < n ? dop_row_col<I>(2 * m + 1) : -1;
+      constexpr double aa = dop_row_coef<I>(ja);
+      constexpr double ab = jb >= 0 ? dop_row_coef<I>(jb) : aa;
+      const double v = h * (role ? ab : aa);
+      c[ja] = __shfl_sync(gmask, v, base);
+      if constexpr (jb >= 0) c[jb] = __shfl_sync(gmask, v, base + 1);
+    });
+  }
+  template <int I, int J>
+  __device__ __forceinline__ double a() const {
+    return c[J];
+  }
+  template <int J>
+  __device__ __forceinline__ double b() const {
+    return c[J];
+  }
+};
+
+// Row preparation of a coefficient provider: DopPairCoef forms a row's
+// products ahead of its sum; the others form them where they are used.
+template <int I, class CF>
+__device__ __forceinline__ void dop_coef_row(const CF&) {}
+template <int I>
+__device__ __forceinline__ void dop_coef_row(const DopPairCoef& cf) {
+  cf.template row<I>();
+}
+
 template <class LT>
 struct DopLaneT {
   static constexpr int NC = LT::NC;
@@ -1265,6 +1330,7 @@ struct DopLaneT {
     using T = DopTab;
     static_for<T::S - 1>([&](auto ic) {
       constexpr int i = decltype(ic)::value + 1;
+      dop_coef_row<i>(cf);
       double ys[NC];
 #pragma unroll
       for (int d = 0; d < NC; ++d) ys[d] = y[d];
@@ -1278,6 +1344,7 @@ struct DopLaneT {
       });
       L.rhs(ys, mu, dir, k[i]);
     });
+    dop_coef_row<T::S>(cf);
 #pragma unroll
     for (int d = 0; d < NC; ++d) yh[d] = y[d];
     static_for<T::S>([&](auto jc) {
@@ -1399,18 +1466,27 @@ template <int G>
 using DopLane = DopLaneT<Layout<G>>;
 
 // Step-coefficient provider of a layout: spread over the group for the
-// groups of 6 and 14 lanes (few components per lane), formed inline for 1,
-// 2 and 7 (whose lanes have no registers to spare).
+// groups of 6 and 14 lanes (few components per lane), formed row by row in
+// pairs for lane pairs, formed inline for 1 and 7 (whose lanes have no
+// registers to spare).
 template <int G>
 __host__ __device__ constexpr bool dop_spread_coef() {
   return G == 6 || G == 14;
 }
 template <int G>
 __device__ __forceinline__ auto dop_coef(const Layout<G>& L, const double* tab) {
-  if constexpr (dop_spread_coef<G>())
+  if constexpr (dop_spread_coef<G>()) {
     return DopGroupCoef<G>(tab, L.role, L.base, L.gmask);
-  else
+  } else if constexpr (G == 2) {
+    DopPairCoef cf;
+    cf.h = 0.0;
+    cf.role = L.role;
+    cf.base = L.base;
+    cf.gmask = L.gmask;
+    return cf;
+  } else {
     return DopInlineCoef{0.0};
+  }
 }
 
 // Lane -> (group, role) for one launch; false for the idle lanes of a warp.
