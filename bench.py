@@ -87,7 +87,7 @@ def dominant_launch(run_segment, plan, n, sm_count, stream, reps=3):
     import torch
     if not plan.get("scheduled"):
         return None
-    g = sched_lanes(n, plan.get("sm_capacity", 3.0) * sm_count)
+    g = plan.get("lanes_d6") or sched_lanes(n, plan.get("sm_capacity", 3.0) * sm_count)
     seg = int(plan.get("seg_steps", 16))
     run_segment(g, seg)  # warm
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

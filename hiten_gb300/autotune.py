@@ -35,6 +35,8 @@ DOP853_PLANS = (
     {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 32, "sm_capacity": 4.5},
     {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 48, "sm_capacity": 4.5},
     {"scheduled": True, "lanes_d6": 0, "block": 32, "spread": 0, "seg_steps": 64, "sm_capacity": 4.5},
+    {"scheduled": True, "lanes_d6": 2, "block": 32, "spread": 0, "seg_steps": 16},
+    {"scheduled": True, "lanes_d6": 2, "block": 32, "spread": 0, "seg_steps": 32},
 )
 _plan_cache = {}
 
@@ -68,7 +70,8 @@ def tune_dop853(key, run, plans=DOP853_PLANS, reps=2, device=None):
 def plan_name(plan):
     if plan["scheduled"]:
         cap = f"_cap{plan['sm_capacity']:g}" if "sm_capacity" in plan else ""
-        return f"scheduled_seg{plan.get('seg_steps', 16)}{cap}"
+        lanes = f"_lanes{plan['lanes_d6']}" if plan.get("lanes_d6") else ""
+        return f"scheduled_seg{plan.get('seg_steps', 16)}{cap}{lanes}"
     return f"lanes{plan['lanes_d6']}_block{plan['block']}" + ("_spread" if plan.get("spread") else "")
 
 
