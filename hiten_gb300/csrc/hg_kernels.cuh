@@ -366,7 +366,8 @@ struct Layout<14> {
 // role 0 holds the position (x, y, z), role 1 the velocity.  The right-hand
 // side splits by primary: role 0 evaluates the terms of the first primary,
 // role 1 those of the second, with one instruction stream and per-lane
-// constants, and the pair exchanges the three quotients.  Every operation
+// constants; the pair exchanges quotients and then splits the accelerations
+// the same way (role 0 forms ax, role 1 ay).  Every operation
 // is the one rhs6 performs (x - (1-mu) == x + (-(1-mu)), x - 1 == x + (-1)),
 // so the result is bit-identical; the per-step FP64 critical path is about
 // half that of G = 1, at ~7% more total work.
@@ -403,15 +404,19 @@ struct Layout<2> {
     const double qx = hg_div_rn(mb * ((x + a1) + a2), rc, ir);
     const double qy = hg_div_rn(mb * y, rc, ir);
     const double qz = hg_div_rn(mz * z, rc, ir);
-    const double px = __shfl_xor_sync(gmask, qx, 1);
-    const double py = __shfl_xor_sync(gmask, qy, 1);
+    // The accelerations ((2 vy + x) - q1x) - q2x and ((-2 vx + y) - q1y) - q2y
+    // (q1 the first primary's quotient, role 0's; q2 the second's, role 1's)
+    // in one instruction stream: role 0 forms ax, role 1 ay, and role 1
+    // takes ax from its partner; az = q1z - q2z on role 1.
+    const double p = __shfl_xor_sync(gmask, r0 ? qy : qx, 1);  // role 0: the second qx; role 1: the first qy
     const double pz = __shfl_xor_sync(gmask, qz, 1);
-    // role 1 owns the accelerations: q1 = partner (first primary), q2 = own
-    const double ax = ((2.0 * vy + x) - px) - qx;
-    const double ay = ((-2.0 * vx + y) - py) - qy;
+    const double q1 = r0 ? qx : p;
+    const double q2 = r0 ? p : qy;
+    const double acc = (((r0 ? 2.0 : -2.0) * (r0 ? vy : vx) + (r0 ? x : y)) - q1) - q2;
+    const double ax = __shfl_xor_sync(gmask, acc, 1);
     const double az = pz - qz;
     dv[0] = r0 ? vx : ax;
-    dv[1] = r0 ? vy : ay;
+    dv[1] = r0 ? vy : acc;
     dv[2] = r0 ? vz : az;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
