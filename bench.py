@@ -799,18 +799,6 @@ def main():
     def one_step():
         return batch.run(seeds_dev)
 
-    # the clock sampler starts here, ahead of the warm-up steps, so that its start-up is over before
-    # the timed region; it is stopped after the timed steps
-    clk = ClockSampler(local).__enter__()
-    for _ in range(max(args.warmup, 3)):
-        one_step()
-    torch.cuda.synchronize(dev)
-    _ref = run(sched)
-    _got = one_step()
-    if not (torch.equal(_ref.y_end, _got.y_end) and torch.equal(_ref.n_accept, _got.n_accept)
-            and torch.equal(_ref.hit_t.nan_to_num(), _got.hit_t.nan_to_num())):
-        raise SystemExit("prepared batch and propagate_dop853 disagree")
-
     # plain form: one kernel call per trajectory, the reference's call
     # granularity (one _propagate_dynsys per seed), on a bounded sample
     n_plain = 64
@@ -818,36 +806,49 @@ def main():
     p0 = torch.cuda.Event(enable_timing=True)
     p1 = torch.cuda.Event(enable_timing=True)
     p0.record(stream)
-    plain_acc = 0
     plain_res = [M.propagate_to_plane(seeds_dev[i:i + 1], mu, tf=TF, forward=-1, device=dev) for i in range(n_plain)]
     p1.record(stream)
     torch.cuda.synchronize(dev)
     plain_acc = sum(int(x.n_accept.sum().item()) for x in plain_res)
     plain_value = plain_acc / (p0.elapsed_time(p1) * 1e-3)
 
-    # ---- device-resident timing (CUDA events on the launching stream)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    acc = att = 0
-    H = _lib.handle(local)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize(dev)
-    launches0 = H.kernel_launches()
-    gc.collect()
-    gc.disable()  # no collector pause inside the host-synchronised steps
+    # the clock sampler starts here, ahead of the warm-up steps, so that its start-up is over before
+    # the timed region; it is stopped after the timed steps, on every path
+    clk = ClockSampler(local).__enter__()
     try:
-        clk.begin()
-        results = []
-        for i in range(args.steps):
-            flush.fill_(float(i))
-            evs[i][0].record(stream)
-            r = one_step()
-            evs[i][1].record(stream)
-            results.append(r)
+        for _ in range(max(args.warmup, 3)):
+            one_step()
         torch.cuda.synchronize(dev)
-        clk.end()
+        _ref = run(sched)
+        _got = one_step()
+        if not (torch.equal(_ref.y_end, _got.y_end) and torch.equal(_ref.n_accept, _got.n_accept)
+                and torch.equal(_ref.hit_t.nan_to_num(), _got.hit_t.nan_to_num())):
+            raise SystemExit("prepared batch and propagate_dop853 disagree")
+
+        # ---- device-resident timing (CUDA events on the launching stream)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        H = _lib.handle(local)
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        launches0 = H.kernel_launches()
+        gc.collect()
+        gc.disable()  # no collector pause inside the host-synchronised steps
+        try:
+            clk.begin()
+            results = []
+            for i in range(args.steps):
+                flush.fill_(float(i))
+                evs[i][0].record(stream)
+                r = one_step()
+                evs[i][1].record(stream)
+                results.append(r)
+            torch.cuda.synchronize(dev)
+            clk.end()
+        finally:
+            gc.enable()
     finally:
-        gc.enable()
         clk.__exit__(None, None, None)
     launches = H.kernel_launches() - launches0
     if world > 1:
