@@ -3,9 +3,9 @@
 The propagation kernels have launch-shape knobs that never change results
 (lanes per 6-dim DOP853 trajectory, threads per block; see
 `propagate.tuning`).  Which shape is fastest depends on the batch: a batch
-that fills every SM sub-partition is throughput-bound and wants one lane per
-trajectory; a small or very uneven batch is bound by its longest trajectory
-and wants lane pairs, which halve the per-step latency.  `tune` times every
+that keeps every SM's FP64 unit busy is throughput-bound and wants one lane
+per trajectory; a small or very uneven batch is bound by its longest
+trajectory and wants lane pairs, which halve the per-step latency.  `tune` times every
 candidate shape on the caller's own workload with CUDA events and keeps the
 fastest; results are cached per workload key for the life of the process and
 optionally in a JSON file.

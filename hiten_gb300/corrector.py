@@ -65,7 +65,7 @@ class GpuShootingBackend:
     """The two propagations single shooting needs, batched on the GPU.
 
     ``spec_traj``: the event-leg size that still runs at the per-step latency
-    floor (six lanes per trajectory, one warp per SM sub-partition)."""
+    floor (six lanes per trajectory, four warps per SM)."""
 
     def __init__(self, mu, options=None, device=None):
         self.mu = float(mu)

@@ -300,7 +300,8 @@ int ensure_scratch(hg_handle* h, long long bytes) {
 // Launch shape of a DOP853 kernel: threads per block, dynamic shared memory
 // and resident blocks per SM.  In spread mode a block of four warps reserves
 // more than half of the SM's shared memory (unused), so no two blocks share
-// an SM and every warp gets an SM sub-partition's FP64 pipe to itself.
+// an SM: four warps per SM, which share its FP64 unit at nearly the rate of
+// one warp each.
 struct Shape {
   int block;
   size_t smem;
@@ -354,9 +355,10 @@ int launch_dop853(hg_handle* h, hg::DopParams p, cudaStream_t s) {
 }
 
 // Lanes per 6-dim DOP853 trajectory when the caller did not choose: the
-// largest group whose warps still fit one per SM sub-partition (the longest
-// trajectory sets the time and its per-step latency falls with the group
-// size), single lanes once even those oversubscribe.
+// largest group whose warps still fit four per SM, about what an SM's FP64
+// unit serves at each warp's full rate (the longest trajectory sets the time
+// and its per-step latency falls with the group size), single lanes once even
+// those oversubscribe.
 int auto_lanes_d6(const hg_handle* h, int N) {
   const long long smsp = 4LL * h->sm_count;
   if ((N + 4LL) / 5 <= smsp) return 6;

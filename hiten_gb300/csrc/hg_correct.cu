@@ -285,7 +285,7 @@ int hg_correct_halo(hg_handle* h, double mu, int N, double* x, long long ld, dou
   };
 
   // trajectories an event leg takes at its per-step latency floor (six lanes
-  // per trajectory, one warp per SM sub-partition: 4 x SMs x 5), at most N
+  // per trajectory, four warps per SM: 4 x SMs x 5), at most N
   // (the buffers' capacity)
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=

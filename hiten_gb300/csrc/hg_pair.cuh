@@ -2,15 +2,14 @@
 // (fixed_rk_pair_kernel) and single-pass DOP853 without an event
 // (dop853_pair_kernel).
 //
-// Why.  On GB300 an FP64 warp instruction holds its SM sub-partition's FP64
-// pipe for 64 (DFMA) to 76 (DMUL, DADD) cycles whatever the number of active
-// lanes, so one warp's step costs (its FP64 instructions) x ~70 cycles.  A
-// batch of about a thousand 42-dim trajectories fills fewer warps than the
-// GPU has sub-partitions, and its time is the per-warp instruction count of
-// a step.  The state of a trajectory (6 components, the Hessian of the
-// potential and the accelerations) and its STM (36 components, F(x) Phi)
-// are two instruction streams of about the same length; run on two warps of
-// one block, on two sub-partitions, they halve that count.
+// Why.  On GB300 a warp has one FP64 instruction in flight at a time, for
+// 64 cycles whatever the number of active lanes (76 when four warps share the
+// SM's FP64 unit), so one warp's step costs (its FP64 instructions) x 64-76
+// cycles.  A batch of about a thousand 42-dim trajectories gives only a few
+// warps per SM, and its time is the per-warp instruction count of a step.
+// The state of a trajectory (6 components, the Hessian of the potential and
+// the accelerations) and its STM (36 components, F(x) Phi) are two
+// instruction streams; run on two warps of one block they split that count.
 //
 // Layout.  A trajectory group is five trajectories served by two warps:
 //   * the state warp: lane 6t + j (t < 5, j < 6) holds state component 36 + j
@@ -386,9 +385,10 @@ __global__ void __launch_bounds__(128) fixed_rk_pair_kernel(FixedParams p) {
 // the state warp of five trajectories, warps 1 and 2 their STM as half
 // columns (PairStmHalf), as dop853_trio_kernel lays them out.  The STM
 // warp's stage work is halved and a batch of N trajectories issues 3N / 5
-// warps instead of 2N / 5, so a batch of about a thousand fills every SM
-// sub-partition's FP64 pipe.  The Hessian ring's "empty" barriers take both
-// STM warps' arrivals.
+// warps instead of 2N / 5: faster while every SM holds at most one group
+// (below about 760 trajectories), level or slower beyond, where two groups'
+// six warps share an SM's FP64 unit.  The Hessian ring's "empty" barriers
+// take both STM warps' arrivals.
 template <int ORDER>
 __global__ void __launch_bounds__(96) fixed_rk_trio_kernel(FixedParams p) {
   __shared__ PairLink link;
