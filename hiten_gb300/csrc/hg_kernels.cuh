@@ -204,10 +204,14 @@ __device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, do
   const double mu2 = 1.0 - mu;
   const double t1 = x + mu;
   const double t2 = x - mu2;
-  const double ys = y * y;
-  const double zs = z * z;
-  const double t1s = t1 * t1;
-  const double t2s = t2 * t2;
+  // the four squares in one multiply (job 0: t1, 1: t2, 2: y, 3: z; further
+  // jobs repeat t1), gathered from their lanes
+  const double base_sq = job == 1 ? t2 : (job == 2 ? y : (job == 3 ? z : t1));
+  const double sq = base_sq * base_sq;
+  const double t1s = L.from(sq, 0);
+  const double t2s = L.from(sq, 1);
+  const double ys = L.from(sq, 2);
+  const double zs = L.from(sq, 3);
   const bool b2 = job >= 3;
   const int k = b2 ? job - 3 : job;
   const double rr = ((b2 ? t2s : t1s) + ys) + zs;
@@ -229,16 +233,18 @@ __device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, do
   // acceleration lanes 3/4/5 read the x/y/z quotients of both primaries
   const int ua = job == 3 ? 0 : 1, wa = job == 3 ? 3 : 4;
   const double u0 = L.from(q0, ua), u1 = L.from(q1, ua), w0 = L.from(q0, wa), w1 = L.from(q1, wa);
-  const double a3 = qa * 3.0;
-  const double b3 = qb * 3.0;
-  const double c3 = c3a + c3b;
   // job 0 xx, 1 yy, 2 zz, 3 ax, 4 ay, 5 az
   const bool acc = b2;
   const int e = job;
+  // one multiply forms a3 = qa * 3 on jobs 0..2 and the Coriolis term
+  // 2 vy / -2 vx on jobs 3, 4
+  const double f1 = (acc ? (e == 4 ? -2.0 : 2.0) : qa) * (acc ? (e == 4 ? vx : vy) : 3.0);
+  const double b3 = qb * 3.0;
+  const double c3 = c3a + c3b;
   double P, A, U, B, W, Cc;
   if (!acc) {
     P = e == 2 ? -0.0 : 1.0;
-    A = a3;
+    A = f1;
     U = e == 0 ? t1s : (e == 1 ? ys : zs);
     B = b3;
     W = e == 0 ? t2s : (e == 1 ? ys : zs);
@@ -249,7 +255,7 @@ __device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, do
     U = e == 3 ? u1 : (e == 4 ? u0 : u1);  // t1/r3 | y/r3 | z/r3
     B = -mu;
     W = e == 3 ? w1 : (e == 4 ? w0 : w1);  // t2/R3 | y/R3 | z/R3
-    Cc = e == 3 ? 2.0 * vy : (e == 4 ? -2.0 * vx : -0.0);
+    Cc = e == 5 ? -0.0 : f1;
   }
   const double form = ((P + A * U) + B * W) + Cc;
   Hess H;
@@ -396,8 +402,12 @@ struct Layout<2> {
     const double mb = r0 ? omu : mu;
     const double mz = r0 ? -omu : mu;
     const double t = x + cb;
-    const double yy = y * y;
-    const double zz = z * z;
+    // y*y on role 0 and z*z on role 1 in one multiply, exchanged
+    const double w = r0 ? y : z;
+    const double sq = w * w;
+    const double sqo = __shfl_xor_sync(gmask, sq, 1);
+    const double yy = r0 ? sq : sqo;
+    const double zz = r0 ? sqo : sq;
     const double r = sqrt((t * t + yy) + zz);
     const double rc = r * (r * r);
     const double ir = hg_rcp_rn(rc);
@@ -461,9 +471,14 @@ struct Layout<6> {
     const double a1 = b0 ? mu : -1.0;  // x-numerator: (x + a1) + a2
     const double a2 = b0 ? 0.0 : mu;
     const double t = x + cb;
-    const double yy = y * y;
-    const double zz = z * z;
-    const double r = sqrt((t * t + yy) + zz);
+    // the squares t_b^2, y^2, z^2 in one multiply: lane (b, a) squares t_b,
+    // y or z for a = 0, 1, 2, and each lane gathers its primary's three
+    const double w = ax == 0 ? t : (ax == 1 ? y : z);
+    const double sq = w * w;
+    const double tt = __shfl_sync(gmask, sq, base + (b0 ? 0 : 3));
+    const double yy = __shfl_sync(gmask, sq, base + 1);
+    const double zz = __shfl_sync(gmask, sq, base + 2);
+    const double r = sqrt((tt + yy) + zz);
     const double rc = r * (r * r);
     const double ir = hg_rcp_rn(rc);
     const double nx = (x + a1) + a2;
