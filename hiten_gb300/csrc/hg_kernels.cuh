@@ -195,9 +195,9 @@ struct Layout<1> {
 // ((p + a u) + b w) + c whose operands reproduce hessian42's exactly
 // (x - m == x + (-m), (-a) u == -(a u), -0 + v == v), and those six are
 // exchanged again.  Same operations on the same operands: same bits.
-// With OFFDIAG = false the off-diagonal entries are left to the caller:
-// H.xy then carries sxy and H.yz carries qa + qb (H.xz is unset), from which
-// xy = (3y) sxy, xz = (3z) sxy, yz = ((3y) z)(qa + qb) as below.
+// With OFFDIAG = false each of lanes 3..5 forms one off-diagonal entry, in
+// H.xy: job 3 xy, job 4 yz, job 5 xz (the products below, their factors
+// formed in the instructions that give lanes 0..2 b3 and c3).
 template <class LT, bool OFFDIAG = true>
 __device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, double y, double z, double vx, double vy,
                                             double mu) {
@@ -239,8 +239,19 @@ __device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, do
   // one multiply forms a3 = qa * 3 on jobs 0..2 and the Coriolis term
   // 2 vy / -2 vx on jobs 3, 4
   const double f1 = (acc ? (e == 4 ? -2.0 : 2.0) : qa) * (acc ? (e == 4 ? vx : vy) : 3.0);
-  const double b3 = qb * 3.0;
-  const double c3 = c3a + c3b;
+  double b3, c3, f3 = 0.0, s2 = 0.0;
+  if constexpr (OFFDIAG) {
+    b3 = qb * 3.0;
+    c3 = c3a + c3b;
+  } else {
+    // jobs 0..2 form b3 = qb * 3 and c3, jobs 3..5 the first factor of their
+    // off-diagonal entry (3y or 3z) and its sum (sxy, or qa + qb for yz), in
+    // the same two instructions
+    f3 = (acc ? (e == 5 ? z : y) : qb) * 3.0;
+    s2 = (acc ? (e == 4 ? qa : sxa) : c3a) + (acc ? (e == 4 ? qb : sxb) : c3b);
+    b3 = f3;
+    c3 = s2;
+  }
   double P, A, U, B, W, Cc;
   if (!acc) {
     P = e == 2 ? -0.0 : 1.0;
@@ -265,15 +276,18 @@ __device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, do
   H.ax = L.from(form, 3);
   H.ay = L.from(form, 4);
   H.az = L.from(form, 5);
-  const double sxy = sxa + sxb;
   if constexpr (OFFDIAG) {
+    const double sxy = sxa + sxb;
     H.xy = (3.0 * y) * sxy;
     H.xz = (3.0 * z) * sxy;
     H.yz = ((3.0 * y) * z) * (qa + qb);
   } else {
-    H.xy = sxy;
+    // this lane's off-diagonal entry as hessian42 forms it: job 3 xy = (3y) sxy,
+    // job 4 yz = ((3y) z)(qa + qb), job 5 xz = (3z) sxy, one product
+    // ((3a) b) c (c = 1.0 where two factors suffice: exact)
+    H.xy = (f3 * (e == 4 ? z : s2)) * (e == 4 ? s2 : 1.0);
     H.xz = 0.0;
-    H.yz = qa + qb;
+    H.yz = 0.0;
   }
   return H;
 }

@@ -159,14 +159,9 @@ struct PairState {
       broken = !__all_sync(0xFFFFFFFFu, ok);
     }
     if (!broken) {
-      // the six Hessian entries xx, yy, zz, xy, yz, xz, the off-diagonal ones
-      // as hessian42 forms them: xy = (3y) sxy, yz = ((3y) z)(qa + qb),
-      // xz = (3z) sxy, one product ((3a) b) c on lanes 3..5 (c = 1.0 where
-      // two factors suffice: exact); H.xy holds sxy and H.yz qa + qb here
-      const double fa = role == 5 ? z : y;
-      const double fb = role == 4 ? z : H.xy;
-      const double fc = role == 4 ? H.yz : 1.0;
-      const double off = ((3.0 * fa) * fb) * fc;
+      // the six Hessian entries xx, yy, zz, xy, yz, xz: lanes 3..5 formed
+      // the off-diagonal ones as hessian42 does (H.xy holds this lane's)
+      const double off = H.xy;
       if (role < 6) link->H[b][t][role] = role == 0 ? H.xx : (role == 1 ? H.yy : (role == 2 ? H.zz : off));
       mbar_arrive(&link->full[b]);
     }
