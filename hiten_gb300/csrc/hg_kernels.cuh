@@ -202,26 +202,25 @@ template <class LT, bool OFFDIAG = true>
 __device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, double y, double z, double vx, double vy,
                                             double mu) {
   const double mu2 = 1.0 - mu;
-  const double t1 = x + mu;
-  const double t2 = x - mu2;
-  // the four squares in one multiply (job 0: t1, 1: t2, 2: y, 3: z; further
-  // jobs repeat t1), gathered from their lanes
-  const double base_sq = job == 1 ? t2 : (job == 2 ? y : (job == 3 ? z : t1));
-  const double sq = base_sq * base_sq;
-  const double t1s = L.from(sq, 0);
-  const double t2s = L.from(sq, 1);
-  const double ys = L.from(sq, 2);
-  const double zs = L.from(sq, 3);
   const bool b2 = job >= 3;
   const int k = b2 ? job - 3 : job;
+  const double m = b2 ? mu : mu2;
+  // this lane's primary: tt = x + mu | x - mu2 (x - m == x + (-m))
+  const double tt = x + (b2 ? -mu2 : mu);
+  // the four squares and both numerators m tt in one multiply (job 0: t1^2,
+  // 1: y^2, 2: mu2 t1, 3: t2^2, 4: z^2, 5: mu t2; further jobs repeat
+  // job 0), the squares gathered from their lanes
+  const double sq = (k == 0 ? tt : (job == 1 ? y : (job == 4 ? z : m))) * (job == 1 ? y : (job == 4 ? z : tt));
+  const double t1s = L.from(sq, 0);
+  const double t2s = L.from(sq, 3);
+  const double ys = L.from(sq, 1);
+  const double zs = L.from(sq, 4);
   const double rr = ((b2 ? t2s : t1s) + ys) + zs;
   double p3, p5;
   hg_pow15_25(rr, p3, p5);
   const double den = k == 2 ? p5 : p3;
   const double inv = hg_rcp_rn(den);
-  const double m = b2 ? mu : mu2;
-  const double tt = b2 ? t2 : t1;
-  const double mt = m * tt;
+  const double mt = sq;  // jobs 2 and 5
   const double n0 = k == 1 ? y : m;
   const double n1 = k == 0 ? tt : (k == 1 ? z : mt);
   const double q0 = hg_div_rn(n0, den, inv);
