@@ -205,6 +205,47 @@ HG_HD void hg_pow15_25(double x, double& p15, double& p25) {
   }
 }
 
+// One of the two powers: RN(x^1.5) when !want25, RN(x^2.5) when want25 --
+// the bits hg_pow15_25 gives.  For lanes of a warp that want different
+// ones: the final sum hi + lo of x^1.5 and the leading product RN(x * hi) of
+// x^2.5 share one fused multiply-add (fma(1, hi, lo) = RN(hi + lo),
+// fma(x, hi, 0) = RN(x hi) for x hi > 0), one FP64 instruction fewer than
+// forming both.
+HG_HD double hg_pow15_or_25(double x, bool want25) {
+#if defined(__CUDA_ARCH__)
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  if ((unsigned)(bits >> 52) - 625u > 796u) return pow(x, want25 ? 2.5 : 1.5);
+  double y0;
+  asm("rsqrt.approx.f64 %0, %1;" : "=d"(y0) : "d"(x));
+  double g = x * y0, h = 0.5 * y0;
+  double r = fma(-g, h, 0.5);
+  g = fma(g, r, g);
+  h = fma(h, r, h);
+  r = fma(-g, h, 0.5);
+  g = fma(g, r, g);
+  h = fma(h, r, h);
+  const double e = fma(-g, g, x) * h;
+  const double hi = x * g;
+  double lo = fma(x, g, -hi);
+  lo = fma(x, e, lo);
+  const double f = fma(want25 ? x : 1.0, hi, want25 ? 0.0 : lo);  // hi + lo | RN(x hi)
+  double l2 = fma(x, hi, -f);
+  l2 = fma(x, lo, l2);
+  double p = want25 ? f + l2 : f;
+  const uint64_t b = bits;
+  if ((b & 0x000FFFFFFFFFFFFFull) == 0x000FFFFFFFFFFFFFull && ((b >> 52) & 1u) == 0) {
+    const int q = ((int)(b >> 52) - 1022) / 2;
+    p = want25 ? hg_from_bits(((uint64_t)(5 * q + 1022) << 52) | 0x000FFFFFFFFFFFFEull)
+               : hg_from_bits(((uint64_t)(3 * q + 1022) << 52) | 0x000FFFFFFFFFFFFFull);
+  }
+  return p;
+#else
+  double p15, p25;
+  hg_pow15_25(x, p15, p25);
+  return want25 ? p25 : p15;
+#endif
+}
+
 // log(x) as double-double, x > 0 finite.  Absolute error <~ 2^-85.
 HG_HD void hg_log_dd(double x, double& Lh, double& Ll) {
   int e = 0;

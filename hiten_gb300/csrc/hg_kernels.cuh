@@ -216,9 +216,7 @@ __device__ __forceinline__ Hess hessian_split(const LT& L, int job, double x, do
   const double ys = L.from(sq, 1);
   const double zs = L.from(sq, 4);
   const double rr = ((b2 ? t2s : t1s) + ys) + zs;
-  double p3, p5;
-  hg_pow15_25(rr, p3, p5);
-  const double den = k == 2 ? p5 : p3;
+  const double den = hg_pow15_or_25(rr, k == 2);  // r^3 (jobs 0, 1) or r^5 (job 2) of the lane's primary
   const double inv = hg_rcp_rn(den);
   const double mt = sq;  // jobs 2 and 5
   const double n0 = k == 1 ? y : m;
@@ -657,10 +655,21 @@ struct Gather<6> {
     }
     return s;
   }
+  // the two dots in the same six fused multiply-adds: lanes 0..2 accumulate
+  // a, lanes 3..5 b, then each is broadcast
   __device__ __forceinline__ void dot2(const Layout<6>& L, const double (&a)[1], const double (&b)[1], double& da,
                                        double& db) const {
-    da = dot(L, a);
-    db = dot(L, b);
+    const bool first = L.role < 3;
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const double ca = __shfl_sync(L.gmask, a[0], L.base + i);
+      const double cb = __shfl_sync(L.gmask, b[0], L.base + i);
+      const double c = first ? ca : cb;
+      s = fma(c, c, s);
+    }
+    da = __shfl_sync(L.gmask, s, L.base);
+    db = __shfl_sync(L.gmask, s, L.base + 3);
   }
 };
 

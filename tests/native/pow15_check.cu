@@ -1,4 +1,4 @@
-// Checks the device hg_pow15_25 (Goldschmidt square root from the hardware
+// Checks the device hg_pow15_25 and hg_pow15_or_25 (Goldschmidt square root from the hardware
 // estimate) against the host method (correctly rounded sqrt, double-double,
 // the midpoint family set exactly), written out here with CUDA's sqrt and rsqrt, on random x with uniformly
 // random mantissas and exponents in [-100, 100] plus mantissas next to a
@@ -61,7 +61,9 @@ __global__ void check(unsigned long long n, unsigned long long seed, unsigned lo
     double a, b, c, d;
     hg_pow15_25(x, a, b);
     host_method(x, c, d);
-    if (__double_as_longlong(a) != __double_as_longlong(c) || __double_as_longlong(b) != __double_as_longlong(d))
+    const double a1 = hg_pow15_or_25(x, false), b1 = hg_pow15_or_25(x, true);
+    if (__double_as_longlong(a) != __double_as_longlong(c) || __double_as_longlong(b) != __double_as_longlong(d) ||
+        __double_as_longlong(a1) != __double_as_longlong(c) || __double_as_longlong(b1) != __double_as_longlong(d))
       ++local;
     double y0;
     asm("rsqrt.approx.f64 %0, %1;" : "=d"(y0) : "d"(x));
