@@ -23,11 +23,13 @@ reference-shaped public API (hiten_gb300.manifold.propagate_to_plane, a full
 per-call setup).  `gpu_launches`:
 kernels launched in the timed region, read from the library's counter.
 
-`secondary`: the other BASELINE configs measured in the same run after the
-headline -- config 1 (RK8 + STM), config 3 (synodic section), config 4 (halo
-correction, ||r|| and ||dx||) and config 5 (serving mix, p50/p99) -- each with
-its time, roofline fraction of the FP64 peak, plain-GPU form and CPU oracle
-baseline (`--no-secondary` skips them; `--workload W` runs one alone).
+`secondary`: the other workloads of the metric, measured in the same run
+after the headline -- fixed-step RK8 with the STM (1024 states x 3000 steps),
+the synodic section (65536 states, <= 8 crossings), batched halo correction
+(2048 guesses, ||r|| and ||dx||) and the serving mix (Poisson 200 req/s,
+p50/p99) -- each with its time, roofline fraction of the FP64 peak, plain-GPU
+form and CPU oracle baseline (`--no-secondary` skips them; `--workload W`
+runs one alone).
 
 `--impl reference`: the reference's algorithm on the host cores (the CPU
 oracle in numba-lowering mode, one trajectory per task, all host threads),
@@ -329,7 +331,7 @@ FLOPS_PER_ATTEMPT_D42 = 8586.0
 
 
 def sec_fixed_stm(steps, dev, peak, cpu=True):
-    """BASELINE config 1: fixed-step RK8 with the 42-dim variational system, 1024 states (STM = I),
+    """Fixed-step RK8 with the 42-dim variational system, 1024 states (STM = I),
     t in [0, 3], 3000 steps, every 100th state written."""
     import torch
     from hiten_gb300 import propagate as P
@@ -367,7 +369,7 @@ def bench_fixed_stm(args):
 
 
 def sec_section(steps, dev, peak, cpu=True):
-    """BASELINE config 3: 65536 Jacobi-matched states near L1/L2, DOP853 1e-11 to t = 20, up to 8 y = 0
+    """Synodic section: 65536 Jacobi-matched states near L1/L2, DOP853 1e-11 to t = 20, up to 8 y = 0
     crossings (direction -1) each; the execution plan (single pass or host-scheduled segments, same bits)
     chosen by the autotuner on this workload."""
     import torch
@@ -461,7 +463,7 @@ def bench_synodic_detect(args):
 
 
 def sec_correct(steps, dev, peak, cpu=True):
-    """BASELINE config 4: batched halo correction, 2048 third-order guesses (half L1, half L2,
+    """Batched halo correction: 2048 third-order guesses (half L1, half L2,
     Az ~ U[0.01, 0.4], zenith 50/50 seeded), single shooting on the half-period y = 0 crossing until
     ||r||_inf < 1e-12 (the reference's criterion); ||dx||_inf of one more Newton step at the result is
     reported beside it."""
@@ -570,7 +572,7 @@ def bench_correct(args):
 
 
 def sec_serving(steps, dev, peak, cpu=True, seeds=None):
-    """BASELINE config 5: seeded Poisson stream (200 req/s for 1 s) of manifold (64-4096 seeds), correction
+    """Serving mix: seeded Poisson stream (200 req/s for 1 s) of manifold (64-4096 seeds), correction
     (1-256 guesses) and synodic (1k-32k states) requests; continuous batching vs the same stream run
     sequentially in the plain form (one single-pass call per request)."""
     from hiten_gb300 import serving
@@ -612,7 +614,7 @@ def sec_serving(steps, dev, peak, cpu=True, seeds=None):
            "sequential_plain_burst": seq_burst,
            "merged_batches_poisson": served_batch, "merged_batches_burst": served_batch_burst,
            "speedup_vs_plain": served_burst["traj_steps_per_s"] / seq_burst["traj_steps_per_s"],
-           "roofline": {"bound": "fp64", "note": "the served batches run the kernels of configs 2-4; see their "
+           "roofline": {"bound": "fp64", "note": "the served batches run the manifold, section and correction kernels; see their "
                                                   "roofline entries"}}
     if cpu:
         from oracle import hgo
@@ -739,7 +741,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
-                    help="skip the other BASELINE configs (1, 3, 4, 5) measured after the headline")
+                    help="skip the other workloads (RK8 + STM, section, correction, serving) measured after the headline")
     ap.add_argument("--plan", default=None,
                     help="force an execution plan by name (autotune.plan_name), e.g. scheduled_seg16")
     ap.add_argument("--workload", default="manifold", choices=["manifold"] + sorted(EXTRA),
@@ -932,16 +934,16 @@ def main():
     dom = dominant_launch(run_segment, plan, N, torch.cuda.get_device_properties(dev).multi_processor_count,
                           stream)
 
-    # the other BASELINE configs, each measured in this run after the headline
+    # the other workloads of the metric, each measured in this run after the headline
     # (rank 0 of a single-GPU run; replicas add nothing to them)
     secondary = None
     if rank == 0 and world == 1 and not args.no_secondary:
         cpu_ok = not args.no_cpu_baseline
         secondary = {}
-        for key, fn in (("config1_fixed_stm", lambda: sec_fixed_stm(args.steps, dev, peak, cpu_ok)),
-                        ("config3_section", lambda: sec_section(args.steps, dev, peak, cpu_ok)),
-                        ("config4_correct", lambda: sec_correct(args.steps, dev, peak, cpu_ok)),
-                        ("config5_serving", lambda: sec_serving(args.steps, dev, peak, cpu_ok, seeds=seeds))):
+        for key, fn in (("fixed_rk8_stm_1024x3000", lambda: sec_fixed_stm(args.steps, dev, peak, cpu_ok)),
+                        ("section_65536", lambda: sec_section(args.steps, dev, peak, cpu_ok)),
+                        ("halo_correction_2048", lambda: sec_correct(args.steps, dev, peak, cpu_ok)),
+                        ("serving_poisson_200hz", lambda: sec_serving(args.steps, dev, peak, cpu_ok, seeds=seeds))):
             t0 = time.perf_counter()
             try:
                 secondary[key] = fn()
