@@ -186,8 +186,9 @@ struct Layout<1> {
 
 // hessian42 with its work spread over a lane group: lane base + job does job
 // (0..5); L.from(v, r) reads lane base + r.  Lane b*3 + k (b = primary,
-// k < 3) takes one power pair r^3, r^5 of its primary (hg_pow15_25), one
-// reciprocal and two of the twelve quotients:
+// k < 3) takes the power of its primary its quotients divide by (r^3 for
+// k < 2, r^5 for k = 2; hg_pow15_or_25), one reciprocal and two of the
+// twelve quotients:
 //   0: mu2/r3, t1/r3     1: y/r3, z/r3     2: mu2/r5, (mu2 t1)/r5
 //   3: mu/R3,  t2/R3     4: y/R3, z/R3     5: mu/R5,  (mu t2)/R5
 // (further lanes repeat job 0).  The quotients are exchanged, lanes 0..5
