@@ -100,6 +100,56 @@ HG_HD void hg_fast_two_sum(double a, double b, double& s, double& e) {
   e = b - (s - a);
 }
 
+// ---------------------------------------------------------------------------
+// IEEE comparisons on the integer pipes.  In the propagation kernels the SM's
+// FP64 unit is the bottleneck and a floating-point compare takes a slot of it;
+// these compare bit patterns (hg_bits) instead and equal the IEEE comparison
+// for every operand (a NaN compares false, -0 equals +0).  Non-negative
+// doubles order like their bit patterns read as integers.
+// ---------------------------------------------------------------------------
+static const uint64_t HG_BITS_INF = 0x7FF0000000000000ull;
+static const uint64_t HG_BITS_NEG_INF = 0xFFF0000000000000ull;
+
+HG_HD bool hg_isnan_cmp(double x) { return (hg_bits(x) << 1) > (HG_BITS_INF << 1); }
+// x == 0
+HG_HD bool hg_eq0(double x) { return (hg_bits(x) << 1) == 0; }
+// x == 0 && y == 0
+HG_HD bool hg_both0(double x, double y) { return ((hg_bits(x) | hg_bits(y)) << 1) == 0; }
+// x > 0: the patterns of +denorm_min .. +inf
+HG_HD bool hg_gt0(double x) { return hg_bits(x) - 1ull < HG_BITS_INF; }
+// x < 0: the patterns of -denorm_min .. -inf
+HG_HD bool hg_lt0(double x) { return hg_bits(x) - 0x8000000000000001ull < HG_BITS_INF; }
+// 0 < x < c for c > 0 given by its pattern cb (c not NaN)
+HG_HD bool hg_in_open_pos(double x, uint64_t cb) { return hg_bits(x) - 1ull < cb - 1ull; }
+// x < c, x <= c and x > c for c > 0 given by its pattern cb (c may be +inf,
+// not NaN): a negative x (any pattern with the sign set but a NaN's) is below c
+HG_HD bool hg_lt_pos(double x, uint64_t cb) {
+  const uint64_t b = hg_bits(x);
+  return (int64_t)b < (int64_t)cb && b <= HG_BITS_NEG_INF;
+}
+HG_HD bool hg_le_pos(double x, uint64_t cb) {
+  const uint64_t b = hg_bits(x);
+  return (int64_t)b <= (int64_t)cb && b <= HG_BITS_NEG_INF;
+}
+HG_HD bool hg_gt_pos(double x, uint64_t cb) {
+  const uint64_t b = hg_bits(x);
+  return (int64_t)b > (int64_t)cb && (int64_t)b <= (int64_t)HG_BITS_INF;
+}
+// a > b for any a, b: the sign-magnitude patterns mapped to ordered
+// two's-complement keys (-0 and +0 to the same key 0)
+HG_HD int64_t hg_order_key(uint64_t b) {
+  const int64_t m = (int64_t)(b & 0x7FFFFFFFFFFFFFFFull);
+  return (int64_t)b < 0 ? -m : m;
+}
+HG_HD bool hg_gt(double a, double b) {
+  return !hg_isnan_cmp(a) && !hg_isnan_cmp(b) && hg_order_key(hg_bits(a)) > hg_order_key(hg_bits(b));
+}
+// patterns of the constants the step control compares with
+static const uint64_t HG_BITS_0_2 = 0x3FC999999999999Aull;    // 0.2
+static const uint64_t HG_BITS_1 = 0x3FF0000000000000ull;      // 1.0
+static const uint64_t HG_BITS_10 = 0x4024000000000000ull;     // 10.0
+static const uint64_t HG_BITS_1E300 = 0x7E37E43C8800759Cull;  // 1e300
+
 // Correctly rounded quotient a / b from the correctly rounded reciprocal
 // rb = RN(1/b) (Markstein's theorem, IBM J. Res. Dev. 34(1), 1990; see also
 // the Handbook of Floating-Point Arithmetic, sec. 4.7): q0 = RN(a*rb) is

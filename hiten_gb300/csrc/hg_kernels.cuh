@@ -636,10 +636,29 @@ struct Gather<2> {
     for (int i = 0; i < 3; ++i) s = fma(v[i], v[i], s);
     return __shfl_sync(L.gmask, s, L.base + 1);
   }
+  // the two dots side by side, each the same sequential fused accumulation
+  // over components 0..5: role 0 accumulates a, role 1 b; one exchange per
+  // component gives role 0 the partner's a (components 3..5) and role 1 the
+  // partner's b (components 0..2)
   __device__ __forceinline__ void dot2(const Layout<2>& L, const double (&a)[3], const double (&b)[3], double& da,
                                        double& db) const {
-    da = dot(L, a);
-    db = dot(L, b);
+    const bool r0 = L.role == 0;
+    double u[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) u[i] = __shfl_xor_sync(L.gmask, r0 ? b[i] : a[i], 1);
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const double c = r0 ? a[i] : u[i];
+      s = fma(c, c, s);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const double c = r0 ? u[i] : b[i];
+      s = fma(c, c, s);
+    }
+    da = __shfl_sync(L.gmask, s, L.base);
+    db = __shfl_sync(L.gmask, s, L.base + 1);
   }
 };
 
@@ -686,13 +705,15 @@ __device__ __forceinline__ double pick(const double (&v)[NC], int r) {
 // ---------------------------------------------------------------------------
 // Step-size helpers, integrators/utils.py:126-296
 // ---------------------------------------------------------------------------
+// The step bounds are > 0 and not NaN (the entry points check them), so the
+// comparisons with them run on the integer pipes.
 __device__ __forceinline__ double clamp_step(double h, double max_step, double min_step) {
-  if (h > max_step) h = max_step;
-  if (h < min_step) h = min_step;
+  if (hg_gt_pos(h, hg_bits(max_step))) h = max_step;
+  if (hg_lt_pos(h, hg_bits(min_step))) h = min_step;
   return h;
 }
 __device__ __forceinline__ double adjust_step_to_endpoint(double t, double h, double t_end) {
-  if (t + h > t_end) return fabs(t_end - t);
+  if (hg_gt(t + h, t_end)) return fabs(t_end - t);
   return h;
 }
 __device__ __forceinline__ double select_initial_step(double d0, double d1, double min_step, double max_step) {
@@ -731,7 +752,7 @@ __device__ __forceinline__ double pi_factor(const LT& L, bool accepted, double e
   const double beta = 1.0 / (8.0 + 1.0);
   const double alpha = 0.4 * beta;
   const double rexp = 1.0 / 8.0;
-  const bool regular = err > 0.0 && err < 1e300;
+  const bool regular = hg_in_open_pos(err, HG_BITS_1E300);  // 0 < err < 1e300
   double p1 = 0.0, pa = 0.0;
   if (regular) {
     double Lh, Ll;
@@ -748,28 +769,30 @@ __device__ __forceinline__ double pi_factor(const LT& L, bool accepted, double e
   }
   double factor;
   if (accepted) {
-    if (err == 0.0) {
+    if (hg_eq0(err)) {
       factor = 10.0;
       prev_pow = 0.0;
     } else {
-      factor = err_prev < 0.0 ? 0.9 * p1 : (0.9 * p1) * prev_pow;
+      factor = hg_lt0(err_prev) ? 0.9 * p1 : (0.9 * p1) * prev_pow;
       prev_pow = pa;
-      if (!(factor == factor)) factor = 10.0;
+      if (hg_isnan_cmp(factor)) factor = 10.0;
     }
   } else {
     factor = regular ? 0.9 * p1 : 0.2;
-    if (!(factor == factor)) factor = 0.2;
+    if (hg_isnan_cmp(factor)) factor = 0.2;
   }
-  if (factor < 0.2) factor = 0.2;
-  if (factor > 10.0) factor = 10.0;
+  if (hg_lt_pos(factor, HG_BITS_0_2)) factor = 0.2;
+  if (hg_gt_pos(factor, HG_BITS_10)) factor = 10.0;
   return factor;
 }
 
 // integrators/utils.py:13-68
+// (the sign tests on the integer pipes: hg_lt0 / hg_gt0 / hg_eq0 equal
+// g < 0, g > 0, g == 0)
 __device__ __forceinline__ bool event_crossed(double g_prev, double g_new, int dir) {
-  if (dir == 0) return (g_prev < 0.0 && g_new > 0.0) || (g_prev > 0.0 && g_new < 0.0) || (g_new == 0.0);
-  if (dir > 0) return (g_prev < 0.0 && g_new > 0.0) || (g_new == 0.0);
-  return (g_prev > 0.0 && g_new < 0.0) || (g_new == 0.0);
+  if (dir == 0) return (hg_lt0(g_prev) && hg_gt0(g_new)) || (hg_gt0(g_prev) && hg_lt0(g_new)) || hg_eq0(g_new);
+  if (dir > 0) return (hg_lt0(g_prev) && hg_gt0(g_new)) || hg_eq0(g_new);
+  return (hg_gt0(g_prev) && hg_lt0(g_new)) || hg_eq0(g_new);
 }
 __device__ __forceinline__ bool crossed_direction(double g_left, double g_mid, int dir) {
   if (dir == 0) return (g_left < 0.0 && g_mid > 0.0) || (g_left > 0.0 && g_mid < 0.0);
@@ -1826,7 +1849,7 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
 
     // integrators/rk.py loop test (t - t_end) * direction < 0 with direction
     // +1; the product by 1 is exact, so it is left out
-    while (t - tmax < 0.0) {
+    while (hg_lt0(t - tmax)) {
       if (p.seg && seg_count >= seg_budget) {
         paused = true;
         break;
@@ -1853,12 +1876,12 @@ __global__ void __launch_bounds__(128) dop853_kernel(DopParams p) {
         }
         double n5, n3;
         gat.dot2(L, s5, s3, n5, n3);
-        if (n5 == 0.0 && n3 == 0.0)
+        if (hg_both0(n5, n3))
           err_norm = 0.0;
         else
           err_norm = (fabs(h) * n5) / sqrt((n5 + 0.01 * n3) * (double)D);
       }
-      const bool accepted = err_norm <= 1.0;
+      const bool accepted = hg_le_pos(err_norm, HG_BITS_1);  // err_norm <= 1
       bool fin = true;
       if (accepted) {
         ++acc;

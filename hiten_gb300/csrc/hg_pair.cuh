@@ -538,7 +538,7 @@ __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, Pa
   if (dense) step_ls = (tmax - t0) / (double)(p.m - 1);
   auto sample_t = [&](int q) -> double { return q == p.m - 1 ? tmax : (double)q * step_ls + t0; };
   // integrators/rk.py loop test (t - t_end) * direction < 0, direction +1
-  bool live = running && (t - tmax < 0.0);
+  bool live = running && hg_lt0(t - tmax);
   DopGroupCoef<6> cf(coef_tab, L.role % 6, L.base, L.gmask);
   while (vote_any(live)) {
     bool go = live;
@@ -570,11 +570,11 @@ __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, Pa
     pair_exchange(L, gx, gseq, s5, s3, fin ? 1.0 : 0.0, n5, n3, fin_all);
     fin = fin_all != 0.0;
     double err_norm;
-    if (n5 == 0.0 && n3 == 0.0)
+    if (hg_both0(n5, n3))
       err_norm = 0.0;
     else
       err_norm = (fabs(hh) * n5) / sqrt((n5 + 0.01 * n3) * (double)D);
-    const bool accepted = err_norm <= 1.0;
+    const bool accepted = hg_le_pos(err_norm, HG_BITS_1);  // err_norm <= 1
     const double t_new = t + hh;
     // dense samples inside (t, t_new] (reference: searchsorted on nodes);
     // the cache's three extra evaluations run on the whole warp
@@ -622,7 +622,7 @@ __device__ __forceinline__ bool pair_dop_run(const LT& L, const DopParams& p, Pa
         h = clamp_step(h, p.max_step, p.min_step);
       }
     }
-    live = running && (t - tmax < 0.0) && !L.broken;
+    live = running && hg_lt0(t - tmax) && !L.broken;
   }
   if (valid && writes) {
     // the reference's dense output falls back to the single stored node when

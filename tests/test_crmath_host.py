@@ -18,3 +18,15 @@ def test_crmath_matches_quad_pow(tmp_path):
     out = subprocess.check_output([exe, "200000"]).decode().split()
     n, bad15, bad25, badp = map(int, out)
     assert n == 200000 and bad15 == 0 and bad25 == 0 and badp == 0
+
+
+def test_integer_pipe_compares_match_ieee(tmp_path):
+    """The kernels' step control compares bit patterns on the integer pipes
+    (hg_gt0, hg_lt_pos, hg_gt, ...); each equals the IEEE comparison, NaNs of
+    either sign and signed zeros included."""
+    exe = str(tmp_path / "cmp_check")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                           "-I" + os.path.join(REPO, "hiten_gb300", "csrc"),
+                           os.path.join(REPO, "tests", "native", "cmp_check.cpp"), "-o", exe])
+    checks, bad = map(int, subprocess.check_output([exe, "100000"]).decode().split())
+    assert checks > 1_000_000 and bad == 0
