@@ -135,6 +135,12 @@ HG_HD bool hg_gt_pos(double x, uint64_t cb) {
   const uint64_t b = hg_bits(x);
   return (int64_t)b > (int64_t)cb && (int64_t)b <= (int64_t)HG_BITS_INF;
 }
+// x < c for c < 0 given by its pattern cb (c not NaN): x is negative with a
+// larger magnitude pattern, and not a NaN
+HG_HD bool hg_lt_neg(double x, uint64_t cb) {
+  const uint64_t b = hg_bits(x);
+  return b > cb && b <= HG_BITS_NEG_INF;
+}
 // a > b for any a, b: the sign-magnitude patterns mapped to ordered
 // two's-complement keys (-0 and +0 to the same key 0)
 HG_HD int64_t hg_order_key(uint64_t b) {
@@ -297,21 +303,31 @@ HG_HD double hg_pow15_or_25(double x, bool want25) {
 }
 
 // log(x) as double-double, x > 0 finite.  Absolute error <~ 2^-85.
+// The reduction x = 2^e m, m in (sqrt(2)/2, sqrt(2)], and the table index
+// j = rint((m - 1) * 1024) with F = 1 + j / 1024 are formed from the bit
+// pattern on the integer pipes: for m = 1 + M 2^-52 (M the mantissa field),
+// (m - 1) * 1024 = M 2^-42; for m = (1 + M 2^-52) / 2 it is M 2^-43 - 512; the
+// shift rounds half to even as rint does, and F's pattern is 1.0's plus
+// j 2^42 (j >= 0) or minus |j| 2^43 (j < 0, F in [1/2, 1)).  Every value is
+// the one the floating-point reduction gives.
 HG_HD void hg_log_dd(double x, double& Lh, double& Ll) {
   int e = 0;
-  if (x < 2.2250738585072014e-308) {
-    x *= 18014398509481984.0;  // 2^54
+  if (hg_lt_pos(x, 0x0010000000000000ull)) {  // x < 2^-1022 (subnormal)
+    x *= 18014398509481984.0;                  // 2^54
     e = -54;
   }
   const uint64_t b = hg_bits(x);
-  e += (int)((b >> 52) & 0x7ff) - 1023;
-  double m = hg_from_bits((b & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull);
-  if (m > 1.4142135623730951) {
-    m *= 0.5;
-    e += 1;
-  }
-  const int j = (int)rint((m - 1.0) * 1024.0);
-  const double F = 1.0 + (double)j * 0.0009765625;
+  const uint64_t M = b & 0x000FFFFFFFFFFFFFull;
+  const bool halve = M > 0x6A09E667F3BCDull;  // 1 + M 2^-52 > 1.4142135623730951
+  e += (int)((b >> 52) & 0x7ff) - 1023 + (halve ? 1 : 0);
+  const double m = hg_from_bits(M | (halve ? 0x3FE0000000000000ull : 0x3FF0000000000000ull));
+  const int sh = halve ? 43 : 42;
+  const uint64_t jq = M >> sh;
+  const uint64_t jr = M & ((1ull << sh) - 1ull);
+  const uint64_t jh = 1ull << (sh - 1);
+  const int j = (int)(jq + ((jr > jh || (jr == jh && (jq & 1ull))) ? 1ull : 0ull)) - (halve ? 512 : 0);
+  const double F = hg_from_bits(j >= 0 ? 0x3FF0000000000000ull + ((uint64_t)j << 42)
+                                       : 0x3FF0000000000000ull - ((uint64_t)(-j) << 43));
   const double f = m - F;  // exact (Sterbenz)
   const int ti = j - HG_LOG_JMIN;
   const double invF = HG_TAB(log_invf, ti);
@@ -343,8 +359,8 @@ HG_HD void hg_log_dd(double x, double& Lh, double& Ll) {
 
 // exp(th + tl), |th| <= 85, correctly rounded except with probability ~2^-29.
 HG_HD double hg_exp_dd(double th, double tl) {
-  if (th > 85.0) return 8.0e36;
-  if (th < -85.0) return 1.2e-37;
+  if (hg_gt_pos(th, 0x4055400000000000ull)) return 8.0e36;   // th > 85
+  if (hg_lt_neg(th, 0xC055400000000000ull)) return 1.2e-37;  // th < -85
   const double kd = rint(th * HG_INV_L256);
   const int k = (int)kd;
   const double r0 = th - kd * HG_L256_1;  // exact (Sterbenz, 38-bit constant)

@@ -75,6 +75,7 @@ int main(int argc, char** argv) {
       expect(hg_lt_pos(x, cb), x < c);
       expect(hg_le_pos(x, cb), x <= c);
       expect(hg_gt_pos(x, cb), x > c);
+      expect(hg_lt_neg(x, hg_bits(-c)), x < -c);
     }
   }
   // pairs: every special value with every value, and random pairs

@@ -30,3 +30,17 @@ def test_integer_pipe_compares_match_ieee(tmp_path):
                            os.path.join(REPO, "tests", "native", "cmp_check.cpp"), "-o", exe])
     checks, bad = map(int, subprocess.check_output([exe, "100000"]).decode().split())
     assert checks > 1_000_000 and bad == 0
+
+
+def test_log_reduction_on_integer_pipes_is_bit_identical(tmp_path):
+    """hg_log_dd forms its reduction (exponent, sqrt(2) fold, table index
+    with round-half-even, F = 1 + j/1024) from the bit pattern; the outputs
+    equal those of the same function with the reduction in floating point,
+    bit for bit, on random, boundary and tie inputs.  hg_exp_dd's overflow
+    guards compare on the integer pipes too."""
+    exe = str(tmp_path / "logexp_check")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-builtin",
+                           "-I" + os.path.join(REPO, "hiten_gb300", "csrc"),
+                           os.path.join(REPO, "tests", "native", "logexp_check.cpp"), "-o", exe])
+    n_in, bad, n_exp, bad_exp = map(int, subprocess.check_output([exe, "400000"]).decode().split())
+    assert n_in > 1_000_000 and bad == 0 and n_exp == 15 and bad_exp == 0
