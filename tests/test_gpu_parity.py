@@ -192,6 +192,60 @@ def test_dop853_vs_reference_golden(gpu):
                 assert rowwise_rel(_np(r.y_end), S[-1:]) <= 1e-9
 
 
+def test_step_control_edges_match_oracle(gpu, shape, dev_oracle):
+    """The kernels' step control compares bit patterns (loop test, step
+    clamps, endpoint, acceptance, PI factor guards, event signs); on the
+    edges it must decide as the oracle's IEEE comparisons do: a start on the
+    first primary (0/0 in the right-hand side) and a NaN start (a NaN step,
+    every attempt rejected until max_steps), an active max_step clamp, an
+    active min_step clamp, a span at negative times and an empty span."""
+    y0 = W.section_states(14, seed=21)
+    y0[3] = [-MU, 0.0, 0.0, 0.0, 0.3, 0.0]
+    y0[7, 4] = np.nan
+    ev = gpu.EventSpec(index=1, offset=0.0, direction=0, max_hits=2)
+    cases = [(0.0, 1.5, 0.02, None), (0.0, 1.5, 1e4, 0.03), (-2.0, -0.5, 1e4, None), (0.7, 0.7, 1e4, None)]
+    for t0, tmax, max_step, min_step in cases:
+        res = gpu.propagate_dop853(y0, t0, tmax, MU, rtol=1e-11, atol=1e-11, max_step=max_step, min_step=min_step,
+                                   max_steps=300, event=ev)
+        ref = dev_oracle.dop853_event_batch(y0, t0, tmax, MU, 1, 0.0, 0, 2, rtol=1e-11, atol=1e-11,
+                                            max_step=max_step, min_step=min_step, max_steps=300)
+        case = (t0, tmax, max_step, min_step)
+        assert np.array_equal(_np(res.status), ref["status"]), case
+        assert np.array_equal(_np(res.n_accept), ref["n_accept"]), case
+        assert np.array_equal(_np(res.n_reject), ref["n_reject"]), case
+        assert np.array_equal(_np(res.t_end), ref["t_end"]), case
+        assert np.array_equal(_np(res.y_end), ref["y_end"], equal_nan=True), case
+        n_hits = _np(res.n_hits)
+        assert np.array_equal(n_hits, ref["n_hits"]), case
+        for i, k in enumerate(n_hits):
+            assert np.array_equal(_np(res.hit_t)[i, :k], ref["hit_t"][i, :k]), case
+            assert np.array_equal(_np(res.hit_y)[i, :k], ref["hit_y"][i, :k]), case
+    # the start states that never leave t0 keep their values and count every attempt as a rejection
+    assert int(_np(res.n_accept)[3]) == 0 and int(_np(res.n_accept)[7]) == 0
+
+
+@pytest.mark.parametrize("lanes42", [7, 14, 12, 18])
+def test_step_control_edges_42_match_oracle(gpu, dev_oracle, lanes42):
+    """The same edges on the 42-dim (state + STM) DOP853 kernels: the 7- and
+    14-lane groups, the paired and the three-warp layouts."""
+    x = W.stm_fixed_batch(1024, seed=0)[:9, 36:]
+    y0 = np.array([stm_state(v) for v in x])
+    y0[2, 36:] = [-MU, 0.0, 0.0, 0.0, 0.3, 0.0]
+    y0[5, 40] = np.nan
+    for t0, tmax, max_step, min_step in [(0.0, 1.2, 0.02, None), (0.0, 1.2, 1e4, 0.03), (0.9, 0.9, 1e4, None)]:
+        with gpu.tuning(lanes_d42=lanes42):
+            res = gpu.propagate_dop853(y0, t0, tmax, MU, rtol=1e-11, atol=1e-11, max_step=max_step,
+                                       min_step=min_step, max_steps=300, n_samples=2)
+        out = _np(res.samples)
+        for i in range(len(y0)):
+            ref, na, nr, st = dev_oracle.dop853_dense(y0[i], np.array([t0, tmax]), MU, rtol=1e-11, atol=1e-11,
+                                                      max_step=max_step, min_step=min_step, max_steps=300)
+            case = (t0, tmax, max_step, min_step, i)
+            assert np.array_equal(out[:, i], ref, equal_nan=True), case
+            assert int(_np(res.n_accept)[i]) == na and int(_np(res.n_reject)[i]) == nr, case
+            assert int(_np(res.status)[i]) == st, case
+
+
 def test_max_steps_status(gpu):
     y0 = W.section_states(5, seed=2)
     res = gpu.propagate_dop853(y0, 0.0, 20.0, MU, rtol=1e-11, atol=1e-11, max_steps=3)
