@@ -7,6 +7,7 @@ torch float64 CUDA tensors.  Device buffers are laid out structure-of-arrays
 Every call goes through ``libhitengpu.so``; there is no CPU path.
 """
 import ctypes as C
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -247,7 +248,8 @@ class Dop853Batch:
     queries, result views) is done once.  Results are the same bits as
     `propagate_dop853` with the same arguments; `run` returns one
     Dop853Result whose tensors are views of the batch's buffers, valid until
-    the next `run`.  Scalar t0 / tmax; no dense samples."""
+    the next `run`.  The outputs share one device arena, so `to_host()` reads
+    all of them back in a single copy.  Scalar t0 / tmax; no dense samples."""
 
     def __init__(self, n, dim, t0, tmax, mu, rtol=1e-12, atol=1e-12, max_step=1e4, min_step=None,
                  max_steps=100_000, fwd=1, flip=None, event=None, scheduled=None, device=None):
@@ -261,30 +263,35 @@ class Dop853Batch:
             raise ValueError("a prepared batch needs at least one state")
         self.scheduled = ((self.dim == 6 and self.n >= SCHEDULE_MIN) if scheduled is None else bool(scheduled))
         n, d, ld, dev = self.n, self.dim, self.n, self.dev
-        f64 = dict(dtype=torch.float64, device=dev)
-        i32 = dict(dtype=torch.int32, device=dev)
-        self.Y0 = torch.empty((d, ld), **f64)
+        self.Y0 = torch.empty((d, ld), dtype=torch.float64, device=dev)
         self.stage = None  # (N, dim) device copy of host inputs, made on the first host run
-        self.y_end = torch.empty((d, ld), **f64)
-        self.t_end = torch.empty(ld, **f64)
-        self.n_acc = torch.empty(ld, **i32)
-        self.n_rej = torch.empty(ld, **i32)
-        self.status = torch.empty(ld, **i32)
+        mh = int(event.max_hits) if event is not None else 0
+        # the outputs, carved from one arena: float64 parts first, then int32 (every part 8-byte aligned)
+        self.layout = [("y_end", torch.float64, (d, ld)), ("t_end", torch.float64, (ld,))]
+        if mh:
+            self.layout.append(("hits", torch.float64, (mh * ld * (1 + d),)))  # hit_t then hit_y, one fill per run
+        self.layout += [("n_acc", torch.int32, (ld,)), ("n_rej", torch.int32, (ld,)), ("status", torch.int32, (ld,))]
+        if mh:
+            self.layout.append(("n_hits", torch.int32, (ld,)))
+        nbytes = sum(((math.prod(shape) * (8 if dt == torch.float64 else 4) + 7) // 8) * 8 for _, dt, shape in self.layout)
+        self.out = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        self.out_host = None  # pinned mirror of the arena, made on the first to_host()
+        v = self._carve(self.out)
+        self.y_end, self.t_end, self.n_acc, self.n_rej, self.status = (v["y_end"], v["t_end"], v["n_acc"],
+                                                                        v["n_rej"], v["status"])
         lo, hi = _flip(d, fwd, flip)
         self.opts = _lib.hg_dop853_opts(float(rtol), float(atol), float(max_step),
                                         float(10.0 * EPS if min_step is None else min_step), int(max_steps),
                                         int(fwd), lo, hi)
         self.evp = None
         self.hits = None
-        mh = 0
         if event is not None:
-            mh = int(event.max_hits)
             self.evp = _lib.hg_event(int(event.index), float(event.offset), int(event.direction), mh,
                                      float(event.xtol), float(event.gtol))
-            self.hits = torch.empty(mh * ld * (1 + d), **f64)  # hit_t then hit_y, one fill per run
+            self.hits = v["hits"]
             hit_t = self.hits[:mh * ld].view(mh, ld)
             hit_y = self.hits[mh * ld:].view(mh, d, ld)
-            self.n_hits = torch.empty(ld, **i32)
+            self.n_hits = v["n_hits"]
         self.H = _lib.handle(dev.index or 0)
         self.ws_bytes = int(self.H.lib.hg_dop853_segmented_workspace_bytes(n, d, mh)) if self.scheduled else 0
         self.ws = torch.empty(max(self.ws_bytes, 1), dtype=torch.uint8, device=dev) if self.scheduled else None
@@ -293,12 +300,41 @@ class Dop853Batch:
                      _ptr(self.y_end), _ptr(self.t_end), _ptr(hit_t) if mh else None,
                      _ptr(hit_y) if mh else None, _ptr(self.n_hits) if mh else None, _ptr(self.n_acc),
                      _ptr(self.n_rej), _ptr(self.status))
-        self.result = Dop853Result(y_end=self.y_end.t(), t_end=self.t_end, n_accept=self.n_acc,
-                                   n_reject=self.n_rej, status=self.status)
-        if mh:
-            self.result.hit_t = hit_t.t()
-            self.result.hit_y = hit_y.permute(2, 0, 1)
-            self.result.n_hits = self.n_hits
+        self.mh = mh
+        self.result = self._result(v)
+        self.result_host = None
+
+    def _carve(self, buf):
+        """The named output parts as views of the byte buffer `buf` (the
+        device arena or its pinned host mirror)."""
+        views, off = {}, 0
+        for name, dt, shape in self.layout:
+            size = math.prod(shape) * (8 if dt == torch.float64 else 4)
+            views[name] = buf[off:off + size].view(dt).view(shape)
+            off += ((size + 7) // 8) * 8
+        return views
+
+    def _result(self, v):
+        n, d = self.n, self.dim
+        r = Dop853Result(y_end=v["y_end"].t(), t_end=v["t_end"], n_accept=v["n_acc"], n_reject=v["n_rej"],
+                         status=v["status"])
+        if self.mh:
+            r.hit_t = v["hits"][:self.mh * n].view(self.mh, n).t()
+            r.hit_y = v["hits"][self.mh * n:].view(self.mh, d, n).permute(2, 0, 1)
+            r.n_hits = v["n_hits"]
+        return r
+
+    def to_host(self):
+        """The last run's results on the host: one device-to-host copy of the
+        output arena into pinned memory (allocated on the first call), after
+        the run on the current stream.  Returns a Dop853Result of CPU tensors
+        that view that memory, valid until the next `to_host`."""
+        if self.out_host is None:
+            self.out_host = torch.empty(self.out.numel(), dtype=torch.uint8, pin_memory=True)
+            self.result_host = self._result(self._carve(self.out_host))
+        self.out_host.copy_(self.out, non_blocking=True)
+        torch.cuda.current_stream(self.dev).synchronize()
+        return self.result_host
 
     def run(self, y0):
         """Propagate the (N, dim) states `y0` (a CUDA tensor on the batch's

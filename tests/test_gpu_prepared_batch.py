@@ -41,3 +41,17 @@ def test_prepared_batch_from_pinned_host_states(gpu):
     host = b.run(torch.as_tensor(y).pin_memory())
     for f, v in d.items():
         assert torch.equal(getattr(host, f), v), f
+
+
+def test_prepared_batch_to_host_reads_every_output(gpu):
+    """to_host() reads the whole output arena back in one copy: every field
+    on the host equals the device result's, run after run."""
+    ev = gpu.EventSpec(index=1, offset=0.0, direction=-1, max_hits=3)
+    b = gpu.Dop853Batch(700, 6, 0.0, 4.0, MU, rtol=1e-11, atol=1e-11, event=ev)
+    for seed in (5, 6):
+        r = b.run(torch.as_tensor(W.section_states(700, seed=seed)).pin_memory())
+        h = b.to_host()
+        for f in ("y_end", "t_end", "n_accept", "n_reject", "status", "n_hits", "hit_t", "hit_y"):
+            dv, hv = getattr(r, f), getattr(h, f)
+            assert hv.device.type == "cpu" and hv.shape == dv.shape, (seed, f)
+            assert np.array_equal(hv.numpy(), dv.cpu().numpy(), equal_nan=True), (seed, f)
