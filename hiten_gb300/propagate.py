@@ -266,14 +266,9 @@ class Dop853Batch:
         self.Y0 = torch.empty((d, ld), dtype=torch.float64, device=dev)
         self.stage = None  # (N, dim) device copy of host inputs, made on the first host run
         mh = int(event.max_hits) if event is not None else 0
-        # the outputs, carved from one arena: float64 parts first, then int32 (every part 8-byte aligned)
-        self.layout = [("y_end", torch.float64, (d, ld)), ("t_end", torch.float64, (ld,))]
-        if mh:
-            self.layout.append(("hits", torch.float64, (mh * ld * (1 + d),)))  # hit_t then hit_y, one fill per run
-        self.layout += [("n_acc", torch.int32, (ld,)), ("n_rej", torch.int32, (ld,)), ("status", torch.int32, (ld,))]
-        if mh:
-            self.layout.append(("n_hits", torch.int32, (ld,)))
-        nbytes = sum(((math.prod(shape) * (8 if dt == torch.float64 else 4) + 7) // 8) * 8 for _, dt, shape in self.layout)
+        # the outputs, carved from one arena
+        self.layout = self.arena_layout(d, ld, mh)
+        nbytes = sum(self.part_bytes(dt, shape) for _, dt, shape in self.layout)
         self.out = torch.empty(nbytes, dtype=torch.uint8, device=dev)
         self.out_host = None  # pinned mirror of the arena, made on the first to_host()
         v = self._carve(self.out)
@@ -304,6 +299,25 @@ class Dop853Batch:
         self.result = self._result(v)
         self.result_host = None
 
+    @staticmethod
+    def arena_layout(dim, n, max_hits):
+        """(name, dtype, shape) of the output parts in arena order: float64
+        parts first, then int32; the hits part holds hit_t then hit_y (one
+        NaN fill per run)."""
+        lay = [("y_end", torch.float64, (dim, n)), ("t_end", torch.float64, (n,))]
+        if max_hits:
+            lay.append(("hits", torch.float64, (max_hits * n * (1 + dim),)))
+        lay += [("n_acc", torch.int32, (n,)), ("n_rej", torch.int32, (n,)), ("status", torch.int32, (n,))]
+        if max_hits:
+            lay.append(("n_hits", torch.int32, (n,)))
+        return lay
+
+    @staticmethod
+    def part_bytes(dtype, shape):
+        """Bytes a part takes in the arena: its size rounded up to 8, so that
+        every part starts 8-byte aligned."""
+        return ((math.prod(shape) * (8 if dtype == torch.float64 else 4) + 7) // 8) * 8
+
     def _carve(self, buf):
         """The named output parts as views of the byte buffer `buf` (the
         device arena or its pinned host mirror)."""
@@ -311,7 +325,7 @@ class Dop853Batch:
         for name, dt, shape in self.layout:
             size = math.prod(shape) * (8 if dt == torch.float64 else 4)
             views[name] = buf[off:off + size].view(dt).view(shape)
-            off += ((size + 7) // 8) * 8
+            off += self.part_bytes(dt, shape)
         return views
 
     def _result(self, v):
