@@ -17,8 +17,10 @@ Metric: accepted trajectory-steps per second (attempted steps reported
 beside it).  `value`: throughput with the seeds resident in HBM, each step
 one run of the call prepared once (propagate.Dop853Batch: static input,
 output and workspace buffers; checked bit-identical to propagate_dop853);
-`e2e`: the same prepared call from pinned host seeds, H2D and D2H copies
-inside the timed region (wall clock); `e2e.dropin` the same through the
+`e2e`: the same prepared call from pinned host seeds, the H2D copy of the
+seeds and the D2H copy of every output (the batch's output arena, one copy:
+Dop853Batch.to_host) inside the timed region (wall clock); `e2e.dropin` the
+same through the
 reference-shaped public API (hiten_gb300.manifold.propagate_to_plane, a full
 per-call setup).  `gpu_launches`:
 kernels launched in the timed region, read from the library's counter.
@@ -873,8 +875,8 @@ def main():
     host_seeds = torch.as_tensor(seeds).pin_memory()
     h2d = host_seeds.numel() * 8
 
-    # the results are read back into pinned host buffers allocated once (no host allocation or page
-    # faults inside the timed steps); one synchronisation per step
+    # the drop-in's results (separate tensors) are read back into pinned host buffers allocated once
+    # (no host allocation or page faults inside the timed steps); one synchronisation per step
     out_host = {}
 
     def fetch(r):
